@@ -1,0 +1,278 @@
+"""Generate the golden fixtures in tests/golden/ from the reference implementation itself.
+
+Run in a container that has the reference sources (default /root/reference) after
+`python oracle/build_ref.py`:
+
+    python tests/golden/make_golden.py
+
+It loads the reference's own pybind11 module `_crt` (oracle/_ref/golden/, built from
+src/pybind.cpp unmodified) and oracle/_ref/golden/libref_driver.so (oracle/ref_driver.cpp over
+the reference headers), runs them on small seeded scenes written as OBJ files, and stores the
+scene inputs together with the reference outputs:
+
+  cornell.npz   Cornell box (36 triangles, 6 entities): BodyFixedGroup intersection / instance /
+                normal passes at 128x128, the dynamic-scene passes (rendering_dynamic path), and
+                the path tracer's float radiance (mean and Welford M2) at 48x48, 512 spp, 3 bounces,
+                and a deterministic 1-spp, 1-bounce point-light render.
+  asteroid.npz  8000-triangle asteroid (smooth, rotated, scaled, translated) plus a flat box:
+                BodyFixedGroup passes at 64x64, per-ray closest hits (primitive, t, u, v) and
+                any-hit flags for seeded rays, and batch_simulate_lidar ranges for 512 poses.
+
+Nothing at test time reads the reference: the tests only read these .npz files.
+"""
+import ctypes
+import importlib.util
+import os
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(REPO, "ceres-raytracer_gb300"))
+from crt_gb300 import scenes  # noqa: E402
+
+REF_DIR = os.path.join(REPO, "oracle", "_ref", "golden")
+
+
+def load_ref_module():
+    import sysconfig
+    path = os.path.join(REF_DIR, "_crt" + sysconfig.get_config_var("EXT_SUFFIX"))
+    spec = importlib.util.spec_from_file_location("_crt", path)
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def load_driver():
+    d = ctypes.CDLL(os.path.join(REF_DIR, "libref_driver.so"))
+    vp = ctypes.c_void_p
+    d.ref_scene_create.argtypes = [ctypes.c_int, vp, vp, vp, vp, vp, vp]
+    d.ref_scene_create.restype = vp
+    d.ref_num_tris.argtypes = [vp]
+    d.ref_num_tris.restype = ctypes.c_size_t
+    d.ref_tris.argtypes = [vp, vp]
+    d.ref_trace_closest.argtypes = [vp, vp, ctypes.c_size_t, vp, vp, vp, vp]
+    d.ref_trace_any.argtypes = [vp, vp, ctypes.c_size_t, vp]
+    d.ref_render.argtypes = [vp, ctypes.c_double, vp, vp, ctypes.c_int, vp, vp, ctypes.c_int, vp, ctypes.c_int,
+                             ctypes.c_int, ctypes.c_double, ctypes.c_int, vp, vp]
+    return d
+
+
+def entity_arrays(ents, prefix="e"):
+    """Flatten entity specs into npz-storable arrays."""
+    out = {f"{prefix}_count": np.array(len(ents))}
+    for i, e in enumerate(ents):
+        out[f"{prefix}{i}_v"] = e.mesh.vertices
+        out[f"{prefix}{i}_f"] = e.mesh.faces
+        out[f"{prefix}{i}_color"] = np.array(e.color, dtype=np.float64)
+        out[f"{prefix}{i}_smooth"] = np.array(int(e.smooth))
+        out[f"{prefix}{i}_scale"] = np.array(float(e.scale))
+        out[f"{prefix}{i}_pos"] = np.asarray(e.position, dtype=np.float64)
+        out[f"{prefix}{i}_rot"] = np.asarray(e.rotation, dtype=np.float64)
+    return out
+
+
+def camera_arrays(cam, prefix="cam"):
+    return {f"{prefix}_focal": np.array(cam["focal_length"], dtype=np.float64),
+            f"{prefix}_res": np.array(cam["resolution"], dtype=np.float64),
+            f"{prefix}_sensor": np.array(cam["sensor_size"], dtype=np.float64),
+            f"{prefix}_zpos": np.array(int(cam["z_positive"])),
+            f"{prefix}_pos": np.asarray(cam["position"], dtype=np.float64),
+            f"{prefix}_rot": np.asarray(cam["rotation"], dtype=np.float64)}
+
+
+def write_objs(ents, tmp):
+    paths = []
+    for i, e in enumerate(ents):
+        p = os.path.join(tmp, f"{i}_{e.name}.obj")
+        e.mesh.write_obj(p)
+        paths.append(p)
+    return paths
+
+
+def ref_camera(R, cam):
+    c = R.SimpleCamera(float(cam["focal_length"]), list(map(float, cam["resolution"])),
+                       list(map(float, cam["sensor_size"])), bool(cam["z_positive"]))
+    c.set_pose(np.asarray(cam["position"], dtype=np.float64), np.ascontiguousarray(cam["rotation"], dtype=np.float64))
+    return c
+
+
+def body_fixed_group(R, ents, paths):
+    bfes = []
+    for e, p in zip(ents, paths):
+        b = R.BodyFixedEntity(p, "obj", bool(e.smooth), [float(x) for x in e.color])
+        b.set_scale(float(e.scale))
+        b.set_pose(np.asarray(e.position, dtype=np.float64), np.ascontiguousarray(e.rotation, dtype=np.float64))
+        bfes.append(b)
+    return R.BodyFixedGroup(bfes)
+
+
+def dynamic_entities(R, ents, paths):
+    out = []
+    for e, p in zip(ents, paths):
+        x = R.Entity(p, "obj", bool(e.smooth), [float(x) for x in e.color])
+        x.set_scale(float(e.scale))
+        x.set_pose(np.asarray(e.position, dtype=np.float64), np.ascontiguousarray(e.rotation, dtype=np.float64))
+        out.append(x)
+    return out
+
+
+def driver_scene(D, ents, paths):
+    n = len(ents)
+    cpaths = (ctypes.c_char_p * n)(*[p.encode() for p in paths])
+    smooth = np.array([int(e.smooth) for e in ents], dtype=np.int32)
+    colors = np.array([e.color for e in ents], dtype=np.float64)
+    scales = np.array([e.scale for e in ents], dtype=np.float64)
+    pos = np.array([e.position for e in ents], dtype=np.float64)
+    rot = np.array([np.asarray(e.rotation).ravel() for e in ents], dtype=np.float64)
+    return D.ref_scene_create(n, cpaths, smooth.ctypes.data, colors.ctypes.data, scales.ctypes.data, pos.ctypes.data,
+                              rot.ctypes.data)
+
+
+def driver_closest(D, h, rays):
+    n = rays.shape[0]
+    prim = np.empty(n, np.int64)
+    t, u, v = np.empty(n), np.empty(n), np.empty(n)
+    D.ref_trace_closest(h, rays.ctypes.data, n, prim.ctypes.data, t.ctypes.data, u.ctypes.data, v.ctypes.data)
+    return prim, t, u, v
+
+
+def driver_any(D, h, rays):
+    occ = np.empty(rays.shape[0], np.uint8)
+    D.ref_trace_any(h, rays.ctypes.data, rays.shape[0], occ.ctypes.data)
+    return occ
+
+
+def light_array(lights):
+    arr = np.zeros((len(lights), 16))
+    for i, l in enumerate(lights):
+        arr[i, 0] = 1.0 if l["type"] == "area" else 0.0
+        arr[i, 1] = l["intensity"]
+        arr[i, 2:5] = l["position"]
+        arr[i, 5:14] = np.asarray(l.get("rotation", np.eye(3))).ravel()
+        arr[i, 14:16] = l.get("size", [0.0, 0.0])
+    return arr
+
+
+def make_cornell(R, D, tmp):
+    ents, cam, lights = scenes.cornell()
+    paths = write_objs(ents, tmp)
+    out = entity_arrays(ents)
+    cam = dict(cam, resolution=[128, 128])
+    out.update(camera_arrays(cam))
+    g = body_fixed_group(R, ents, paths)
+    c = ref_camera(R, cam)
+    out["bf_xyz"] = g.intersection_pass(c)
+    out["bf_ids"] = g.instance_pass(c)
+    out["bf_normals"] = g.normal_pass(c)
+    dyn = dynamic_entities(R, ents, paths)
+    out["dyn_ids"] = R.instance_pass(c, dyn)
+    out["dyn_normals"] = R.normal_pass(c, dyn)
+    out["dyn_xyz"] = R.intersection_pass(c, dyn)
+    # path tracer radiance (reference RNG under the determinism shim)
+    rcam = dict(cam, resolution=[48, 48])
+    out.update(camera_arrays(rcam, "rcam"))
+    h = driver_scene(D, ents, paths)
+    W = H = 48
+    spp, bounces = 512, 3
+    L = light_array(lights)
+    rad = np.empty((H, W, 3), np.float32)
+    m2 = np.empty((H, W, 3), np.float32)
+    # keep every argument array alive for the duration of the call
+    res_a = np.array(rcam["resolution"], dtype=np.float64)
+    sen_a = np.array(rcam["sensor_size"], dtype=np.float64)
+    pos_a = np.asarray(rcam["position"], dtype=np.float64)
+    rot_a = np.ascontiguousarray(rcam["rotation"], dtype=np.float64)
+    D.ref_render(h, float(rcam["focal_length"]), res_a.ctypes.data, sen_a.ctypes.data, int(rcam["z_positive"]),
+                 pos_a.ctypes.data, rot_a.ctypes.data, len(lights), L.ctypes.data, spp, spp, 0.0, bounces,
+                 rad.ctypes.data, m2.ctypes.data)
+    out["render_mean"] = rad
+    out["render_m2"] = m2
+    out["render_spp"] = np.array(spp)
+    out["render_bounces"] = np.array(bounces)
+    out["lights"] = L
+    # deterministic render: point light, 1 sample at the pixel corner, 1 bounce (no random draws)
+    point = [dict(type="point", intensity=0.5, position=np.array([0.5, 0.8, 0.5]))]
+    Lp = light_array(point)
+    radp = np.empty((H, W, 3), np.float32)
+    D.ref_render(h, float(rcam["focal_length"]), res_a.ctypes.data, sen_a.ctypes.data, int(rcam["z_positive"]),
+                 pos_a.ctypes.data, rot_a.ctypes.data, 1, Lp.ctypes.data, 1, 1, 0.0, 1, radp.ctypes.data, None)
+    out["point_lights"] = Lp
+    out["point_radiance"] = radp
+    return out
+
+
+def make_asteroid(R, D, tmp):
+    ast = scenes.asteroid(8000, seed=7)
+    c, s = 0.8, 0.6
+    rot = np.array([[c, -s, 0.0], [s, c, 0.0], [0.0, 0.0, 1.0]]) @ np.array([[1.0, 0.0, 0.0], [0.0, c, -s], [0.0, s, c]])
+    ents = [scenes.EntitySpec("asteroid", ast, (0.1, 0.1, 0.1), smooth=True, scale=1.25,
+                              position=np.array([10.0, -20.0, 5.0]), rotation=rot),
+            scenes.EntitySpec("box", scenes.box_mesh((0.0, 0.0, 0.0), (300.0, 200.0, 100.0), 1.0, 0.0), (0.5, 0.5, 0.5),
+                              position=np.array([1500.0, 200.0, 0.0]))]
+    paths = write_objs(ents, tmp)
+    out = entity_arrays(ents)
+    cam = scenes.fov_camera(0.3, (64, 64), (6000.0, 1000.0, 2500.0), (200.0, 0.0, 0.0))
+    out.update(camera_arrays(cam))
+    g = body_fixed_group(R, ents, paths)
+    rc = ref_camera(R, cam)
+    out["bf_xyz"] = g.intersection_pass(rc)
+    out["bf_ids"] = g.instance_pass(rc)
+    out["bf_normals"] = g.normal_pass(rc)
+    # seeded rays: origins on a 4 km shell aimed near the body, plus short/inside rays
+    rng = np.random.Generator(np.random.PCG64(2024))
+    n = 3072
+    o = rng.normal(size=(n, 3))
+    o = 4000.0 * o / np.linalg.norm(o, axis=1)[:, None]
+    tgt = rng.uniform(-1400.0, 1400.0, size=(n, 3))
+    d = tgt - o
+    d /= np.linalg.norm(d, axis=1)[:, None]
+    rays = np.zeros((n, 8))
+    rays[:, 0:3], rays[:, 3:6], rays[:, 6], rays[:, 7] = o, d, 0.0, np.finfo(np.float64).max
+    # a quarter of the rays get a finite tmax (shadow-style queries)
+    q = n // 4
+    rays[:q, 7] = rng.uniform(1000.0, 5000.0, size=q)
+    out["rays"] = rays
+    h = driver_scene(D, ents, paths)
+    out["ref_tris"] = np.empty(0)
+    ntri = D.ref_num_tris(h)
+    tri = np.empty((ntri, 21))
+    D.ref_tris(h, tri.ctypes.data)
+    out["ref_tris"] = tri
+    out["closest_prim"], out["closest_t"], out["closest_u"], out["closest_v"] = driver_closest(D, h, rays)
+    out["any_occluded"] = driver_any(D, h, rays)
+    # batch lidar through the reference module (lidars/simple_lidar.hpp, do_lidar.hpp:80-155)
+    npose = 512
+    pp = rng.normal(size=(npose, 3))
+    pp = 3000.0 * pp / np.linalg.norm(pp, axis=1)[:, None]
+    rots = np.zeros((3, 3, 100000))
+    rlist = []
+    for k in range(npose):
+        aim = rng.uniform(-900.0, 900.0, size=3)
+        Rk = scenes.look_at(pp[k], aim, up=(0.0, 0.0, 1.0) if abs(pp[k][2]) < 2900 else (1.0, 0.0, 0.0))
+        rots[:, :, k] = Rk
+        rlist.append(Rk)
+    lid = R.SimpleLidar(False)
+    lid.batch_set_pose(np.ascontiguousarray(pp), rots, npose)
+    out["lidar_pos"] = pp
+    out["lidar_rot"] = np.array(rlist)
+    out["lidar_range"] = g.batch_simulate_lidar(lid, 1.0)[0]
+    return out
+
+
+def main():
+    R = load_ref_module()
+    D = load_driver()
+    with tempfile.TemporaryDirectory() as tmp:
+        c = make_cornell(R, D, tmp)
+        np.savez_compressed(os.path.join(HERE, "cornell.npz"), **c)
+        a = make_asteroid(R, D, tmp)
+        np.savez_compressed(os.path.join(HERE, "asteroid.npz"), **a)
+    for f in ("cornell.npz", "asteroid.npz"):
+        print(f, os.path.getsize(os.path.join(HERE, f)))
+
+
+if __name__ == "__main__":
+    main()
