@@ -1,0 +1,419 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 ray-query path on the procedural-asteroid workload.
+
+One step = one render request (2048^2, 1 spp: primary + sun shadow ray) and one LiDAR scan
+(1024^2 beams, range + triangle id) on the device-resident BVH of the 2M-triangle asteroid.
+`value` is Mrays/s (primary + shadow + LiDAR rays) with inputs resident on the device and
+outputs left in device memory, timed with CUDA events on the library's stream, an L2 flush
+(256 MiB write) between steps outside the timed events.  `e2e` is the same workload through the
+public `crt` API (BodyFixedGroup.render / lidar_scan) returning numpy arrays.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+--impl reference times the CPU oracle (FP64 C restatement of the reference path, all host cores).
+Multi-GPU (torchrun): every rank runs the same workload on its own GPU (replicas; weak scaling).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(REPO, "ceres-raytracer_gb300")
+for _p in (PKG, REPO):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "Mrays/s and p50/p99 request latency, batched/served vs per-call GPU, one GB300"
+UNIT = "Mrays/s"
+NODE_BYTES, TRI_BYTES, RAY_BYTES, HIT_BYTES = 80, 48, 32, 16
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--faces", type=int, default=2_000_000)
+    ap.add_argument("--res", type=int, default=2048)
+    ap.add_argument("--lidar", type=int, default=1024)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def dist_info():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def percentile(xs, q):
+    xs = sorted(xs)
+    if not xs:
+        return None
+    k = (len(xs) - 1) * q / 100.0
+    lo, hi = int(np.floor(k)), int(np.ceil(k))
+    return xs[lo] + (xs[hi] - xs[lo]) * (k - lo)
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+    FIELDS = "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown," \
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown," \
+             "clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200", "-f", self.path],
+                                         stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def measured_peak():
+    path = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic():
+    """dram bytes per launch of the primary trace kernel, from the committed ncu summary."""
+    path = os.path.join(REPO, "profiles", "trace_closest_asteroid2M.md")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.strip().startswith("dram_bytes_per_launch_full"):
+            try:
+                return float(line.split("=")[1].split()[0])
+            except (IndexError, ValueError):
+                return None
+    return None
+
+
+def lidar_rays64(lid):
+    """FP64 beam rays of a LiDAR grid (same construction as crt_lidar_grid)."""
+    nx, ny = lid["nx"], lid["ny"]
+    tx = np.tan(-lid["half_x"] + (np.arange(nx) + 0.5) * 2 * lid["half_x"] / nx)
+    ty = np.tan(-lid["half_y"] + (np.arange(ny) + 0.5) * 2 * lid["half_y"] / ny)
+    s = np.stack(np.broadcast_arrays(tx[None, :], ty[:, None], -np.ones((ny, nx))), -1).reshape(-1, 3)
+    s /= np.linalg.norm(s, axis=1)[:, None]
+    d = s @ np.asarray(lid["rotation"])
+    rays = np.zeros((nx * ny, 8))
+    rays[:, 0:3] = lid["position"]
+    rays[:, 3:6] = d
+    rays[:, 7] = np.finfo(np.float64).max
+    return rays
+
+
+# ------------------------------------------------------------------ CPU (oracle port) timing
+def cpu_measure(ents, cfg, budget_s):
+    """Time the CPU oracle on the step's workload with all host threads; returns (Mrays/s, detail)."""
+    import oracle
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    o = oracle.Scene(ents, nthreads=threads)
+    build_s = time.perf_counter() - t0
+    cam, lights = cfg["camera"], cfg["lights"]
+    W, H = int(cam["resolution"][0]), int(cam["resolution"][1])
+    lid_rays = lidar_rays64(cfg["lidar"])
+    # probe: 16 rows of the image + 1/64 of the beams, then scale the sample to ~budget_s
+    rows = 16
+    t = time.perf_counter()
+    o.render(cam, lights, 1, 1, 1.0, cfg["bounces"], row0=0, row1=rows)
+    o.trace_closest(lid_rays[: len(lid_rays) // 64])
+    probe = time.perf_counter() - t
+    frac = min(1.0, max(rows / H, (budget_s / max(probe, 1e-3)) * rows / H))
+    rows = max(16, min(H, int(H * frac)))
+    nl = max(1024, int(len(lid_rays) * rows / H))
+    _, ids, _, _ = o.passes(cam, 0, rows)
+    shadow = int((ids > 0).sum()) * len(lights)
+    reps, el = 0, 0.0
+    while reps == 0 or (el < 0.5 * budget_s and reps < 8):
+        t = time.perf_counter()
+        o.render(cam, lights, 1, 1, 1.0, cfg["bounces"], row0=0, row1=rows)
+        o.trace_closest(lid_rays[:nl])
+        el += time.perf_counter() - t
+        reps += 1
+    rays = (rows * W + shadow + nl) * reps
+    return rays / el / 1e6, dict(cores=threads, seconds=el, rays=rays, build_s=build_s,
+                                 sample=f"{reps} x (rows 0..{rows} of the {W}x{H} render, primary + shadow, and {nl} "
+                                        f"of {len(lid_rays)} LiDAR beams); BVH built once (untimed)")
+
+
+# ------------------------------------------------------------------ reference arm
+def reference_arm(args):
+    rank, world, _ = dist_info()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo", init_method="env://")
+        if rank != 0:
+            dist.barrier()
+            return
+    from crt_gb300 import build, workloads
+    build.build()
+    ents = workloads.asteroid_entities(args.faces)
+    cfg = workloads.asteroid_config(args.res, args.lidar)
+    # one bounded sample (about --cpu-seconds of work) of the step's workload; the BVH build is not timed
+    mr, det = cpu_measure(ents, cfg, args.cpu_seconds)
+    line = {"impl": "reference", "metric": METRIC, "value": round(mr, 3), "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "asteroid-2M render 2048^2 1spp + sun shadow, LiDAR 1024^2", "triangles": args.faces},
+            "cpu_baseline": {"value": round(mr, 3), "unit": UNIT, "cores": det["cores"], "kind": "port",
+                             "sample": det["sample"]},
+            "e2e": {"value": round(mr, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    rays_step = args.res * args.res * 2 + args.lidar * args.lidar
+    line["ms_per_step"] = round(rays_step / (mr * 1e6) * 1e3, 3)
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+# ------------------------------------------------------------------ GPU arm
+def gpu_arm(args):
+    import torch
+    from crt_gb300 import build, lib, scenes, workloads
+    build.build()
+    rank, world, local = dist_info()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", init_method="env://", device_id=torch.device("cuda", local))
+
+    ents = workloads.asteroid_entities(args.faces)
+    cfg = workloads.asteroid_config(args.res, args.lidar)
+    cam, lights, lid = cfg["camera"], cfg["lights"], cfg["lidar"]
+    ctx = lib.Context(local)
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+    sc = ctx.scene(ents)
+    st = sc.stats()
+    W = H = args.res
+    dev = torch.device("cuda", local)
+    rgba = torch.empty((H, W, 4), dtype=torch.uint8, device=dev)
+    rng_out = torch.empty((lid["ny"], lid["nx"]), dtype=torch.float64, device=dev)
+    prim_out = torch.empty((lid["ny"], lid["nx"]), dtype=torch.int32, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    def render():
+        sc.render(cam, lights, 1, 1, 1.0, cfg["bounces"], want_radiance=False, out_rgba=rgba)
+
+    def scan():
+        sc.lidar_grid(lid["position"], lid["rotation"], lid["nx"], lid["ny"], lid["half_x"], lid["half_y"],
+                      out_range=rng_out, out_prim=prim_out)
+
+    # rays per step: primary + shadow (one per primary hit, one light) + LiDAR beams
+    with torch.cuda.stream(stream):
+        ctx.reset_counters()
+        ctx.set_counting(True)
+        render()
+        c_render = ctx.counters()
+        ctx.reset_counters()
+        scan()
+        c_scan = ctx.counters()
+        ctx.set_counting(False)
+        ctx.synchronize()
+    rays_step = int(c_render["rays"] + c_scan["rays"])
+
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True),
+           torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            flush.zero_()
+            render()
+            scan()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    ctx.reset_counters()
+    torch.cuda.synchronize()
+    t_wall = time.perf_counter()
+    with torch.cuda.stream(stream):
+        for k in range(args.steps):
+            flush.zero_()
+            a, b, c = ev[k]
+            a.record(stream)
+            render()
+            b.record(stream)
+            scan()
+            c.record(stream)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t_wall
+    launches = ctx.counters()["launches"]
+    if world > 1:
+        torch.distributed.barrier()
+    clk = clocks.stop()
+    lat_render = [a.elapsed_time(b) for a, b, c in ev]
+    lat_lidar = [b.elapsed_time(c) for a, b, c in ev]
+    step_ms = [a.elapsed_time(c) for a, b, c in ev]
+    ms = float(np.mean(step_ms))
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = rays_step * world / (ms / 1e3) / 1e6
+
+    # ---- roofline of the dominant kernel: closest-hit traversal of the primary camera rays
+    rays64 = scenes_camera_rays(cam)
+    rays_dev = torch.from_numpy(rays64).to(dev)
+    hits_dev = torch.empty((rays64.shape[0], 4), dtype=torch.float32, device=dev)
+    with torch.cuda.stream(stream):
+        ctx.reset_counters()
+        ctx.set_counting(True)
+        sc.trace_closest(rays_dev, out=hits_dev)
+        cnt = ctx.counters()
+        ctx.set_counting(False)
+        times = []
+        for _ in range(max(5, min(20, args.steps))):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            sc.trace_closest(rays_dev, out=hits_dev)
+            b.record(stream)
+            times.append((a, b))
+    torch.cuda.synchronize()
+    t_kernel = float(np.mean([a.elapsed_time(b) for a, b in times])) / 1e3
+    nodes_ray = cnt["nodes"] / cnt["rays"]
+    tris_ray = cnt["tris"] / cnt["rays"]
+    b_ray = NODE_BYTES * nodes_ray + TRI_BYTES * tris_ray + RAY_BYTES + HIT_BYTES
+    achieved = b_ray * cnt["rays"] / t_kernel / 1e9
+    peak, peak_kind = measured_peak()
+    traffic = profiled_traffic()
+    roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 4), "traffic": traffic, "peak_source": peak_kind,
+            "kernel": "k_trace<closest> on 2048^2 primary camera rays (crt_trace_closest)",
+            "bytes_per_ray": round(b_ray, 1), "nodes_per_ray": round(nodes_ray, 2), "tris_per_ray": round(tris_ray, 2),
+            "kernel_ms": round(t_kernel * 1e3, 3), "kernel_mrays_s": round(cnt["rays"] / t_kernel / 1e6, 1)}
+
+    # ---- end to end through the public crt API (host numpy outputs)
+    e2e = None
+    if not args.no_e2e and rank == 0:
+        e2e = e2e_measure(args, ents, cfg, rays_step)
+
+    line = None
+    if rank == 0:
+        line = {"metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": {"workload": "asteroid-2M: render 2048^2 1 spp (primary + sun shadow) + LiDAR 1024^2 "
+                                       "(range + triangle id), per-call GPU path, resident BVH",
+                           "triangles": st["n_tris"], "wide_nodes": st["n_nodes"], "bvh_depth": st["depth"],
+                           "bvh_build_ms": round(st["build_ms"], 2), "rays_per_step": rays_step,
+                           "l2": "256 MiB buffer written between steps (outside the timed events)",
+                           "wall_s": round(wall, 3)},
+                "latency_ms": {"render_p50": round(percentile(lat_render, 50), 3),
+                               "render_p99": round(percentile(lat_render, 99), 3),
+                               "lidar_p50": round(percentile(lat_lidar, 50), 3),
+                               "lidar_p99": round(percentile(lat_lidar, 99), 3)},
+                "roofline": roof, "gpu_launches": int(launches), "clocks": clk, "e2e": e2e}
+        if world == 1 and not args.no_cpu:
+            mr, det = cpu_measure(ents, cfg, args.cpu_seconds)
+            line["cpu_baseline"] = {"value": round(mr, 3), "unit": UNIT, "cores": det["cores"], "kind": "port",
+                                    "sample": det["sample"]}
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.barrier()
+        torch.distributed.destroy_process_group()
+    ctx.close()
+
+
+def scenes_camera_rays(cam):
+    """FP32 camera rays (as an [n, 8] float32 array) for the roofline probe."""
+    import oracle
+    r = oracle.camera_rays(cam).astype(np.float32)
+    r[:, 7] = np.finfo(np.float32).max
+    return np.ascontiguousarray(r)
+
+
+def e2e_measure(args, ents, cfg, rays_step):
+    import crt
+    from crt.body_fixed import BodyFixedEntity, BodyFixedGroup
+    from crt.cameras import SimpleCamera
+    from crt.lidars import SimpleLidar
+    from crt.lights import PointLight
+    from crt_gb300 import scenes
+    cache = os.environ.get("CRT_SCENE_CACHE", "/tmp/crt_scene_cache")
+    os.makedirs(cache, exist_ok=True)
+    path = os.path.join(cache, f"asteroid_{args.faces}.obj")
+    if not os.path.exists(path):
+        scenes.write_obj_fast(ents[0].mesh, path + ".tmp")
+        os.replace(path + ".tmp", path)
+    group = BodyFixedGroup([BodyFixedEntity(path, color=[0.1, 0.1, 0.1])])
+    cam = cfg["camera"]
+    camera = SimpleCamera(cam["focal_length"], cam["resolution"], cam["sensor_size"], False,
+                          position=cam["position"], rotation=cam["rotation"])
+    light = PointLight(cfg["lights"][0]["intensity"], position=cfg["lights"][0]["position"])
+    lid = cfg["lidar"]
+    lidar = SimpleLidar(False, position=lid["position"], rotation=lid["rotation"])
+    lidar.set_beam_grid(lid["nx"], lid["ny"], lid["half_x"], lid["half_y"])
+    for _ in range(max(3, args.warmup)):
+        img = group.render(camera, light, 1, 1, 1.0, cfg["bounces"])
+        rng, prim = group.lidar_scan(lidar)
+    n = max(3, min(args.steps, 20))
+    t = time.perf_counter()
+    for _ in range(n):
+        img = group.render(camera, light, 1, 1, 1.0, cfg["bounces"])
+        rng, prim = group.lidar_scan(lidar)
+    el = (time.perf_counter() - t) / n
+    d2h = img.nbytes + rng.nbytes + prim.nbytes
+    h2d = 3 * 160   # camera, light and LiDAR descriptors (kernel parameters); the BVH stays resident
+    return {"value": round(rays_step / el / 1e6, 2), "unit": UNIT, "h2d_bytes_per_step": h2d,
+            "d2h_bytes_per_step": int(d2h), "ms_per_step": round(el * 1e3, 3), "api": "crt.BodyFixedGroup"}
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        reference_arm(args)
+    else:
+        gpu_arm(args)
+
+
+if __name__ == "__main__":
+    main()

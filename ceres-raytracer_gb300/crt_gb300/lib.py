@@ -1,0 +1,341 @@
+"""ctypes binding of libcrt_gpu.so: every entry point declared in include/crt_gpu.h.
+
+This is the raw C ABI as a foreign caller sees it (plain pointers and sizes).  Arrays may be
+numpy arrays (host memory) or torch CUDA tensors (device memory); the library detects which.
+Raises `CrtError` for any non-zero status.  There is no CPU fallback: loading fails loudly when
+the shared library is missing, and every compute call needs a GB300.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import PKG_DIR
+
+LIB_PATH = os.path.join(PKG_DIR, "libcrt_gpu.so")
+
+CRT_OK = 0
+CRT_MISS = 0xFFFFFFFF
+
+vp = ctypes.c_void_p
+sz = ctypes.c_size_t
+u32 = ctypes.c_uint32
+i32 = ctypes.c_int
+dbl = ctypes.c_double
+
+
+class CrtError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"{msg} (status {status})")
+        self.status = status
+
+
+class EntityDesc(ctypes.Structure):
+    _fields_ = [("tri_xyz", vp), ("tri_vn", vp), ("n_tris", sz), ("scale", dbl), ("position", dbl * 3),
+                ("rotation", dbl * 9), ("color", ctypes.c_float * 3), ("smooth_shading", i32), ("id", u32),
+                ("rho_s", ctypes.c_float), ("rho_d", ctypes.c_float)]
+
+
+class CameraDesc(ctypes.Structure):
+    _fields_ = [("position", dbl * 3), ("rotation", dbl * 9), ("focal_length", dbl), ("resolution", dbl * 2),
+                ("sensor_size", dbl * 2), ("z_positive", i32)]
+
+
+class LightDesc(ctypes.Structure):
+    _fields_ = [("type", i32), ("intensity", dbl), ("position", dbl * 3), ("rotation", dbl * 9), ("size", dbl * 2)]
+
+
+class RenderParams(ctypes.Structure):
+    _fields_ = [("min_samples", i32), ("max_samples", i32), ("noise_threshold", dbl), ("num_bounces", i32),
+                ("seed", ctypes.c_uint64), ("request", u32)]
+
+
+class LidarGridDesc(ctypes.Structure):
+    _fields_ = [("position", dbl * 3), ("rotation", dbl * 9), ("z_positive", i32), ("nx", u32), ("ny", u32),
+                ("half_angle_x", dbl), ("half_angle_y", dbl)]
+
+
+class SrpDesc(ctypes.Structure):
+    _fields_ = [("sun_dir_inertial", dbl * 3), ("flux", dbl), ("c", dbl), ("center_of_mass", dbl * 3),
+                ("grid", u32), ("num_bounces", u32)]
+
+
+class SceneStats(ctypes.Structure):
+    _fields_ = [("n_tris", sz), ("n_nodes", sz), ("n_entities", sz), ("depth", u32), ("build_ms", dbl),
+                ("device_bytes", sz), ("bounds", ctypes.c_float * 6)]
+
+
+class Counters(ctypes.Structure):
+    _fields_ = [("rays", ctypes.c_uint64), ("nodes", ctypes.c_uint64), ("tris", ctypes.c_uint64),
+                ("launches", ctypes.c_uint64)]
+
+
+RAY_DTYPE = np.dtype([("o", np.float32, 3), ("tmin", np.float32), ("d", np.float32, 3), ("tmax", np.float32)])
+HIT_DTYPE = np.dtype([("t", np.float32), ("u", np.float32), ("v", np.float32), ("prim", np.uint32)])
+
+# name -> (argtypes, restype)
+SIGNATURES = {
+    "crt_abi_version": ([], i32),
+    "crt_status_string": ([i32], ctypes.c_char_p),
+    "crt_context_create": ([i32, ctypes.POINTER(vp)], i32),
+    "crt_context_destroy": ([vp], i32),
+    "crt_context_set_stream": ([vp, vp], i32),
+    "crt_context_get_stream": ([vp], vp),
+    "crt_context_synchronize": ([vp], i32),
+    "crt_context_set_counting": ([vp, i32], i32),
+    "crt_context_get_counters": ([vp, ctypes.POINTER(Counters)], i32),
+    "crt_context_reset_counters": ([vp], i32),
+    "crt_context_last_error": ([vp], ctypes.c_char_p),
+    "crt_mesh_load_obj": ([ctypes.c_char_p, ctypes.POINTER(vp)], i32),
+    "crt_mesh_num_tris": ([vp], sz),
+    "crt_mesh_xyz": ([vp], vp),
+    "crt_mesh_normals": ([vp], vp),
+    "crt_mesh_destroy": ([vp], None),
+    "crt_scene_create": ([vp, vp, u32, ctypes.POINTER(vp)], i32),
+    "crt_scene_destroy": ([vp], i32),
+    "crt_scene_get_stats": ([vp, ctypes.POINTER(SceneStats)], i32),
+    "crt_trace_closest": ([vp, vp, sz, vp], i32),
+    "crt_trace_any": ([vp, vp, sz, vp], i32),
+    "crt_passes": ([vp, ctypes.POINTER(CameraDesc), vp, vp, vp], i32),
+    "crt_lidar_batch": ([vp, vp, vp, sz, i32, vp, vp], i32),
+    "crt_lidar_grid": ([vp, ctypes.POINTER(LidarGridDesc), vp, vp], i32),
+    "crt_render": ([vp, ctypes.POINTER(CameraDesc), vp, u32, ctypes.POINTER(RenderParams), vp, vp], i32),
+    "crt_srp": ([vp, ctypes.POINTER(SrpDesc), vp, sz, vp, vp, vp], i32),
+}
+
+_lib = None
+
+
+def load():
+    """Load libcrt_gpu.so (raises if it is missing: there is no fallback)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise FileNotFoundError(f"{LIB_PATH} is missing: build the CUDA library first")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (args, res) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = res
+        _lib = L
+    return _lib
+
+
+def ptr(a):
+    """Data pointer of a numpy array or torch tensor (None passes NULL)."""
+    if a is None:
+        return None
+    if hasattr(a, "data_ptr"):
+        return a.data_ptr()
+    if not a.flags["C_CONTIGUOUS"]:
+        raise ValueError("array must be C-contiguous")
+    return a.ctypes.data
+
+
+def fill_camera(cam):
+    c = CameraDesc()
+    c.position[:] = [float(x) for x in np.asarray(cam["position"], dtype=np.float64).ravel()]
+    c.rotation[:] = [float(x) for x in np.asarray(cam["rotation"], dtype=np.float64).ravel()]
+    c.focal_length = float(cam["focal_length"])
+    c.resolution[:] = [float(x) for x in cam["resolution"]]
+    c.sensor_size[:] = [float(x) for x in cam["sensor_size"]]
+    c.z_positive = int(bool(cam.get("z_positive", False)))
+    return c
+
+
+def fill_lights(lights):
+    arr = (LightDesc * max(1, len(lights)))()
+    for i, l in enumerate(lights):
+        arr[i].type = 1 if l["type"] == "area" else 0
+        arr[i].intensity = float(l["intensity"])
+        arr[i].position[:] = [float(x) for x in np.asarray(l["position"], dtype=np.float64).ravel()]
+        arr[i].rotation[:] = [float(x) for x in np.asarray(l.get("rotation", np.eye(3)), dtype=np.float64).ravel()]
+        s = l.get("size", [0.0, 0.0])
+        arr[i].size[:] = [float(s[0]), float(s[1])]
+    return arr
+
+
+class Context:
+    """Owns a crt_context; scenes created from it are destroyed before it (the C ABI requires
+    scenes to be released before their context)."""
+
+    def __init__(self, device=0):
+        import weakref
+        self.L = load()
+        self._scenes = weakref.WeakSet()
+        self.h = None
+        h = vp()
+        self._check(self.L.crt_context_create(device, ctypes.byref(h)), None)
+        self.h = h
+
+    def _check(self, rc, h=-1):
+        if rc != CRT_OK:
+            hh = self.h if h == -1 else h
+            msg = self.L.crt_context_last_error(hh).decode() if hh else self.L.crt_status_string(rc).decode()
+            raise CrtError(rc, msg)
+
+    def close(self):
+        if getattr(self, "h", None):
+            for s in list(self._scenes):
+                s.close()
+            self.L.crt_context_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream_handle):
+        self._check(self.L.crt_context_set_stream(self.h, stream_handle))
+
+    def synchronize(self):
+        self._check(self.L.crt_context_synchronize(self.h))
+
+    def set_counting(self, on):
+        self._check(self.L.crt_context_set_counting(self.h, int(bool(on))))
+
+    def counters(self):
+        c = Counters()
+        self._check(self.L.crt_context_get_counters(self.h, ctypes.byref(c)))
+        return dict(rays=c.rays, nodes=c.nodes, tris=c.tris, launches=c.launches)
+
+    def reset_counters(self):
+        self._check(self.L.crt_context_reset_counters(self.h))
+
+    def scene(self, entities):
+        return Scene(self, entities)
+
+
+class Scene:
+    """Device-resident scene built from entity specs (objects with mesh/color/smooth/scale/position/
+    rotation/rho_s/rho_d attributes, e.g. crt_gb300.scenes.EntitySpec)."""
+
+    def __init__(self, ctx, entities, ids=None):
+        self.ctx = ctx
+        L = ctx.L
+        arr = (EntityDesc * max(1, len(entities)))()
+        keep = []
+        for i, e in enumerate(entities):
+            xyz = np.ascontiguousarray(e.mesh.soup(), dtype=np.float32)
+            vn = np.ascontiguousarray(e.mesh.soup_normals(), dtype=np.float32) if e.smooth else None
+            keep += [xyz, vn]
+            arr[i].tri_xyz = xyz.ctypes.data
+            arr[i].tri_vn = vn.ctypes.data if vn is not None else None
+            arr[i].n_tris = xyz.shape[0]
+            arr[i].scale = float(e.scale)
+            arr[i].position[:] = [float(x) for x in np.asarray(e.position, dtype=np.float64).ravel()]
+            arr[i].rotation[:] = [float(x) for x in np.asarray(e.rotation, dtype=np.float64).ravel()]
+            arr[i].color[:] = [float(x) for x in e.color]
+            arr[i].smooth_shading = int(bool(e.smooth))
+            arr[i].id = (i + 1) if ids is None else int(ids[i])
+            arr[i].rho_s = float(getattr(e, "rho_s", 0.0))
+            arr[i].rho_d = float(getattr(e, "rho_d", 0.0))
+        h = vp()
+        self.h = None
+        ctx._check(L.crt_scene_create(ctx.h, arr, len(entities), ctypes.byref(h)))
+        self.h = h
+        ctx._scenes.add(self)
+        del keep
+
+    def close(self):
+        if getattr(self, "h", None) and getattr(self.ctx, "h", None):
+            self.ctx.L.crt_scene_destroy(self.h)
+        self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def stats(self):
+        s = SceneStats()
+        self.ctx._check(self.ctx.L.crt_scene_get_stats(self.h, ctypes.byref(s)))
+        return dict(n_tris=s.n_tris, n_nodes=s.n_nodes, n_entities=s.n_entities, depth=s.depth, build_ms=s.build_ms,
+                    device_bytes=s.device_bytes, bounds=list(s.bounds))
+
+    def trace_closest(self, rays, out=None):
+        """rays: structured RAY_DTYPE array (or [n, 8] float32); returns HIT_DTYPE array."""
+        rays = np.ascontiguousarray(rays).view(RAY_DTYPE).reshape(-1) if not hasattr(rays, "data_ptr") else rays
+        n = rays.shape[0]
+        if out is None:
+            out = np.empty(n, HIT_DTYPE)
+        self.ctx._check(self.ctx.L.crt_trace_closest(self.h, ptr(rays), n, ptr(out)))
+        return out
+
+    def trace_any(self, rays, out=None):
+        rays = np.ascontiguousarray(rays).view(RAY_DTYPE).reshape(-1) if not hasattr(rays, "data_ptr") else rays
+        n = rays.shape[0]
+        if out is None:
+            out = np.empty(n, np.uint8)
+        self.ctx._check(self.ctx.L.crt_trace_any(self.h, ptr(rays), n, ptr(out)))
+        return out
+
+    def passes(self, cam, xyz=True, ids=True, normals=True):
+        c = fill_camera(cam)
+        W, H = int(np.floor(cam["resolution"][0])), int(np.floor(cam["resolution"][1]))
+        ox = np.empty((H, W, 3)) if xyz is True else (xyz or None)
+        oi = np.empty((H, W), np.uint32) if ids is True else (ids or None)
+        on = np.empty((H, W, 3)) if normals is True else (normals or None)
+        self.ctx._check(self.ctx.L.crt_passes(self.h, ctypes.byref(c), ptr(ox), ptr(oi), ptr(on)))
+        return ox, oi, on
+
+    def lidar_batch(self, positions, rotations, z_positive=False, want_prim=True):
+        positions = np.ascontiguousarray(positions, dtype=np.float64).reshape(-1, 3)
+        rotations = np.ascontiguousarray(rotations, dtype=np.float64).reshape(-1, 9)
+        n = positions.shape[0]
+        rng = np.empty(n)
+        prim = np.empty(n, np.uint32) if want_prim else None
+        self.ctx._check(self.ctx.L.crt_lidar_batch(self.h, ptr(positions), ptr(rotations), n, int(bool(z_positive)),
+                                                   ptr(rng), ptr(prim)))
+        return rng, prim
+
+    def lidar_grid(self, position, rotation, nx, ny, half_x, half_y, z_positive=False, out_range=None, out_prim=None):
+        g = LidarGridDesc()
+        g.position[:] = [float(x) for x in np.asarray(position, dtype=np.float64).ravel()]
+        g.rotation[:] = [float(x) for x in np.asarray(rotation, dtype=np.float64).ravel()]
+        g.z_positive = int(bool(z_positive))
+        g.nx, g.ny = int(nx), int(ny)
+        g.half_angle_x, g.half_angle_y = float(half_x), float(half_y)
+        rng = np.empty((ny, nx)) if out_range is None else out_range
+        prim = np.empty((ny, nx), np.uint32) if out_prim is None else out_prim
+        self.ctx._check(self.ctx.L.crt_lidar_grid(self.h, ctypes.byref(g), ptr(rng), ptr(prim)))
+        return rng, prim
+
+    def render(self, cam, lights, min_samples=1, max_samples=1, noise_threshold=1.0, num_bounces=1, seed=0,
+               request=0, want_radiance=True, out_rgba=None, out_radiance=None):
+        c = fill_camera(cam)
+        L = fill_lights(lights)
+        p = RenderParams(int(min_samples), int(max_samples), float(noise_threshold), int(num_bounces), int(seed),
+                         int(request))
+        W, H = int(np.floor(cam["resolution"][0])), int(np.floor(cam["resolution"][1]))
+        rgba = np.empty((H, W, 4), np.uint8) if out_rgba is None else out_rgba
+        rad = (np.empty((H, W, 4), np.float32) if want_radiance else None) if out_radiance is None else out_radiance
+        self.ctx._check(self.ctx.L.crt_render(self.h, ctypes.byref(c), L, len(lights), ctypes.byref(p), ptr(rgba),
+                                              ptr(rad)))
+        return rgba, rad
+
+    def srp(self, sun_dir, quaternions, grid, num_bounces=2, flux=1361.0, c=299792458.0, center_of_mass=(0, 0, 0),
+            facet_power=False):
+        d = SrpDesc()
+        d.sun_dir_inertial[:] = [float(x) for x in sun_dir]
+        d.flux, d.c = float(flux), float(c)
+        d.center_of_mass[:] = [float(x) for x in center_of_mass]
+        d.grid, d.num_bounces = int(grid), int(num_bounces)
+        q = np.ascontiguousarray(quaternions, dtype=np.float64).reshape(-1, 4)
+        n = q.shape[0]
+        f, t = np.empty((n, 3)), np.empty((n, 3))
+        fp = np.empty((n, self.stats()["n_tris"])) if facet_power else None
+        self.ctx._check(self.ctx.L.crt_srp(self.h, ctypes.byref(d), ptr(q), n, ptr(f), ptr(t), ptr(fp)))
+        return f, t, fp
+
+
+def make_rays(o, d, tmin=0.0, tmax=3.4e38):
+    """Structured FP32 ray array from [n, 3] origins and directions."""
+    o, d = np.asarray(o), np.asarray(d)
+    r = np.empty(o.shape[0], RAY_DTYPE)
+    r["o"], r["d"] = o, d
+    r["tmin"], r["tmax"] = tmin, tmax
+    return r

@@ -162,6 +162,17 @@ def _lib():
     return _scene_lib
 
 
+def write_obj_fast(mesh, path):
+    """Write a mesh as OBJ through the C writer ('%.9g', float32 round trip)."""
+    lib = _lib()
+    v = np.ascontiguousarray(mesh.vertices, dtype=np.float32)
+    f = np.ascontiguousarray(mesh.faces, dtype=np.int32)
+    lib.crt_obj_write.argtypes = [ctypes.c_char_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t]
+    rc = lib.crt_obj_write(path.encode(), v.ctypes.data, v.shape[0], f.ctypes.data, f.shape[0])
+    if rc != 0:
+        raise OSError(f"crt_obj_write failed ({rc}) for {path}")
+
+
 def asteroid_level_for(target_faces):
     """Smallest icosphere level with at least 2.5x the target face count (9 for 2M, 10 for 8M)."""
     level = 0

@@ -1,0 +1,75 @@
+"""Seeded synthetic workloads with the shapes of the benchmark configurations.
+
+asteroid_config()   procedural asteroid (icosphere level 9 decimated to 2M triangles, radius 1 km,
+                    6-octave value noise, 5 % amplitude, albedo 0.1); camera 2048^2, 10 deg FOV at
+                    5 km; sun as a point light 1e9 m away along a random direction with
+                    intensity / d^2 = 1; 1 spp, 1 bounce (primary + shadow ray); LiDAR 1024^2 beams
+                    over +-5 deg from the camera pose.
+batched_config()    64 requests on the same asteroid: 32 renders (resolution in {128..2048}^2, spp in
+                    {1, 4, 16, 64}, 2 bounces, poses on a 3-10 km shell) and 32 LiDAR scans of
+                    64^2 .. 1024^2 beams; seed 1.
+srp_config()        spacecraft (~50k triangles), 256 random attitudes, 4096^2 rays, 2 bounces.
+"""
+import numpy as np
+
+from . import scenes
+
+SUN_DISTANCE = 1.0e9
+
+
+def asteroid_entities(target_faces=2_000_000, seed=0, smooth=False):
+    mesh = scenes.cached_asteroid(target_faces, seed=seed)
+    return [scenes.EntitySpec("asteroid", mesh, (0.1, 0.1, 0.1), smooth=smooth)]
+
+
+def pose_on_shell(rng, rmin, rmax):
+    d = rng.normal(size=3)
+    d /= np.linalg.norm(d)
+    return d * rng.uniform(rmin, rmax)
+
+
+def asteroid_config(res=2048, lidar_n=1024, seed=0):
+    cam_pos = 5000.0 * scenes.unit_vector(1000 + seed)
+    camera = scenes.fov_camera(scenes.TAN5, (res, res), cam_pos, (0.0, 0.0, 0.0))
+    sun = scenes.unit_vector(2000 + seed)
+    lights = [dict(type="point", intensity=SUN_DISTANCE ** 2, position=SUN_DISTANCE * sun)]
+    lidar = dict(position=cam_pos, rotation=camera["rotation"], nx=lidar_n, ny=lidar_n,
+                 half_x=np.deg2rad(5.0), half_y=np.deg2rad(5.0))
+    return dict(camera=camera, lights=lights, lidar=lidar, spp=1, bounces=1)
+
+
+def batched_config(seed=1, n_render=32, n_lidar=32):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    sun = scenes.unit_vector(3000 + seed)
+    lights = [dict(type="point", intensity=SUN_DISTANCE ** 2, position=SUN_DISTANCE * sun)]
+    reqs = []
+    for i in range(n_render):
+        res = int(rng.choice([128, 256, 512, 1024, 2048]))
+        spp = int(rng.choice([1, 4, 16, 64]))
+        pos = pose_on_shell(rng, 3000.0, 10000.0)
+        # FOV wide enough to frame the body from the pose's range
+        tan_half = 1100.0 / np.linalg.norm(pos)
+        cam = scenes.fov_camera(tan_half, (res, res), pos, (0.0, 0.0, 0.0))
+        reqs.append(dict(kind="render", camera=cam, lights=lights, spp=spp, bounces=2, request=i))
+    for i in range(n_lidar):
+        n = int(rng.choice([64, 128, 256, 512, 1024]))
+        pos = pose_on_shell(rng, 3000.0, 10000.0)
+        R = scenes.look_at(pos, (0.0, 0.0, 0.0))
+        reqs.append(dict(kind="lidar", position=pos, rotation=R, nx=n, ny=n, half_x=np.deg2rad(5.0),
+                         half_y=np.deg2rad(5.0), request=n_render + i))
+    order = rng.permutation(len(reqs))
+    return [reqs[k] for k in order]
+
+
+def request_rays(req):
+    """Primary rays of a request (renders: pixels x samples; LiDAR: beams)."""
+    if req["kind"] == "render":
+        w, h = req["camera"]["resolution"]
+        return int(w) * int(h) * int(req["spp"])
+    return int(req["nx"]) * int(req["ny"])
+
+
+def srp_config(n_att=256, grid=4096, seed=0):
+    ents = scenes.spacecraft()
+    q = scenes.random_quaternions(n_att, seed=seed)
+    return dict(entities=ents, quaternions=q, grid=grid, num_bounces=2, sun=np.array([1.0, 0.0, 0.0]))

@@ -1,0 +1,278 @@
+// Internal declarations shared by the CUDA translation units of libcrt_gpu.so.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstddef>
+#include <string>
+#include <vector>
+#include <mutex>
+
+#include "crt_gpu.h"
+
+// ------------------------------------------------------------------ error plumbing
+struct CrtError {
+    int status;
+    std::string msg;
+};
+
+#define CRT_CUDA(call)                                                                        \
+    do {                                                                                      \
+        cudaError_t e_ = (call);                                                              \
+        if (e_ != cudaSuccess)                                                                \
+            throw CrtError{e_ == cudaErrorMemoryAllocation ? CRT_ERR_OOM : CRT_ERR_CUDA,      \
+                           std::string(#call) + ": " + cudaGetErrorString(e_)};               \
+    } while (0)
+
+#define CRT_CHECK(cond, status, msg)                                                          \
+    do {                                                                                      \
+        if (!(cond)) throw CrtError{(status), (msg)};                                         \
+    } while (0)
+
+// ------------------------------------------------------------------ device error word bits
+enum : uint32_t {
+    DEVERR_STACK_OVERFLOW = 1u << 0,
+    DEVERR_BUILD_OVERFLOW = 1u << 1,
+    DEVERR_QUANT_RANGE = 1u << 2,
+    DEVERR_WAIT_LIMIT = 1u << 3,
+    DEVERR_BAD_INDEX = 1u << 4,
+};
+
+// ------------------------------------------------------------------ context
+enum ScratchSlot {
+    SCR_QUEUE = 0,      // persistent-kernel work counters
+    SCR_RAYS,           // staged rays / hits
+    SCR_OUT0,
+    SCR_OUT1,
+    SCR_OUT2,
+    SCR_IN0,
+    SCR_IN1,
+    SCR_BUILD0,
+    SCR_BUILD1,
+    SCR_BUILD2,
+    SCR_BUILD3,
+    SCR_BUILD4,
+    SCR_BUILD5,
+    SCR_BUILD6,
+    SCR_BUILD7,
+    SCR_WAVE0,
+    SCR_WAVE1,
+    SCR_WAVE2,
+    SCR_WAVE3,
+    SCR_WAVE4,
+    SCR_WAVE5,
+    SCR_WAVE6,
+    SCR_WAVE7,
+    SCR_COUNT
+};
+
+struct crt_context {
+    int device = 0;
+    int sm_count = 0;
+    int max_threads_per_sm = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    std::string last_error;
+    bool counting = false;
+    unsigned long long* d_counters = nullptr;   // rays, nodes, tris
+    uint32_t* d_error = nullptr;                // device error word
+    uint64_t launches = 0;
+    void* scratch[SCR_COUNT] = {};
+    size_t scratch_bytes[SCR_COUNT] = {};
+    void* pinned = nullptr;
+    size_t pinned_bytes = 0;
+};
+
+// Grow-only device scratch buffer for one purpose.  Synchronises the stream before reallocating.
+void* ctx_scratch(crt_context* ctx, ScratchSlot slot, size_t bytes);
+// Pinned host staging buffer (grow-only).
+void* ctx_pinned(crt_context* ctx, size_t bytes);
+bool is_device_ptr(const void* p);
+// Copy helpers: ensure `bytes` of `src` are readable on the device; return a device pointer.
+const void* to_device(crt_context* ctx, const void* src, size_t bytes, ScratchSlot slot);
+// Output staging: returns a device pointer to write into (dst itself when it is device memory).
+void* out_device(crt_context* ctx, void* dst, size_t bytes, ScratchSlot slot);
+// Copy a staged output back to host memory (no-op for device outputs); synchronous for host outputs.
+void out_finish(crt_context* ctx, void* dst, const void* staged, size_t bytes);
+void check_launch(crt_context* ctx, const char* what);
+// Read and clear the device error word; throws CRT_ERR_DEVICE when set.
+void check_device_error(crt_context* ctx, const char* what);
+
+template <typename F>
+int crt_guard(crt_context* ctx, F&& f) {
+    try {
+        f();
+        return CRT_OK;
+    } catch (const CrtError& e) {
+        if (ctx) ctx->last_error = e.msg;
+        return e.status;
+    } catch (const std::bad_alloc&) {
+        if (ctx) ctx->last_error = "host allocation failed";
+        return CRT_ERR_OOM;
+    } catch (const std::exception& e) {
+        if (ctx) ctx->last_error = e.what();
+        return CRT_ERR_INVALID;
+    }
+}
+
+// ------------------------------------------------------------------ scene
+// 8-wide compressed node, 80 bytes = 5 x float4:
+//  w0: origin p (float x3), exponents ex/ey/ez (int8) + imask (uint8)
+//  w1: child_base (uint32), tri_base (uint32), meta[0..7] (uint8)
+//  w2: qlo_x[8], qlo_y[8]     w3: qlo_z[8], qhi_x[8]     w4: qhi_y[8], qhi_z[8]
+// meta per slot: 0 = empty; internal child: (1 << 5) | (24 + slot);
+//                leaf: (unary triangle count << 5) | offset from tri_base (< 24).
+// Internal children are stored contiguously from child_base in slot order.
+struct WideNode {
+    float4 w[5];
+};
+static_assert(sizeof(WideNode) == 80, "wide node must be 80 bytes");
+
+struct EntityDev {
+    float color[3];
+    uint32_t smooth;
+    uint32_t id;
+    float rho_s, rho_d;
+    uint32_t pad;
+};
+
+struct crt_scene {
+    crt_context* ctx = nullptr;
+    size_t n_tris = 0;
+    uint32_t n_entities = 0;
+    size_t n_nodes = 0;
+    uint32_t depth = 0;
+    WideNode* nodes = nullptr;
+    float4* tris = nullptr;           // 3 float4 per leaf slot: (p0, e1.x) (e1.yz, e2.xy) (e2.z, n)
+    uint32_t* leaf_prim = nullptr;    // leaf slot -> scene primitive index
+    float4* leaf_vn = nullptr;        // 3 float4 per leaf slot: vertex normals vn0, vn1, vn2 (xyz)
+    uint32_t* leaf_entity = nullptr;  // leaf slot -> entity index
+    EntityDev* entities = nullptr;
+    float bounds[6] = {0, 0, 0, 0, 0, 0};
+    double build_ms = 0;
+    size_t device_bytes = 0;
+    std::vector<EntityDev> host_entities;
+};
+
+void scene_build(crt_scene* s, const crt_entity_desc* ents, uint32_t n);   // bvh_build.cu
+
+// ------------------------------------------------------------------ device math
+__host__ __device__ __forceinline__ float3 f3(float x, float y, float z) { return make_float3(x, y, z); }
+__host__ __device__ __forceinline__ float3 operator+(float3 a, float3 b) { return f3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__host__ __device__ __forceinline__ float3 operator-(float3 a, float3 b) { return f3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__host__ __device__ __forceinline__ float3 operator*(float3 a, float s) { return f3(a.x * s, a.y * s, a.z * s); }
+__host__ __device__ __forceinline__ float3 operator*(float s, float3 a) { return f3(a.x * s, a.y * s, a.z * s); }
+__host__ __device__ __forceinline__ float dot3(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__host__ __device__ __forceinline__ float3 cross3(float3 a, float3 b) {
+    return f3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+__device__ __forceinline__ float3 normalize3(float3 a) { return a * (1.0f / sqrtf(dot3(a, a))); }
+
+// Ray in registers for traversal.
+struct TRay {
+    float3 o, d;
+    float tmin, tmax;
+    uint32_t skip = CRT_MISS;   // leaf slot not tested (origin triangle of a secondary ray)
+};
+
+// Result of the triangle test in leaf-slot space.
+struct THit {
+    float t, u, v;
+    uint32_t slot;   // CRT_MISS when nothing was hit
+};
+
+// FP32 form of Triangle::intersect (lib/bvh/triangle.hpp:140-160): c = p0 - o, r = d x c,
+// inv_det = 1 / (n . d), u = (r . e2) inv_det, v = (r . e1) inv_det, w = 1 - u - v; accepts
+// u, v, w >= 0 (comparisons reject NaN) and tmin <= t <= tmax with t = (n . c) inv_det.
+__device__ __forceinline__ bool tri_test(const float4 a, const float4 b, const float4 c4, const TRay& r, float& t,
+                                         float& u, float& v) {
+    const float3 p0 = f3(a.x, a.y, a.z);
+    const float3 e1 = f3(a.w, b.x, b.y);
+    const float3 e2 = f3(b.z, b.w, c4.x);
+    const float3 n = f3(c4.y, c4.z, c4.w);
+    const float3 c = p0 - r.o;
+    const float3 rr = cross3(r.d, c);
+    const float inv_det = 1.0f / dot3(n, r.d);
+    const float uu = dot3(rr, e2) * inv_det;
+    const float vv = dot3(rr, e1) * inv_det;
+    const float ww = 1.0f - uu - vv;
+    if (uu >= 0.0f && vv >= 0.0f && ww >= 0.0f) {
+        const float tt = dot3(n, c) * inv_det;
+        if (tt >= r.tmin && tt <= r.tmax) {
+            t = tt;
+            u = uu;
+            v = vv;
+            return true;
+        }
+    }
+    return false;
+}
+
+// Vector::safe_inverse (lib/bvh/vector.hpp:75-80) in FP32.
+__device__ __forceinline__ float safe_rcp(float x) {
+    const float eps = 1.1920929e-07f;
+    return 1.0f / (fabsf(x) < eps ? copysignf(eps, x) : x);
+}
+
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11): counter (c0..c3), key (k0, k1).
+__host__ __device__ __forceinline__ void philox4x32(uint32_t c[4], uint32_t k0, uint32_t k1) {
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+#ifdef __CUDA_ARCH__
+        const uint32_t hi0 = __umulhi(0xD2511F53u, c[0]), lo0 = 0xD2511F53u * c[0];
+        const uint32_t hi1 = __umulhi(0xCD9E8D57u, c[2]), lo1 = 0xCD9E8D57u * c[2];
+#else
+        const uint64_t p0 = (uint64_t)0xD2511F53u * c[0], p1 = (uint64_t)0xCD9E8D57u * c[2];
+        const uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0, hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+#endif
+        const uint32_t n0 = hi1 ^ c[1] ^ k0, n2 = hi0 ^ c[3] ^ k1;
+        c[0] = n0;
+        c[1] = lo1;
+        c[2] = n2;
+        c[3] = lo0;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+}
+// 24-bit uniform in [0, 1), exactly representable in float and double
+__host__ __device__ __forceinline__ float unif24(uint32_t x) { return (float)(x >> 8) * (1.0f / 16777216.0f); }
+
+// Host-side FP64 -> FP32 camera basis: direction(u, v) = normalize(a + u b + v c).
+struct CamBasis {
+    float o[3];
+    float a[3], b[3], c[3];
+    double o64[3], a64[3], b64[3], c64[3];   // the same basis in FP64 (reported distances)
+    uint32_t width, height;
+};
+
+// Distance along an FP64 ray (o, d) to the plane of the FP32 triangle stored at leaf `slot`
+// (p0 and n of the record): the traversal picks the triangle in FP32, the reported hit point and
+// range are then evaluated along the FP64 ray of the FP64 pose, as the reference evaluates them.
+__device__ __forceinline__ double plane_t64(const float4* __restrict__ tris, uint32_t slot, const double o[3],
+                                            const double d[3]) {
+    const float4 a = __ldg(tris + 3ull * slot), c = __ldg(tris + 3ull * slot + 2);
+    const double n0 = c.y, n1 = c.z, n2 = c.w;
+    const double den = n0 * d[0] + n1 * d[1] + n2 * d[2];
+    const double num = n0 * ((double)a.x - o[0]) + n1 * ((double)a.y - o[1]) + n2 * ((double)a.z - o[2]);
+    return num / den;
+}
+
+// Barycentric u, v of the FP64 ray (o, d) on the FP32 triangle at leaf `slot`, with the reference's
+// formula (triangle.hpp:140-160) in FP64; false if the determinant vanishes.
+__device__ __forceinline__ bool bary64(const float4* __restrict__ tris, uint32_t slot, const double o[3],
+                                       const double d[3], double& u, double& v) {
+    const float4 a = __ldg(tris + 3ull * slot), b = __ldg(tris + 3ull * slot + 1), c4 = __ldg(tris + 3ull * slot + 2);
+    const double p0[3] = {a.x, a.y, a.z}, e1[3] = {a.w, b.x, b.y}, e2[3] = {b.z, b.w, c4.x}, n[3] = {c4.y, c4.z, c4.w};
+    const double c[3] = {p0[0] - o[0], p0[1] - o[1], p0[2] - o[2]};
+    const double r[3] = {d[1] * c[2] - d[2] * c[1], d[2] * c[0] - d[0] * c[2], d[0] * c[1] - d[1] * c[0]};
+    const double det = n[0] * d[0] + n[1] * d[1] + n[2] * d[2];
+    if (det == 0.0) return false;
+    const double inv = 1.0 / det;
+    u = (r[0] * e2[0] + r[1] * e2[1] + r[2] * e2[2]) * inv;
+    v = (r[0] * e1[0] + r[1] * e1[1] + r[2] * e1[2]) * inv;
+    return isfinite(u) && isfinite(v);
+}
+CamBasis make_camera_basis(const crt_camera_desc* cam);
+
+// Kernel launch helpers
+int occupancy_grid(crt_context* ctx, const void* kernel, int block, size_t smem);

@@ -1,0 +1,240 @@
+// Context management, scratch memory, host/device staging and status reporting.
+#include "common.cuh"
+
+#include <cmath>
+#include <cstring>
+
+void* ctx_scratch(crt_context* ctx, ScratchSlot slot, size_t bytes) {
+    if (bytes == 0) bytes = 16;
+    if (ctx->scratch_bytes[slot] < bytes) {
+        if (ctx->scratch[slot]) {
+            CRT_CUDA(cudaStreamSynchronize(ctx->stream));
+            CRT_CUDA(cudaFree(ctx->scratch[slot]));
+            ctx->scratch[slot] = nullptr;
+            ctx->scratch_bytes[slot] = 0;
+        }
+        size_t cap = bytes + bytes / 4;
+        cap = (cap + 255) & ~size_t(255);
+        CRT_CUDA(cudaMalloc(&ctx->scratch[slot], cap));
+        ctx->scratch_bytes[slot] = cap;
+    }
+    return ctx->scratch[slot];
+}
+
+void* ctx_pinned(crt_context* ctx, size_t bytes) {
+    if (ctx->pinned_bytes < bytes) {
+        if (ctx->pinned) {
+            CRT_CUDA(cudaStreamSynchronize(ctx->stream));
+            CRT_CUDA(cudaFreeHost(ctx->pinned));
+            ctx->pinned = nullptr;
+            ctx->pinned_bytes = 0;
+        }
+        size_t cap = (bytes + bytes / 4 + 4095) & ~size_t(4095);
+        CRT_CUDA(cudaMallocHost(&ctx->pinned, cap));
+        ctx->pinned_bytes = cap;
+    }
+    return ctx->pinned;
+}
+
+bool is_device_ptr(const void* p) {
+    if (!p) return false;
+    cudaPointerAttributes attr;
+    cudaError_t e = cudaPointerGetAttributes(&attr, p);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged;
+}
+
+const void* to_device(crt_context* ctx, const void* src, size_t bytes, ScratchSlot slot) {
+    if (!src || bytes == 0) return src;
+    if (is_device_ptr(src)) return src;
+    void* d = ctx_scratch(ctx, slot, bytes);
+    CRT_CUDA(cudaMemcpyAsync(d, src, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    return d;
+}
+
+void* out_device(crt_context* ctx, void* dst, size_t bytes, ScratchSlot slot) {
+    if (!dst) return nullptr;
+    if (is_device_ptr(dst)) return dst;
+    return ctx_scratch(ctx, slot, bytes);
+}
+
+void out_finish(crt_context* ctx, void* dst, const void* staged, size_t bytes) {
+    if (!dst || dst == staged || bytes == 0) return;
+    CRT_CUDA(cudaMemcpyAsync(dst, staged, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+}
+
+void check_launch(crt_context* ctx, const char* what) {
+    ctx->launches++;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) throw CrtError{CRT_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e)};
+}
+
+void check_device_error(crt_context* ctx, const char* what) {
+    uint32_t h = 0;
+    CRT_CUDA(cudaMemcpyAsync(&h, ctx->d_error, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+    CRT_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (h) {
+        CRT_CUDA(cudaMemsetAsync(ctx->d_error, 0, sizeof(uint32_t), ctx->stream));
+        std::string m = std::string(what) + ": device check failed (";
+        if (h & DEVERR_STACK_OVERFLOW) m += " traversal-stack-overflow";
+        if (h & DEVERR_BUILD_OVERFLOW) m += " build-overflow";
+        if (h & DEVERR_QUANT_RANGE) m += " quantisation-range";
+        if (h & DEVERR_WAIT_LIMIT) m += " wait-limit";
+        if (h & DEVERR_BAD_INDEX) m += " bad-index";
+        m += " )";
+        throw CrtError{(h & DEVERR_WAIT_LIMIT) ? CRT_ERR_TIMEOUT : CRT_ERR_DEVICE, m};
+    }
+}
+
+int occupancy_grid(crt_context* ctx, const void* kernel, int block, size_t smem) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, smem) != cudaSuccess || per_sm < 1) {
+        cudaGetLastError();
+        per_sm = 1;
+    }
+    return per_sm * ctx->sm_count;
+}
+
+CamBasis make_camera_basis(const crt_camera_desc* cam) {
+    // SimpleCamera::pixel_to_ray (cameras/simple_camera.hpp:61-81) is, before normalisation,
+    // R^T ((u - cx)/sx, (cy - v)/sy, +-f): affine in (u, v).  Evaluate its three FP64 terms once.
+    const double* R = cam->rotation;
+    const double cx = cam->resolution[0] / 2.0, cy = cam->resolution[1] / 2.0;
+    const double sx = cam->resolution[0] / cam->sensor_size[0], sy = cam->resolution[1] / cam->sensor_size[1];
+    const double fz = cam->z_positive ? cam->focal_length : -cam->focal_length;
+    const double a_cam[3] = {-cx / sx, cy / sy, fz};
+    const double b_cam[3] = {1.0 / sx, 0.0, 0.0};
+    const double c_cam[3] = {0.0, -1.0 / sy, 0.0};
+    CamBasis cb;
+    for (int k = 0; k < 3; ++k) {
+        // (R^T v)_k = R[0][k] v0 + R[1][k] v1 + R[2][k] v2
+        cb.a64[k] = R[k] * a_cam[0] + R[3 + k] * a_cam[1] + R[6 + k] * a_cam[2];
+        cb.b64[k] = R[k] * b_cam[0] + R[3 + k] * b_cam[1] + R[6 + k] * b_cam[2];
+        cb.c64[k] = R[k] * c_cam[0] + R[3 + k] * c_cam[1] + R[6 + k] * c_cam[2];
+        cb.o64[k] = cam->position[k];
+        cb.a[k] = (float)cb.a64[k];
+        cb.b[k] = (float)cb.b64[k];
+        cb.c[k] = (float)cb.c64[k];
+        cb.o[k] = (float)cb.o64[k];
+    }
+    cb.width = (uint32_t)std::floor(cam->resolution[0]);
+    cb.height = (uint32_t)std::floor(cam->resolution[1]);
+    return cb;
+}
+
+extern "C" {
+
+int crt_abi_version(void) { return CRT_ABI_VERSION; }
+
+const char* crt_status_string(int s) {
+    switch (s) {
+        case CRT_OK: return "ok";
+        case CRT_ERR_INVALID: return "invalid argument";
+        case CRT_ERR_CUDA: return "CUDA error";
+        case CRT_ERR_OOM: return "out of memory";
+        case CRT_ERR_TIMEOUT: return "timeout";
+        case CRT_ERR_IO: return "I/O error";
+        case CRT_ERR_DEVICE: return "device-side check failed";
+        case CRT_ERR_NO_DEVICE: return "no usable CUDA device";
+        default: return "unknown status";
+    }
+}
+
+int crt_context_create(int device, crt_context** out) {
+    if (!out) return CRT_ERR_INVALID;
+    *out = nullptr;
+    crt_context* ctx = new crt_context();
+    int rc = crt_guard(ctx, [&] {
+        int n = 0;
+        cudaError_t e = cudaGetDeviceCount(&n);
+        if (e != cudaSuccess || n == 0) {
+            cudaGetLastError();
+            throw CrtError{CRT_ERR_NO_DEVICE, "no CUDA device available"};
+        }
+        CRT_CHECK(device >= 0 && device < n, CRT_ERR_INVALID, "device index out of range");
+        CRT_CUDA(cudaSetDevice(device));
+        cudaDeviceProp prop;
+        CRT_CUDA(cudaGetDeviceProperties(&prop, device));
+        CRT_CHECK(prop.major * 10 + prop.minor == 103, CRT_ERR_NO_DEVICE,
+                  "libcrt_gpu.so is built for sm_103a (GB300); this device is sm_" + std::to_string(prop.major) +
+                      std::to_string(prop.minor));
+        ctx->device = device;
+        ctx->sm_count = prop.multiProcessorCount;
+        ctx->max_threads_per_sm = prop.maxThreadsPerMultiProcessor;
+        CRT_CUDA(cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking));
+        ctx->stream = ctx->own_stream;
+        CRT_CUDA(cudaMalloc(&ctx->d_counters, 4 * sizeof(unsigned long long)));
+        CRT_CUDA(cudaMemset(ctx->d_counters, 0, 4 * sizeof(unsigned long long)));
+        CRT_CUDA(cudaMalloc(&ctx->d_error, sizeof(uint32_t)));
+        CRT_CUDA(cudaMemset(ctx->d_error, 0, sizeof(uint32_t)));
+    });
+    if (rc != CRT_OK) {
+        crt_context_destroy(ctx);
+        return rc;
+    }
+    *out = ctx;
+    return CRT_OK;
+}
+
+int crt_context_destroy(crt_context* ctx) {
+    if (!ctx) return CRT_OK;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    for (int i = 0; i < SCR_COUNT; ++i)
+        if (ctx->scratch[i]) cudaFree(ctx->scratch[i]);
+    if (ctx->pinned) cudaFreeHost(ctx->pinned);
+    if (ctx->d_counters) cudaFree(ctx->d_counters);
+    if (ctx->d_error) cudaFree(ctx->d_error);
+    if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+    delete ctx;
+    return CRT_OK;
+}
+
+int crt_context_set_stream(crt_context* ctx, void* stream) {
+    if (!ctx) return CRT_ERR_INVALID;
+    return crt_guard(ctx, [&] {
+        CRT_CUDA(cudaStreamSynchronize(ctx->stream));
+        ctx->stream = stream ? (cudaStream_t)stream : ctx->own_stream;
+    });
+}
+
+void* crt_context_get_stream(crt_context* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
+int crt_context_synchronize(crt_context* ctx) {
+    if (!ctx) return CRT_ERR_INVALID;
+    return crt_guard(ctx, [&] { CRT_CUDA(cudaStreamSynchronize(ctx->stream)); });
+}
+
+int crt_context_set_counting(crt_context* ctx, int enabled) {
+    if (!ctx) return CRT_ERR_INVALID;
+    ctx->counting = enabled != 0;
+    return CRT_OK;
+}
+
+int crt_context_get_counters(crt_context* ctx, crt_counters* out) {
+    if (!ctx || !out) return CRT_ERR_INVALID;
+    return crt_guard(ctx, [&] {
+        unsigned long long h[4] = {0, 0, 0, 0};
+        CRT_CUDA(cudaMemcpyAsync(h, ctx->d_counters, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+        CRT_CUDA(cudaStreamSynchronize(ctx->stream));
+        out->rays = h[0];
+        out->nodes = h[1];
+        out->tris = h[2];
+        out->launches = ctx->launches;
+    });
+}
+
+int crt_context_reset_counters(crt_context* ctx) {
+    if (!ctx) return CRT_ERR_INVALID;
+    return crt_guard(ctx, [&] {
+        CRT_CUDA(cudaMemsetAsync(ctx->d_counters, 0, 4 * sizeof(unsigned long long), ctx->stream));
+        ctx->launches = 0;
+    });
+}
+
+const char* crt_context_last_error(const crt_context* ctx) { return ctx ? ctx->last_error.c_str() : "null context"; }
+
+}  // extern "C"

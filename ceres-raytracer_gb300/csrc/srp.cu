@@ -1,0 +1,279 @@
+// Solar radiation pressure over parallel sun-ray grids (no counterpart in the reference; its README
+// names the feature only).
+//
+// Model (flat plate, Montenbruck & Gill, Satellite Orbits, sec. 3.4): a ray of power E travelling
+// along d that hits a facet with unit normal n facing the ray (cos = -d.n >= 0) transfers
+//     dF = (E / c) [ (1 - rs) d - (2 rs cos + 2/3 rd) n ],   dT = (x - c_m) x dF,
+// the facet absorbs (1 - rs - rd) E, and the specular part continues along d - 2 (d.n) n with power
+// rs E for up to num_bounces further segments.  Facets are two-sided.  rs / rd come from the hit
+// triangle's entity.
+//
+// Per attitude the sun direction is rotated into the body frame in FP64 (s_b = R(q)^T s_i); rays
+// start on a grid x grid square of side 2 R_b (R_b = half diagonal of the scene box) centred on the
+// box centre, 2 R_b + 1 upstream, one ray per cell centre, power flux * cell area.
+//
+// Reduction: each persistent warp takes CHUNK tiles (8 x 4 rays each) of one attitude at a time;
+// lanes accumulate force and torque in FP64, the warp reduces them with shuffles, and lane 0 writes
+// the chunk's partial sums to a slot indexed by the chunk, so the per-attitude totals (summed by
+// k_srp_reduce in a fixed order) are bitwise reproducible.  Facet powers use warp-aggregated FP64
+// atomics (reproducible up to the order of additions).
+#include "common.cuh"
+#include "trace.cuh"
+
+#include <cmath>
+#include <vector>
+
+namespace {
+
+constexpr uint32_t CHUNK = 16;   // tiles per work grab
+
+struct SrpAtt {
+    float org[3];   // centre of cell (0, 0)
+    float du[3];    // step to the next cell in x
+    float dv[3];    // step to the next cell in y
+    float dir[3];   // -s_b
+    float E0;       // flux * cell area
+    float pad;
+};
+
+struct SrpArgs {
+    const SrpAtt* att;
+    uint32_t G;
+    uint32_t tiles;          // tiles per attitude
+    uint32_t grabs_per_att;
+    uint32_t n_att;
+    float inv_c;
+    float cm[3];
+    uint32_t nb;
+    double* partial;         // n_att * grabs_per_att * 6
+    double* facet;           // n_att * n_tris or null
+    uint32_t n_tris;
+};
+
+__global__ void __launch_bounds__(CRT_TRACE_BLOCK) k_srp(SceneView sv, SrpArgs A, uint32_t* __restrict__ queue,
+                                                         uint32_t* __restrict__ err) {
+    extern __shared__ uint2 sstack[];
+    const int lane = threadIdx.x & 31;
+    const uint32_t tiles_x = (A.G + 7) >> 3;
+    const uint32_t total = A.n_att * A.grabs_per_att;
+    TravStats st{0u, 0u};
+    while (true) {
+        uint32_t g = 0;
+        if (lane == 0) g = atomicAdd(queue, 1u);
+        g = __shfl_sync(0xffffffffu, g, 0);
+        if (g >= total) break;
+        const uint32_t a = g / A.grabs_per_att;
+        const uint32_t t0 = (g % A.grabs_per_att) * CHUNK;
+        const uint32_t t1 = min(t0 + CHUNK, A.tiles);
+        const SrpAtt P = A.att[a];
+        double acc[6] = {0, 0, 0, 0, 0, 0};
+        for (uint32_t tile = t0; tile < t1; ++tile) {
+            const uint32_t px = (tile % tiles_x) * 8u + (lane & 7), py = (tile / tiles_x) * 4u + (lane >> 3);
+            bool alive = px < A.G && py < A.G;
+            TRay r;
+            r.o = f3(P.org[0] + px * P.du[0] + py * P.dv[0], P.org[1] + px * P.du[1] + py * P.dv[1],
+                     P.org[2] + px * P.du[2] + py * P.dv[2]);
+            r.d = f3(P.dir[0], P.dir[1], P.dir[2]);
+            r.tmin = 0.f;
+            r.tmax = 3.402823466e38f;
+            float E = P.E0;
+            for (uint32_t seg = 0; seg <= A.nb; ++seg) {
+                THit h;
+                h.slot = CRT_MISS;
+                if (alive) {
+                    h = traverse<false, false>(sv, r, sstack + threadIdx.x, CRT_TRACE_BLOCK, st, err);
+                    if (h.slot == CRT_MISS) alive = false;
+                }
+                __syncwarp();
+                const bool hit = h.slot != CRT_MISS;
+                float absorbed = 0.f;
+                uint32_t key = 0xFFFFFFFFu;
+                float3 n = f3(0.f, 0.f, 0.f), x = f3(0.f, 0.f, 0.f);
+                float rs = 0.f;
+                if (hit) {
+                    const SurfacePoint sp = surface_point(sv, h);
+                    const EntityDev& Ent = sv.entities[sp.entity];
+                    rs = Ent.rho_s;
+                    const float rd = Ent.rho_d;
+                    n = sp.flat_n * -1.0f;                       // outward for counter-clockwise meshes
+                    if (dot3(r.d, n) > 0.f) n = n * -1.0f;       // two-sided: face the incoming ray
+                    const float cs = -dot3(r.d, n);
+                    const float k1 = E * A.inv_c * (1.0f - rs);
+                    const float k2 = E * A.inv_c * (2.0f * rs * cs + (2.0f / 3.0f) * rd);
+                    const float3 dF = r.d * k1 - n * k2;
+                    x = sp.x;
+                    const float3 dT = cross3(x - f3(A.cm[0], A.cm[1], A.cm[2]), dF);
+                    acc[0] += dF.x; acc[1] += dF.y; acc[2] += dF.z;
+                    acc[3] += dT.x; acc[4] += dT.y; acc[5] += dT.z;
+                    absorbed = (1.0f - rs - rd) * E;
+                    key = __ldg(sv.leaf_prim + h.slot);
+                }
+                if (A.facet) {
+                    // warp-aggregated facet power: lanes hitting the same facet add once
+                    const uint32_t peers = __match_any_sync(0xffffffffu, key);
+                    double sum = 0.0;
+#pragma unroll 4
+                    for (int j = 0; j < 32; ++j) {
+                        const float v = __shfl_sync(0xffffffffu, absorbed, j);
+                        if ((peers >> j) & 1u) sum += (double)v;
+                    }
+                    if (key != 0xFFFFFFFFu && lane == __ffs(peers) - 1)
+                        atomicAdd(&A.facet[(size_t)a * A.n_tris + key], sum);
+                }
+                if (hit) {
+                    if (rs > 0.f && seg < A.nb) {
+                        const float3 dn = r.d - n * (2.0f * dot3(r.d, n));
+                        const float m = fmaxf(fabsf(x.x), fmaxf(fabsf(x.y), fabsf(x.z)));
+                        int e;
+                        frexpf(m, &e);
+                        const float off = fmaxf(1e-5f, ldexpf(1.0f, e - 24 + 3));
+                        r.o = x + n * off;
+                        r.d = dn;
+                        r.tmin = 0.f;
+                        r.tmax = 3.402823466e38f;
+                        r.skip = h.slot;
+                        E *= rs;
+                    } else {
+                        alive = false;
+                    }
+                }
+                if (!__any_sync(0xffffffffu, alive)) break;
+            }
+        }
+        for (int k = 0; k < 6; ++k)
+            for (int o = 16; o; o >>= 1) acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], o);
+        if (lane == 0)
+            for (int k = 0; k < 6; ++k) A.partial[6ull * g + k] = acc[k];
+    }
+}
+
+// one block per attitude, fixed-order tree sum of its partials
+__global__ void k_srp_reduce(const double* __restrict__ partial, uint32_t grabs_per_att, double* __restrict__ force,
+                             double* __restrict__ torque) {
+    __shared__ double sh[256][6];
+    const uint32_t a = blockIdx.x;
+    double acc[6] = {0, 0, 0, 0, 0, 0};
+    for (uint32_t g = threadIdx.x; g < grabs_per_att; g += blockDim.x)
+        for (int k = 0; k < 6; ++k) acc[k] += partial[6ull * ((size_t)a * grabs_per_att + g) + k];
+    for (int k = 0; k < 6; ++k) sh[threadIdx.x][k] = acc[k];
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if ((int)threadIdx.x < s)
+            for (int k = 0; k < 6; ++k) sh[threadIdx.x][k] += sh[threadIdx.x + s][k];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < 3; ++k) {
+            force[3ull * a + k] = sh[0][k];
+            torque[3ull * a + k] = sh[0][3 + k];
+        }
+    }
+}
+
+}  // namespace
+
+extern "C" int crt_srp(crt_scene* s, const crt_srp_desc* desc, const double* quats, size_t n_att, double* force,
+                       double* torque, double* facet_power) {
+    if (!s || !desc) return CRT_ERR_INVALID;
+    crt_context* ctx = s->ctx;
+    return crt_guard(ctx, [&] {
+        CRT_CHECK(n_att == 0 || (quats && force && torque), CRT_ERR_INVALID, "null buffer");
+        CRT_CHECK(desc->grid > 0 && desc->grid <= 65536, CRT_ERR_INVALID, "grid must be in [1, 65536]");
+        CRT_CHECK(desc->c > 0 && std::isfinite(desc->flux), CRT_ERR_INVALID, "bad flux or speed of light");
+        CRT_CHECK(desc->num_bounces <= 16, CRT_ERR_INVALID, "at most 16 specular bounces");
+        if (!n_att) return;
+        CRT_CUDA(cudaSetDevice(ctx->device));
+        cudaStream_t st = ctx->stream;
+        const double sl = std::sqrt(desc->sun_dir_inertial[0] * desc->sun_dir_inertial[0] +
+                                    desc->sun_dir_inertial[1] * desc->sun_dir_inertial[1] +
+                                    desc->sun_dir_inertial[2] * desc->sun_dir_inertial[2]);
+        CRT_CHECK(sl > 0 && std::isfinite(sl), CRT_ERR_INVALID, "sun direction must be a non-zero vector");
+        const double si[3] = {desc->sun_dir_inertial[0] / sl, desc->sun_dir_inertial[1] / sl,
+                              desc->sun_dir_inertial[2] / sl};
+        // body-frame box of the scene
+        double lo[3], hi[3], ctr[3];
+        for (int k = 0; k < 3; ++k) {
+            lo[k] = s->bounds[k];
+            hi[k] = s->bounds[3 + k];
+            ctr[k] = 0.5 * (lo[k] + hi[k]);
+        }
+        const double Rb = 0.5 * std::sqrt((hi[0] - lo[0]) * (hi[0] - lo[0]) + (hi[1] - lo[1]) * (hi[1] - lo[1]) +
+                                          (hi[2] - lo[2]) * (hi[2] - lo[2]));
+        const uint32_t G = desc->grid;
+        const double h = 2.0 * Rb / G;
+        std::vector<double> hq(4 * n_att);
+        if (is_device_ptr(quats)) {
+            CRT_CUDA(cudaMemcpy(hq.data(), quats, 32 * n_att, cudaMemcpyDeviceToHost));
+        } else {
+            std::copy(quats, quats + 4 * n_att, hq.begin());
+        }
+        std::vector<SrpAtt> att(n_att);
+        for (size_t a = 0; a < n_att; ++a) {
+            double w = hq[4 * a], x = hq[4 * a + 1], y = hq[4 * a + 2], z = hq[4 * a + 3];
+            const double qn = std::sqrt(w * w + x * x + y * y + z * z);
+            CRT_CHECK(qn > 0 && std::isfinite(qn), CRT_ERR_INVALID, "attitude quaternion must be non-zero");
+            w /= qn; x /= qn; y /= qn; z /= qn;
+            // R(q) maps body vectors into the inertial frame; s_b = R^T s_i
+            const double R[9] = {1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y),
+                                 2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x),
+                                 2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)};
+            double sb[3];
+            for (int k = 0; k < 3; ++k) sb[k] = R[k] * si[0] + R[3 + k] * si[1] + R[6 + k] * si[2];
+            // grid basis perpendicular to s_b (same construction as the oracle)
+            double ax[3] = {1, 0, 0};
+            if (std::fabs(sb[0]) >= 0.9) { ax[0] = 0; ax[1] = 1; }
+            double e1[3] = {sb[1] * ax[2] - sb[2] * ax[1], sb[2] * ax[0] - sb[0] * ax[2], sb[0] * ax[1] - sb[1] * ax[0]};
+            const double l1 = std::sqrt(e1[0] * e1[0] + e1[1] * e1[1] + e1[2] * e1[2]);
+            for (int k = 0; k < 3; ++k) e1[k] /= l1;
+            const double e2[3] = {sb[1] * e1[2] - sb[2] * e1[1], sb[2] * e1[0] - sb[0] * e1[2], sb[0] * e1[1] - sb[1] * e1[0]};
+            for (int k = 0; k < 3; ++k) {
+                const double o0 = ctr[k] + sb[k] * (2.0 * Rb + 1.0) + e1[k] * (-Rb + 0.5 * h) + e2[k] * (-Rb + 0.5 * h);
+                att[a].org[k] = (float)o0;
+                att[a].du[k] = (float)(e1[k] * h);
+                att[a].dv[k] = (float)(e2[k] * h);
+                att[a].dir[k] = (float)(-sb[k]);
+            }
+            att[a].E0 = (float)(desc->flux * h * h);
+            att[a].pad = 0.f;
+        }
+        const uint32_t tiles = ((G + 7) / 8) * ((G + 3) / 4);
+        const uint32_t gpa = (tiles + CHUNK - 1) / CHUNK;
+        // keep each launch's grab count well inside 32 bits
+        const size_t att_per_launch = std::max<size_t>(1, std::min<size_t>(n_att, (1u << 30) / gpa));
+        SrpAtt* d_att = (SrpAtt*)ctx_scratch(ctx, SCR_IN1, sizeof(SrpAtt) * n_att);
+        CRT_CUDA(cudaMemcpyAsync(d_att, att.data(), sizeof(SrpAtt) * n_att, cudaMemcpyHostToDevice, st));
+        double* d_partial = (double*)ctx_scratch(ctx, SCR_WAVE3, sizeof(double) * 6 * gpa * att_per_launch);
+        double* d_force = (double*)out_device(ctx, force, n_att * 24, SCR_OUT0);
+        double* d_torque = (double*)out_device(ctx, torque, n_att * 24, SCR_OUT1);
+        double* d_facet = facet_power ? (double*)out_device(ctx, facet_power, n_att * s->n_tris * 8, SCR_OUT2) : nullptr;
+        if (d_facet) CRT_CUDA(cudaMemsetAsync(d_facet, 0, n_att * s->n_tris * 8, st));
+        uint32_t* queue = (uint32_t*)ctx_scratch(ctx, SCR_QUEUE, 256);
+        const size_t smem = (size_t)CRT_STACK_SMEM * CRT_TRACE_BLOCK * sizeof(uint2);
+        const int grid = occupancy_grid(ctx, (const void*)k_srp, CRT_TRACE_BLOCK, smem);
+        const SceneView sv = scene_view(s);
+        for (size_t a0 = 0; a0 < n_att; a0 += att_per_launch) {
+            const size_t na = std::min(att_per_launch, n_att - a0);
+            SrpArgs A;
+            A.att = d_att + a0;
+            A.G = G;
+            A.tiles = tiles;
+            A.grabs_per_att = gpa;
+            A.n_att = (uint32_t)na;
+            A.inv_c = (float)(1.0 / desc->c);
+            for (int k = 0; k < 3; ++k) A.cm[k] = (float)desc->center_of_mass[k];
+            A.nb = desc->num_bounces;
+            A.partial = d_partial;
+            A.facet = d_facet ? d_facet + a0 * s->n_tris : nullptr;
+            A.n_tris = (uint32_t)s->n_tris;
+            CRT_CUDA(cudaMemsetAsync(queue, 0, sizeof(uint32_t), st));
+            k_srp<<<grid, CRT_TRACE_BLOCK, smem, st>>>(sv, A, queue, ctx->d_error);
+            check_launch(ctx, "k_srp");
+            k_srp_reduce<<<(uint32_t)na, 256, 0, st>>>(d_partial, gpa, d_force + 3 * a0, d_torque + 3 * a0);
+            check_launch(ctx, "k_srp_reduce");
+        }
+        out_finish(ctx, force, d_force, n_att * 24);
+        out_finish(ctx, torque, d_torque, n_att * 24);
+        if (facet_power) out_finish(ctx, facet_power, d_facet, n_att * s->n_tris * 8);
+        check_device_error(ctx, "crt_srp");
+    });
+}

@@ -1,0 +1,125 @@
+// Persistent trace-kernel template shared by every query, plus surface reconstruction helpers.
+#pragma once
+
+#include "common.cuh"
+#include "traverse.cuh"
+
+#ifndef CRT_TRACE_BLOCK
+#define CRT_TRACE_BLOCK 128
+#endif
+
+__host__ __device__ __forceinline__ SceneView scene_view(const crt_scene* s) {
+    SceneView v;
+    v.nodes = s->nodes;
+    v.tris = s->tris;
+    v.leaf_prim = s->leaf_prim;
+    v.leaf_vn = s->leaf_vn;
+    v.leaf_entity = s->leaf_entity;
+    v.entities = s->entities;
+    v.n_tris = (uint32_t)s->n_tris;
+    return v;
+}
+
+// SimpleCamera::pixel_to_ray in FP32 from the FP64-derived basis: d = normalize(a + u b + v c).
+__device__ __forceinline__ TRay camera_ray(const CamBasis& c, float u, float v) {
+    TRay r;
+    const float3 d = f3(fmaf(v, c.c[0], fmaf(u, c.b[0], c.a[0])), fmaf(v, c.c[1], fmaf(u, c.b[1], c.a[1])),
+                        fmaf(v, c.c[2], fmaf(u, c.b[2], c.a[2])));
+    r.d = normalize3(d);
+    r.o = f3(c.o[0], c.o[1], c.o[2]);
+    r.tmin = 0.f;
+    r.tmax = 3.402823466e38f;
+    return r;
+}
+
+struct SurfacePoint {
+    float3 x;           // u p1 + v p2 + (1-u-v) p0  (passes.hpp:53)
+    float3 flat_n;      // normalize(n), left-handed (inward) like the reference
+    float3 shading_n;   // smooth ? normalize(u vn1 + v vn2 + w vn0) : flat_n  (passes.hpp:179)
+    uint32_t entity;
+    uint32_t id;
+};
+
+__device__ __forceinline__ SurfacePoint surface_point(const SceneView& sv, const THit& h) {
+    SurfacePoint sp;
+    const float4* tp = sv.tris + 3ull * h.slot;
+    const float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
+    const float3 p0 = f3(a.x, a.y, a.z), e1 = f3(a.w, b.x, b.y), e2 = f3(b.z, b.w, c.x), n = f3(c.y, c.z, c.w);
+    // u (p0 - e1) + v (p0 + e2) + (1 - u - v) p0 = p0 - u e1 + v e2
+    sp.x = p0 - h.u * e1 + h.v * e2;
+    sp.flat_n = normalize3(n);
+    sp.entity = __ldg(sv.leaf_entity + h.slot);
+    const EntityDev& E = sv.entities[sp.entity];
+    sp.id = E.id;
+    if (E.smooth && sv.leaf_vn) {
+        const float4* vp = sv.leaf_vn + 3ull * h.slot;
+        const float4 v0 = __ldg(vp), v1 = __ldg(vp + 1), v2 = __ldg(vp + 2);
+        const float w = 1.0f - h.u - h.v;
+        sp.shading_n = normalize3(f3(h.u * v1.x + h.v * v2.x + w * v0.x, h.u * v1.y + h.v * v2.y + w * v0.y,
+                                     h.u * v1.z + h.v * v2.z + w * v0.z));
+    } else {
+        sp.shading_n = sp.flat_n;
+    }
+    return sp;
+}
+
+template <bool ANY, bool COUNT, class Job>
+__global__ void __launch_bounds__(CRT_TRACE_BLOCK) k_trace(SceneView sv, Job job, uint32_t n_items,
+                                                            const uint32_t* __restrict__ n_dev,
+                                                            uint32_t* __restrict__ queue, uint32_t* __restrict__ err,
+                                                            unsigned long long* __restrict__ counters) {
+    extern __shared__ uint2 sstack[];
+    if (n_dev) n_items = *n_dev;   // item count produced by an earlier kernel on the stream
+    const int lane = threadIdx.x & 31;
+    TravStats st{0u, 0u};
+    uint32_t nrays = 0;
+    while (true) {
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(queue, 32u);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= n_items) break;
+        const uint32_t i = base + lane;
+        TRay r;
+        if (i < n_items && job.ray(i, r)) {
+            const THit h = traverse<ANY, COUNT>(sv, r, sstack + threadIdx.x, CRT_TRACE_BLOCK, st, err);
+            job.write(sv, i, r, h);
+            if (COUNT) ++nrays;
+        }
+    }
+    if (COUNT) {
+        unsigned long long a = nrays, b = st.nodes, c = st.tris;
+        for (int o = 16; o; o >>= 1) {
+            a += __shfl_xor_sync(0xffffffffu, a, o);
+            b += __shfl_xor_sync(0xffffffffu, b, o);
+            c += __shfl_xor_sync(0xffffffffu, c, o);
+        }
+        if (lane == 0) {
+            atomicAdd(counters + 0, a);
+            atomicAdd(counters + 1, b);
+            atomicAdd(counters + 2, c);
+        }
+    }
+}
+
+// Launches the persistent trace kernel over n_items work items (or over *n_dev items when n_dev is
+// given: n_items is then the upper bound used to size the grid).
+template <bool ANY, class Job>
+void launch_trace(crt_scene* s, const Job& job, uint32_t n_items, const uint32_t* n_dev = nullptr,
+                  uint32_t* queue = nullptr) {
+    crt_context* ctx = s->ctx;
+    if (!queue) queue = (uint32_t*)ctx_scratch(ctx, SCR_QUEUE, 256);
+    CRT_CUDA(cudaMemsetAsync(queue, 0, sizeof(uint32_t), ctx->stream));
+    const size_t smem = (size_t)CRT_STACK_SMEM * CRT_TRACE_BLOCK * sizeof(uint2);
+    const void* kfn = ctx->counting ? (const void*)k_trace<ANY, true, Job> : (const void*)k_trace<ANY, false, Job>;
+    int grid = occupancy_grid(ctx, kfn, CRT_TRACE_BLOCK, smem);
+    const uint32_t need = (n_items + CRT_TRACE_BLOCK - 1) / CRT_TRACE_BLOCK;
+    if ((uint32_t)grid > need) grid = (int)std::max<uint32_t>(need, 1u);
+    const SceneView sv = scene_view(s);
+    if (ctx->counting)
+        k_trace<ANY, true, Job><<<grid, CRT_TRACE_BLOCK, smem, ctx->stream>>>(sv, job, n_items, n_dev, queue,
+                                                                             ctx->d_error, ctx->d_counters);
+    else
+        k_trace<ANY, false, Job><<<grid, CRT_TRACE_BLOCK, smem, ctx->stream>>>(sv, job, n_items, n_dev, queue,
+                                                                              ctx->d_error, ctx->d_counters);
+    check_launch(ctx, "k_trace");
+}

@@ -1,0 +1,216 @@
+/* crt_gpu.h -- C ABI of the GB300 ray-query library (libcrt_gpu.so).
+ *
+ * This is the drop-in boundary for the ray-query hot path of ceres-raytracer (CRT v0.6a4): BVH
+ * construction, closest-hit and any-hit traversal with ray/triangle intersection, and the
+ * integrators built on them (primary-ray passes, LiDAR, unidirectional path tracing, solar
+ * radiation pressure).  The reference implements this path as C++ templates behind its pybind11
+ * module `_crt` (src/pybind.cpp); each entry point below cites the reference function it replaces.
+ *
+ * Conventions
+ *  - Every function returns an int status: CRT_OK (0) or a negative CRT_ERR_* code;
+ *    crt_context_last_error() returns the message of the last failure on that context.
+ *  - Plain pointers and sizes only.  Input and output buffers may live in host memory or in device
+ *    memory of the context's GPU: the library inspects each pointer and copies host buffers itself.
+ *    Calls are synchronous with respect to host buffers; device-buffer outputs are ordered on the
+ *    context stream (see crt_context_set_stream).
+ *  - Geometry is FP32 on the device; camera, LiDAR, light and body-frame inputs are FP64 as in the
+ *    reference and are reduced to FP32 rays once per request on the host.  Radiation-pressure sums
+ *    are FP64.
+ *  - A context (and every scene created on it) must not be used from two threads at once.
+ */
+#ifndef CRT_GPU_H
+#define CRT_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CRT_ABI_VERSION 1
+
+enum {
+    CRT_OK = 0,
+    CRT_ERR_INVALID = -1,   /* bad argument, shape or state                              */
+    CRT_ERR_CUDA = -2,      /* CUDA runtime error (message in crt_context_last_error)     */
+    CRT_ERR_OOM = -3,       /* device or host allocation failed / over the memory budget  */
+    CRT_ERR_TIMEOUT = -4,   /* a bounded device wait or a host deadline expired           */
+    CRT_ERR_IO = -5,        /* file could not be read                                     */
+    CRT_ERR_DEVICE = -6,    /* a device-side check failed (e.g. traversal stack overflow) */
+    CRT_ERR_NO_DEVICE = -7  /* no CUDA device / the library was built for another GPU      */
+};
+
+#define CRT_MISS 0xFFFFFFFFu   /* primitive index reported for a ray that hits nothing */
+
+typedef struct crt_context crt_context;
+typedef struct crt_scene crt_scene;
+typedef struct crt_mesh crt_mesh;
+
+/* A ray: bvh::Ray (lib/bvh/ray.hpp:10-23) in FP32, 32 bytes.  Hits are accepted for
+ * tmin <= t <= tmax (inclusive, lib/bvh/triangle.hpp:155). */
+typedef struct {
+    float o[3];
+    float tmin;
+    float d[3];
+    float tmax;
+} crt_ray;
+
+/* Closest hit: ClosestPrimitiveIntersector::Result (lib/bvh/primitive_intersectors.hpp:37-42), 16 bytes.
+ * prim is the index into the scene's triangle list (entities concatenated in order, each entity's
+ * triangles in file order), or CRT_MISS. */
+typedef struct {
+    float t, u, v;
+    uint32_t prim;
+} crt_hit;
+
+/* One entity placed in a scene: Entity (src/crt/rendering_dynamic/entity.hpp:21-86) with its pose.
+ * The library applies resize -> rotate -> translate in FP64 as transform.hpp:43-85 does. */
+typedef struct {
+    const float* tri_xyz;     /* n_tris * 9: p0, p1, p2 (host or device memory) */
+    const float* tri_vn;      /* n_tris * 9 vertex normals, or NULL (only used with smooth shading) */
+    size_t n_tris;
+    double scale;
+    double position[3];
+    double rotation[9];       /* row-major 3x3 */
+    float color[3];           /* ColoredLambertianMaterial colour (entity.hpp:52) */
+    int smooth_shading;
+    uint32_t id;              /* instance id reported by the instance pass */
+    float rho_s, rho_d;       /* specular / diffuse reflectivity (radiation pressure only) */
+} crt_entity_desc;
+
+/* SimpleCamera (src/crt/cameras/simple_camera.hpp:14-81) */
+typedef struct {
+    double position[3];
+    double rotation[9];       /* row-major; directions go to the world frame through its transpose */
+    double focal_length;
+    double resolution[2];
+    double sensor_size[2];
+    int z_positive;
+} crt_camera_desc;
+
+/* PointLight (lights/point_light.hpp) when type == 0, AreaLight (lights/area_light.hpp) when 1 */
+typedef struct {
+    int type;
+    double intensity;
+    double position[3];
+    double rotation[9];
+    double size[2];
+} crt_light_desc;
+
+/* Arguments of BodyFixedGroup.render (src/pybind.cpp:467-498) plus the random stream identity. */
+typedef struct {
+    int min_samples;
+    int max_samples;
+    double noise_threshold;
+    int num_bounces;
+    uint64_t seed;            /* Philox key; results do not depend on how requests are batched */
+    uint32_t request;         /* Philox counter word distinguishing requests with the same seed */
+} crt_render_params;
+
+/* LiDAR beam grid (extension of SimpleLidar, lidars/simple_lidar.hpp:42-64, to nx * ny beams).
+ * Beam (i, j) points along normalize(tan_x[i], tan_y[j], +-1) in the sensor frame with
+ * tan_x[i] = tan(-half_x + (i + 0.5) * 2 half_x / nx) (same for y), i.e. angles uniform over
+ * [-half, half]; the world direction is R^T of that, as for the reference boresight. */
+typedef struct {
+    double position[3];
+    double rotation[9];
+    int z_positive;
+    uint32_t nx, ny;
+    double half_angle_x, half_angle_y;   /* radians */
+} crt_lidar_grid_desc;
+
+/* Solar radiation pressure over a parallel sun-ray grid (no counterpart in the reference). */
+typedef struct {
+    double sun_dir_inertial[3];   /* unit vector toward the sun in the inertial frame */
+    double flux;                  /* W / m^2 at the body */
+    double c;                     /* m / s */
+    double center_of_mass[3];     /* body frame */
+    uint32_t grid;                /* grid x grid rays per attitude */
+    uint32_t num_bounces;         /* specular continuation segments after the primary hit */
+} crt_srp_desc;
+
+typedef struct {
+    size_t n_tris;
+    size_t n_nodes;           /* 8-wide compressed nodes */
+    size_t n_entities;
+    uint32_t depth;           /* levels of the 8-wide tree */
+    double build_ms;          /* device time of the last build */
+    size_t device_bytes;      /* resident bytes held by the scene */
+    float bounds[6];          /* xmin, ymin, zmin, xmax, ymax, zmax */
+} crt_scene_stats;
+
+typedef struct {
+    uint64_t rays;            /* rays traversed by counting-mode kernels */
+    uint64_t nodes;           /* 8-wide nodes fetched */
+    uint64_t tris;            /* triangles tested */
+    uint64_t launches;        /* kernels launched by the library on this context (always counted) */
+} crt_counters;
+
+/* ---------------------------------------------------------------- context */
+int crt_context_create(int device, crt_context** out);
+int crt_context_destroy(crt_context* ctx);
+/* Order all work of this context on `stream` (a cudaStream_t); NULL restores the context's own. */
+int crt_context_set_stream(crt_context* ctx, void* stream);
+void* crt_context_get_stream(crt_context* ctx);
+int crt_context_synchronize(crt_context* ctx);
+/* Counting mode: traversal kernels also count node fetches and triangle tests (slower). */
+int crt_context_set_counting(crt_context* ctx, int enabled);
+int crt_context_get_counters(crt_context* ctx, crt_counters* out);
+int crt_context_reset_counters(crt_context* ctx);
+const char* crt_context_last_error(const crt_context* ctx);
+const char* crt_status_string(int status);
+int crt_abi_version(void);
+
+/* ---------------------------------------------------------------- meshes (host) */
+/* obj::load_from_file (lib/model_loaders/obj.hpp:59-127): `v` lines via strtof, `f` lines
+ * fan-triangulated, negative indices allowed, vertex normals = normalised sums of left-handed face
+ * normals.  Used by Entity's constructor (entity.hpp:31-41). */
+int crt_mesh_load_obj(const char* path, crt_mesh** out);
+size_t crt_mesh_num_tris(const crt_mesh* mesh);
+const float* crt_mesh_xyz(const crt_mesh* mesh);       /* n_tris * 9 */
+const float* crt_mesh_normals(const crt_mesh* mesh);   /* n_tris * 9 */
+void crt_mesh_destroy(crt_mesh* mesh);
+
+/* ---------------------------------------------------------------- scenes */
+/* Upload, transform and build the device-resident BVH: replaces the scene assembly and BVH build of
+ * BodyFixedGroup (rendering_body_fixed/body_fixed_group.hpp:45-89) and of the per-call rebuild in
+ * rendering_dynamic/render.hpp:14-66 (SweepSahBuilder + ParallelReinsertionOptimizer +
+ * NodeLayoutOptimizer, lib/bvh/sweep_sah_builder.hpp:43).  The GPU builder is Morton / LBVH /
+ * 8-wide collapse; results of queries do not depend on the tree. */
+int crt_scene_create(crt_context* ctx, const crt_entity_desc* entities, uint32_t n_entities, crt_scene** out);
+int crt_scene_destroy(crt_scene* scene);
+int crt_scene_get_stats(const crt_scene* scene, crt_scene_stats* out);
+
+/* ---------------------------------------------------------------- ray queries */
+/* SingleRayTraverser::traverse + ClosestPrimitiveIntersector (lib/bvh/single_ray_traverser.hpp:145,
+ * primitive_intersectors.hpp:33-54). */
+int crt_trace_closest(crt_scene* scene, const crt_ray* rays, size_t n, crt_hit* hits);
+/* SingleRayTraverser::traverse + AnyPrimitiveIntersector (primitive_intersectors.hpp:58-76). */
+int crt_trace_any(crt_scene* scene, const crt_ray* rays, size_t n, uint8_t* occluded);
+
+/* ---------------------------------------------------------------- integrators */
+/* get_inetersections / get_instances / get_normals (src/crt/passes.hpp:14-198), fused over one
+ * traversal per pixel; any output may be NULL.  xyz and normals are [H][W][3] doubles, ids [H][W]. */
+int crt_passes(crt_scene* scene, const crt_camera_desc* camera, double* xyz, uint32_t* ids, double* normals);
+/* do_batch_lidar (src/crt/do_lidar.hpp:80-155) with SimpleLidar::batch_cast_rays
+ * (lidars/simple_lidar.hpp:66-96): one boresight ray per pose, range = |hit - position|, 0 on a
+ * miss.  positions n*3, rotations n*9 (row-major per pose).  prim may be NULL. */
+int crt_lidar_batch(crt_scene* scene, const double* positions, const double* rotations, size_t n,
+                    int z_positive, double* range, uint32_t* prim);
+/* nx * ny beam grid from one pose; range and prim are [ny][nx]; prim may be NULL. */
+int crt_lidar_grid(crt_scene* scene, const crt_lidar_grid_desc* desc, double* range, uint32_t* prim);
+/* do_render (src/crt/do_render.hpp:28-141) with unidirectional (path_tracing/unidirectional.hpp:24-96):
+ * rgba8 is [H][W][4] (clamp(v*256, 0, 255)), radiance (optional) the float RGBA before quantisation. */
+int crt_render(crt_scene* scene, const crt_camera_desc* camera, const crt_light_desc* lights, uint32_t n_lights,
+               const crt_render_params* params, uint8_t* rgba8, float* radiance);
+/* Solar radiation pressure for n_att attitudes (unit quaternions w,x,y,z rotating body vectors into the
+ * inertial frame).  force and torque are n_att*3 in the body frame (N, N m); facet_power (optional)
+ * is n_att * n_tris absorbed power per triangle (W).  No reference counterpart (README.md:9). */
+int crt_srp(crt_scene* scene, const crt_srp_desc* desc, const double* quaternions, size_t n_att, double* force,
+            double* torque, double* facet_power);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -234,6 +234,9 @@ def make_asteroid(R, D, tmp):
     # a quarter of the rays get a finite tmax (shadow-style queries)
     q = n // 4
     rays[:q, 7] = rng.uniform(1000.0, 5000.0, size=q)
+    # FP32-representable origins, directions and bounds: an FP32 tracer sees the very same rays
+    rays[:, :7] = rays[:, :7].astype(np.float32).astype(np.float64)
+    rays[:q, 7] = rays[:q, 7].astype(np.float32).astype(np.float64)
     out["rays"] = rays
     h = driver_scene(D, ents, paths)
     out["ref_tris"] = np.empty(0)

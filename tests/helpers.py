@@ -94,24 +94,78 @@ def scene_extent(tris12):
     return float(np.sqrt(((hi - lo) ** 2).sum()))
 
 
+def line_segment_distance(o, d, a, b):
+    """Distance between the line o + s d and the segment [a, b] (row-wise)."""
+    e = b - a
+    w = a - o
+    dd = (d * d).sum(-1)
+    de = (d * e).sum(-1)
+    ee = np.maximum((e * e).sum(-1), 1e-300)
+    dw = (d * w).sum(-1)
+    ew = (e * w).sum(-1)
+    den = dd * ee - de * de
+    with np.errstate(divide="ignore", invalid="ignore"):
+        t = np.where(den > 1e-300 * dd * ee, (de * dw - dd * ew) / den, 0.0)
+    t = np.clip(t, 0.0, 1.0)
+    s = (dw + t * de) / np.maximum(dd, 1e-300)
+    q = w + t[:, None] * e - s[:, None] * d
+    return np.sqrt((q * q).sum(-1))
+
+
+def ray_edge_distance(tris12, prim, rays):
+    """Distance between each ray's line and the nearest edge of triangle prim: how close the ray
+    passes to the triangle's boundary (independent of the incidence angle)."""
+    p0, p1, p2 = tri_vertices(tris12[prim])
+    o, d = rays[:, 0:3], rays[:, 3:6]
+    return np.minimum(np.minimum(line_segment_distance(o, d, p0, p1), line_segment_distance(o, d, p1, p2)),
+                      line_segment_distance(o, d, p2, p0))
+
+
+def point_near_any_edge(tris12, points, eps):
+    """True where a point lies within eps of an edge of any triangle (brute force over the triangles
+    whose box contains the point, for the few pixels that need it).  Covers rays through a shared
+    edge that one side reports as a miss (the Moeller-Trumbore test is not watertight)."""
+    p0, p1, p2 = tri_vertices(tris12)
+    lo = np.minimum(np.minimum(p0, p1), p2)
+    hi = np.maximum(np.maximum(p0, p1), p2)
+    out = np.zeros(len(points), dtype=bool)
+    for k, (x, e) in enumerate(zip(points, np.broadcast_to(eps, (len(points),)))):
+        cand = np.nonzero(((lo - e) <= x).all(1) & (x <= (hi + e)).all(1))[0]
+        if len(cand) == 0:
+            continue
+        xx = np.broadcast_to(x, (len(cand), 3))
+        d = np.minimum(np.minimum(point_segment_distance(xx, p0[cand], p1[cand]),
+                                  point_segment_distance(xx, p1[cand], p2[cand])),
+                       point_segment_distance(xx, p2[cand], p0[cand]))
+        out[k] = (d <= e).any()
+    return out
+
+
 def excused_id_mismatch(tris12, rays, prim_a, t_a, prim_b, t_b):
-    """Boolean mask of ID mismatches that the parity rule excuses: the hit point of either side lies
-    within EDGE_REL*(|origin| + extent) of an edge of its own triangle, or both sides hit at the same
-    distance (coplanar ties), or one side misses while the other grazes an edge."""
+    """Boolean mask of ID mismatches that the parity rule excuses: the ray passes within
+    EDGE_REL * (|origin| + scene extent) of an edge of the triangle hit on either side (exact ties
+    on shared edges, and FP32 rounding of rays that graze a triangle boundary), or both sides hit
+    at the same distance (coplanar overlapping triangles)."""
     ext = scene_extent(tris12)
     o = rays[:, 0:3]
     eps = EDGE_REL * (np.sqrt((o * o).sum(-1)) + ext)
-    d = rays[:, 3:6]
     ok = np.zeros(len(prim_a), dtype=bool)
-    for prim, t in ((prim_a, t_a), (prim_b, t_b)):
-        has = prim >= 0
-        idx = np.nonzero(has)[0]
+    for prim in (prim_a, prim_b):
+        idx = np.nonzero(prim >= 0)[0]
         if len(idx):
-            pts = o[idx] + t[idx, None] * d[idx]
-            ok[idx] |= edge_distance(tris12, prim[idx], pts) <= eps[idx] + DIST_REL * np.abs(t[idx]) * 0.0
+            ok[idx] |= ray_edge_distance(tris12, prim[idx], rays[idx]) <= eps[idx]
     both = (prim_a >= 0) & (prim_b >= 0)
     ok |= both & (np.abs(t_a - t_b) <= DIST_REL * np.maximum(np.abs(t_a), 1e-30))
     return ok
+
+
+def to_f32_rays(rays64):
+    """Round FP64 rays to FP32-representable values (kept as float64), so that an FP32 tracer and
+    an FP64 one see bit-identical rays."""
+    with np.errstate(over="ignore"):
+        r = rays64.astype(np.float32).astype(np.float64)
+    r[:, 7] = np.where(rays64[:, 7] > 3.0e38, np.finfo(np.float64).max, r[:, 7])
+    return r
 
 
 def rel_err(a, b, scale=None):

@@ -1,0 +1,102 @@
+"""Host-side logic of the drop-in `crt` package (no GPU): body-frame transforms, LiDAR pose batches,
+the `_crt` module surface and argument handling."""
+import numpy as np
+import pytest
+
+from crt_gb300 import scenes
+
+
+def reference_transform_to_body(group_pos, group_rot, scale, position, rotation):
+    # crt/body_fixed.py:87-101 of the reference, written out
+    relative_position = scale * np.matmul(group_rot, position - group_pos)
+    relative_rotation = np.matmul(group_rot, rotation.T).T
+    return relative_position, relative_rotation
+
+
+class FakeCpp:
+    def __init__(self):
+        self.calls = []
+
+    def __getattr__(self, name):
+        def f(*a, **k):
+            self.calls.append((name, a, k))
+            return np.zeros((1, 3))
+        return f
+
+
+def make_group(pos, rot, scale=1.0):
+    import crt
+    g = crt.BodyFixedGroup.__new__(crt.BodyFixedGroup)
+    g.position, g.rotation, g.scale = np.asarray(pos, float), np.asarray(rot, float), scale
+    g._cpp = FakeCpp()
+    return g
+
+
+def test_module_surface_matches_reference():
+    import _crt
+    names = {n for n in dir(_crt) if not n.startswith("_")}
+    assert {"AreaLight", "BodyFixedEntity", "BodyFixedGroup", "Entity", "PointLight", "SimpleCamera", "SimpleLidar",
+            "instance_pass", "intersection_pass", "normal_pass", "render", "simulate_lidar"} <= names
+    import crt
+    assert set(crt.__all__) == {"Entity", "RigidBody", "BodyFixedGroup", "BodyFixedEntity"}
+
+
+def test_transform_to_body_matches_reference_formula():
+    rng = np.random.Generator(np.random.PCG64(3))
+    R = scenes.quaternion_to_matrix(scenes.random_quaternions(1, 5)[0])
+    g = make_group(rng.normal(size=3), R, scale=2.5)
+    p, r = rng.normal(size=3), scenes.quaternion_to_matrix(scenes.random_quaternions(1, 6)[0])
+    a = g.transform_to_body(p, r)
+    b = reference_transform_to_body(g.position, g.rotation, g.scale, p, r)
+    np.testing.assert_allclose(a[0], b[0], rtol=1e-14)
+    np.testing.assert_allclose(a[1], b[1], rtol=1e-14, atol=1e-15)
+
+
+def test_batch_lidar_poses_match_per_pose_transform():
+    from crt.lidars import SimpleLidar
+    rng = np.random.Generator(np.random.PCG64(4))
+    R = scenes.quaternion_to_matrix(scenes.random_quaternions(1, 7)[0])
+    g = make_group(rng.normal(size=3), R, scale=0.5)
+    n = 17
+    pos = rng.normal(size=(n, 3)) * 100
+    rots = np.stack([scenes.quaternion_to_matrix(q) for q in scenes.random_quaternions(n, 8)], axis=2)
+    lid = SimpleLidar()
+    lid.batch_set_pose(pos, rots)
+    g.batch_simulate_lidar(lid)
+    # the lidar now holds body-frame poses; compare with the reference's per-pose loop (body_fixed.py:152-162)
+    for k in range(n):
+        p_ref, r_ref = reference_transform_to_body(g.position, g.rotation, g.scale, pos[k], rots[:, :, k])
+        np.testing.assert_allclose(lid.batch_positions[k], p_ref, rtol=1e-13, atol=1e-12)
+        np.testing.assert_allclose(lid.batch_rotations[:, :, k], r_ref, rtol=1e-13, atol=1e-14)
+
+
+def test_render_moves_camera_and_lights_into_body_frame():
+    from crt.cameras import SimpleCamera
+    from crt.lights import AreaLight, PointLight
+    R = scenes.quaternion_to_matrix(scenes.random_quaternions(1, 9)[0])
+    g = make_group([1.0, 2.0, 3.0], R)
+    cam = SimpleCamera(1.0, [8, 8], [1.0, 1.0], position=[10.0, 0.0, 0.0])
+    p_exp, r_exp = g.transform_to_body(cam.position, cam.rotation)
+    lights = [PointLight(5.0, position=[0.0, 9.0, 0.0]), AreaLight(2.0, [1.0, 2.0])]
+    g.render(cam, lights, 1, 2, 0.5, 3)
+    np.testing.assert_allclose(cam.position, p_exp)
+    np.testing.assert_allclose(cam.rotation, r_exp)
+    name, args, kw = g._cpp.calls[-1]
+    assert name == "render" and args[2:] == (1, 2, 0.5, 3) and len(args[1]) == 2
+
+
+def test_lidar_batch_limit_and_shapes():
+    from crt.lidars import SimpleLidar
+    lid = SimpleLidar()
+    with pytest.raises(ValueError):
+        lid.batch_set_pose(np.zeros((100001, 3)), np.zeros((3, 3, 100001)))
+    with pytest.raises(ValueError):
+        SimpleLidar(position=[1.0, 2.0])
+
+
+def test_rotations_module():
+    from crt.rotations import euler_to_rotmat
+    R = euler_to_rotmat("123", [10, 20, 30], degrees=True)
+    np.testing.assert_allclose(R @ R.T, np.eye(3), atol=1e-14)
+    with pytest.raises(Exception):
+        euler_to_rotmat("124", [0, 0, 0])

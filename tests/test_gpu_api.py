@@ -1,0 +1,117 @@
+"""The drop-in `crt` package: the reference's Python calls, unchanged, against the reference's outputs.
+
+Scenes are written as OBJ files and loaded through crt.BodyFixedEntity / crt.Entity, exactly as a
+reference user would; outputs are compared with the fixtures the reference produced on the same
+files (tests/golden/).
+"""
+import numpy as np
+import pytest
+
+from helpers import DIST_REL, camera_from, entities_from, load_golden
+
+pytestmark = pytest.mark.gpu
+
+
+def crt_objects(d, tmp_path, dynamic=False):
+    import crt
+    from crt.cameras import SimpleCamera
+    ents = entities_from(d)
+    objs = []
+    for i, e in enumerate(ents):
+        p = str(tmp_path / f"{i}.obj")
+        e.mesh.write_obj(p)
+        cls = crt.Entity if dynamic else crt.BodyFixedEntity
+        objs.append(cls(p, color=list(e.color), smooth_shading=e.smooth, position=e.position, rotation=e.rotation,
+                        scale=e.scale))
+    cam = camera_from(d)
+    camera = SimpleCamera(cam["focal_length"], cam["resolution"], cam["sensor_size"], cam["z_positive"],
+                          position=cam["position"], rotation=cam["rotation"])
+    return objs, camera
+
+
+def agree(ids, ref_ids, xyz, ref_xyz, normals, ref_n):
+    mism = ids != ref_ids
+    assert mism.mean() < 0.01, mism.mean()
+    ok = ~mism & (ref_ids > 0)
+    # FP32 traversal vs FP64: identical on all but near-edge pixels, whose points lie on either side
+    scale = np.maximum(np.linalg.norm(ref_xyz, axis=-1), 1e-30)
+    rel = np.linalg.norm(xyz - ref_xyz, axis=-1)[ok] / scale[ok]
+    assert np.quantile(rel, 0.99) < DIST_REL
+    assert np.quantile(np.abs(normals - ref_n).max(-1)[ok], 0.99) < DIST_REL
+
+
+@pytest.mark.parametrize("name", ["cornell", "asteroid"])
+def test_body_fixed_group_passes(name, tmp_path):
+    import crt
+    d = load_golden(name)
+    objs, camera = crt_objects(d, tmp_path)
+    group = crt.BodyFixedGroup(objs)
+    ids = group.instance_pass(camera)
+    xyz = group.intersection_pass(camera)
+    nrm = group.normal_pass(camera)
+    assert ids.dtype == np.uint32 and xyz.dtype == np.float64 and xyz.shape == d["bf_xyz"].shape
+    agree(ids, d["bf_ids"], xyz, d["bf_xyz"], nrm, d["bf_normals"])
+    ids2, img = group.instance_pass(camera, return_image=True)
+    assert img.shape == ids.shape + (3,)
+
+
+def test_dynamic_rendering_functions(tmp_path):
+    from crt import rendering
+    d = load_golden("cornell")
+    objs, camera = crt_objects(d, tmp_path, dynamic=True)
+    ids = rendering.instance_pass(camera, objs)
+    xyz = rendering.intersection_pass(camera, objs)
+    nrm = rendering.normal_pass(camera, objs)
+    agree(ids, d["dyn_ids"], xyz, d["dyn_xyz"], nrm, d["dyn_normals"])
+
+
+def test_render_and_lidar_through_api(tmp_path):
+    import crt
+    from crt.lidars import SimpleLidar
+    from crt.lights import PointLight
+    d = load_golden("asteroid")
+    objs, camera = crt_objects(d, tmp_path)
+    group = crt.BodyFixedGroup(objs)
+    light = PointLight(1.0e18, position=1.0e9 * np.array([0.6, 0.0, 0.8]))
+    img = group.render(camera, light, 1, 1, 1.0, 1)
+    assert img.dtype == np.uint8 and img.shape == (64, 64, 4) and (img[..., 3] == 255).all()
+    img2, rad = group.render(camera, [light], 1, 1, 1.0, 1, return_radiance=True)
+    np.testing.assert_array_equal(img, img2)
+    # batch LiDAR with the reference's (3, 3, n) rotation layout
+    lidar = SimpleLidar()
+    pos, rot = d["lidar_pos"], d["lidar_rot"]
+    lidar.batch_set_pose(pos, np.transpose(rot, (1, 2, 0)))
+    rng = group.batch_simulate_lidar(lidar)
+    assert rng.shape == (1, len(pos))
+    ref = d["lidar_range"]
+    both = (rng[0] > 0) & (ref > 0)
+    assert ((rng[0] > 0) != (ref > 0)).mean() < 0.01
+    np.testing.assert_allclose(rng[0][both], ref[both], rtol=DIST_REL)
+    # single-pose LiDAR equals the first batch pose
+    single = SimpleLidar(position=pos[0], rotation=rot[0])
+    assert abs(group.simulate_lidar(single) - rng[0, 0]) <= DIST_REL * max(rng[0, 0], 1.0)
+    # beam-grid extension
+    scan = SimpleLidar(position=pos[1], rotation=rot[1])
+    scan.set_beam_grid(32, 16, np.deg2rad(4), np.deg2rad(2))
+    r2, p2 = group.lidar_scan(scan)
+    assert r2.shape == (16, 32) and p2.dtype == np.uint32
+    assert ((r2 == 0) == (p2 == 0xFFFFFFFF)).all()
+
+
+def test_transform_to_body_moves_queries(tmp_path):
+    """A group pose is applied to cameras through transform_to_body (body_fixed.py:87-101)."""
+    import crt
+    from crt.cameras import SimpleCamera
+    d = load_golden("cornell")
+    objs, camera = crt_objects(d, tmp_path)
+    group = crt.BodyFixedGroup(objs)
+    ref_ids = group.instance_pass(camera)
+    # rotate the group by 90 deg about z and move it; rotate/move the camera with it
+    Rz = np.array([[0.0, -1.0, 0.0], [1.0, 0.0, 0.0], [0.0, 0.0, 1.0]])
+    t = np.array([10.0, -3.0, 2.0])
+    group.set_pose(t, Rz)
+    cam = camera_from(d)
+    cam2 = SimpleCamera(cam["focal_length"], cam["resolution"], cam["sensor_size"], cam["z_positive"],
+                        position=Rz.T @ cam["position"] + t, rotation=cam["rotation"] @ Rz)
+    ids = group.instance_pass(cam2)
+    assert (ids != ref_ids).mean() < 0.01

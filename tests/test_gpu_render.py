@@ -1,0 +1,113 @@
+"""GPU wavefront path tracer vs the reference fixtures and the FP64 oracle, through the C ABI.
+
+* 1 spp at pixel corners, 1 bounce, point light: no random draws; radiance equals the reference's
+  within FP32 rounding except where a shading term crosses zero or a shadow edge moves.
+* Same seed as the oracle: both draw the same Philox streams, so per-pixel radiance agrees closely
+  (paths diverge only where FP32 and FP64 take different branches).
+* Area light, 512 spp, 3 bounces vs the reference's own path tracer (different random streams):
+  per pixel within 4 sigma, image mean within 0.5 % (pixels next to the light plane excluded, see
+  test_oracle_golden.test_area_light_render_statistics).
+"""
+import numpy as np
+import pytest
+
+import oracle
+from crt_gb300 import lib, scenes
+from helpers import camera_from, entities_from, lights_from, load_golden, radiance_stats_ok
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    c = lib.Context(0)
+    yield c
+    c.close()
+
+
+@pytest.fixture(scope="module")
+def cornell(ctx):
+    d = load_golden("cornell")
+    ents = entities_from(d)
+    return d, ents, ctx.scene(ents), oracle.Scene(ents)
+
+
+def test_point_light_deterministic(cornell):
+    d, ents, sc, o = cornell
+    cam = camera_from(d, "rcam")
+    lights = lights_from(d["point_lights"])
+    rgba, rad = sc.render(cam, lights, 1, 1, 0.0, 1)
+    ref = d["point_radiance"]
+    close = np.isclose(rad[..., :3], ref, rtol=1e-4, atol=1e-5).all(-1)
+    assert close.mean() > 0.99, close.mean()
+    # a pixel whose shadow ray grazes an edge may flip between lit and shadowed: image mean 0.5 %
+    assert abs(rad[..., :3].mean() / ref.mean() - 1) < 5e-3
+    assert (rad[..., 3] == 1).all()
+    # quantisation: clamp(v * 256, 0, 255) truncated to uint8 (do_render.hpp:118-134)
+    np.testing.assert_array_equal(rgba, np.clip(rad * 256, 0, 255).astype(np.uint8))
+
+
+def test_same_seed_matches_oracle(cornell):
+    d, ents, sc, o = cornell
+    cam = dict(camera_from(d, "rcam"), resolution=[32, 32])
+    lights = lights_from(d["lights"])
+    _, rad = sc.render(cam, lights, 8, 8, 0.0, 3, seed=5)
+    orad, _, _ = o.render(cam, lights, 8, 8, 0.0, 3, seed=5)
+    rel = np.abs(rad[..., :3] - orad[..., :3]) / np.maximum(np.abs(orad[..., :3]), 1e-3)
+    assert (rel < 1e-3).mean() > 0.9, (rel < 1e-3).mean()
+    assert abs(rad[..., :3].mean() / orad[..., :3].mean() - 1) < 0.01
+
+
+def test_area_light_statistics_vs_reference(cornell):
+    d, ents, sc, o = cornell
+    cam = camera_from(d, "rcam")
+    spp, bounces = int(d["render_spp"]), int(d["render_bounces"])
+    _, rad = sc.render(cam, lights_from(d["lights"]), spp, spp, 0.0, bounces, seed=1)
+    xyz, ids, _, _ = o.passes(cam)
+    mask = ~((ids == 1) & (xyz[..., 1] > 0.94)) & (ids != 6) & (ids > 0)
+    ref, m2 = d["render_mean"], d["render_m2"]
+    z = radiance_stats_ok(rad[..., :3], m2, spp, ref, m2, spp, mask=np.repeat(mask[..., None], 3, -1))
+    assert (z > 4).mean() < 0.01, (z > 4).mean()
+    ours, theirs = rad[..., :3][mask].mean(), ref[mask].mean()
+    assert abs(ours / theirs - 1) < 0.005, (ours, theirs)
+
+
+def test_adaptive_sampling_matches_oracle(cornell):
+    d, ents, sc, o = cornell
+    cam = dict(camera_from(d, "rcam"), resolution=[24, 24])
+    lights = lights_from(d["lights"])
+    _, rad = sc.render(cam, lights, 2, 32, 2.0, 2, seed=9)
+    orad, _, taken = o.render(cam, lights, 2, 32, 2.0, 2, seed=9)
+    # the same random streams stop most pixels after the same sample
+    assert taken.min() >= 2 and taken.max() <= 32 and (taken < 32).any()
+    close = np.isclose(rad[..., :3], orad[..., :3], rtol=2e-3, atol=1e-3).all(-1)
+    assert close.mean() > 0.9, close.mean()
+
+
+def test_multiple_lights_and_no_bounce(cornell):
+    d, ents, sc, o = cornell
+    cam = dict(camera_from(d, "rcam"), resolution=[16, 16])
+    lights = lights_from(d["lights"]) + lights_from(d["point_lights"])
+    _, rad = sc.render(cam, lights, 4, 4, 0.0, 2, seed=3)
+    orad, _, _ = o.render(cam, lights, 4, 4, 0.0, 2, seed=3)
+    assert abs(rad[..., :3].mean() / orad[..., :3].mean() - 1) < 0.01
+    rgba, rad0 = sc.render(cam, lights, 1, 1, 0.0, 0)   # no bounce: black, alpha 1
+    assert (rad0[..., :3] == 0).all() and (rgba[..., 3] == 255).all()
+
+
+def test_asteroid_sun_render_vs_oracle(ctx):
+    """Config-2 style render (1 spp, 1 bounce, sun as a distant point light) on a 100k asteroid."""
+    ents = [scenes.EntitySpec("a", scenes.asteroid(100_000, seed=3), (0.1, 0.1, 0.1))]
+    sc = ctx.scene(ents)
+    o = oracle.Scene(ents)
+    view = scenes.unit_vector(12)
+    sun = np.cross(view, scenes.unit_vector(11))          # sun at 90 deg: the terminator crosses the view
+    sun /= np.linalg.norm(sun)
+    lights = [dict(type="point", intensity=1.0e18, position=1.0e9 * sun)]
+    cam = scenes.fov_camera(scenes.TAN5 * 2.4, (128, 128), 5000.0 * view, (0.0, 0.0, 0.0))
+    _, rad = sc.render(cam, lights, 1, 1, 1.0, 1)
+    orad, _, _ = o.render(cam, lights, 1, 1, 1.0, 1)
+    close = np.isclose(rad[..., :3], orad[..., :3], rtol=1e-3, atol=1e-4).all(-1)
+    assert close.mean() > 0.98, close.mean()
+    lit = orad[..., 0] > 0
+    assert 0.2 < lit.mean() < 0.9

@@ -1,0 +1,96 @@
+"""Solar radiation pressure: analytic known answers and parity with the CPU restatement.
+
+The reference has no radiation-pressure code (its README names the feature only), so parity is
+unpinned by the reference; the oracle is the FP64 restatement of the same flat-plate model and the
+known answers come from the closed-form plate and sphere results (Montenbruck & Gill, sec. 3.4).
+"""
+import numpy as np
+import pytest
+
+import oracle
+from crt_gb300 import lib, scenes
+
+pytestmark = pytest.mark.gpu
+
+C = 299792458.0
+FLUX = 1361.0
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    c = lib.Context(0)
+    yield c
+    c.close()
+
+
+def srp_params(stats, sun_body, grid, nb, cm=(0.0, 0.0, 0.0)):
+    b = np.array(stats["bounds"], dtype=np.float64)
+    lo, hi = b[:3], b[3:]
+    p = oracle.SrpParams()
+    p.sun_dir[:] = list(sun_body)
+    p.flux, p.c = FLUX, C
+    p.center[:] = list(0.5 * (lo + hi))
+    p.half_extent = 0.5 * float(np.sqrt(((hi - lo) ** 2).sum()))
+    p.center_of_mass[:] = list(cm)
+    p.grid, p.num_bounces = grid, nb
+    return p
+
+
+def test_flat_plate_known_answer(ctx):
+    rs, rd = 0.3, 0.2
+    plate = scenes.quad_mesh((-0.5, -0.5, 0.0), (0.5, -0.5, 0.0), (0.5, 0.5, 0.0), (-0.5, 0.5, 0.0))
+    sc = ctx.scene([scenes.EntitySpec("p", plate, rho_s=rs, rho_d=rd)])
+    theta = np.deg2rad(35.0)
+    s = np.array([np.sin(theta), 0.0, np.cos(theta)])     # toward the sun, body frame (identity attitude)
+    f, t, fp = sc.srp(s, [[1.0, 0.0, 0.0, 0.0]], grid=2048, num_bounces=0, facet_power=True)
+    P = FLUX / C
+    n = np.array([0.0, 0.0, 1.0])
+    cs = np.cos(theta)
+    expect = -P * 1.0 * cs * ((1 - rs) * s + 2 * (rs * cs + rd / 3) * n)
+    np.testing.assert_allclose(f[0], expect, rtol=3e-3, atol=3e-3 * np.abs(expect).max())
+    # absorbed power = (1 - rs - rd) * flux * projected area
+    assert abs(fp.sum() / ((1 - rs - rd) * FLUX * cs) - 1) < 3e-3
+    assert np.abs(t[0]).max() < 1e-3 * np.abs(expect).max()
+
+
+def test_sphere_known_answer(ctx):
+    rd = 0.4
+    sph = scenes.asteroid(target_faces=0, level=6, radius=1.0, amplitude=0.0)
+    sc = ctx.scene([scenes.EntitySpec("s", sph, rho_s=0.0, rho_d=rd)])
+    s = scenes.unit_vector(4)
+    f, t, _ = sc.srp(s, [[1.0, 0.0, 0.0, 0.0]], grid=1024, num_bounces=0)
+    P = FLUX / C
+    # cannonball: F = -P pi R^2 (1 + 4 rd / 9) s   (tessellated sphere: projected area slightly < pi)
+    expect = -P * np.pi * (1 + 4 * rd / 9) * s
+    np.testing.assert_allclose(f[0], expect, rtol=0.01, atol=0.01 * np.abs(expect).max())
+    assert np.linalg.norm(t[0]) < 1e-3 * np.linalg.norm(expect)
+
+
+def test_spacecraft_vs_oracle(ctx):
+    ents = scenes.spacecraft(bus_cell=0.25, panel_cell=0.2, dish_rings=16, dish_segments=16)
+    sc = ctx.scene(ents)
+    o = oracle.Scene(ents)
+    stats = sc.stats()
+    q = scenes.random_quaternions(4, seed=21)
+    s_i = np.array([1.0, 0.0, 0.0])
+    cm = (0.1, -0.2, 0.05)
+    f, t, fp = sc.srp(s_i, q, grid=384, num_bounces=2, center_of_mass=cm, facet_power=True)
+    for a in range(len(q)):
+        R = scenes.quaternion_to_matrix(q[a])
+        sb = R.T @ s_i
+        of, ot, ofp = o.srp(srp_params(stats, sb, 384, 2, cm))
+        assert np.linalg.norm(f[a] - of) <= 1e-4 * np.linalg.norm(of)
+        assert np.linalg.norm(t[a] - ot) <= 1e-4 * max(np.linalg.norm(ot), 1e-3 * np.linalg.norm(of))
+        assert abs(fp[a].sum() / ofp.sum() - 1) < 1e-4
+        hitf = ofp > 0
+        assert (np.abs(fp[a] - ofp)[hitf] <= 0.05 * ofp[hitf] + 1e-9).mean() > 0.95
+
+
+def test_reduction_is_deterministic(ctx):
+    ents = scenes.spacecraft(bus_cell=0.5, panel_cell=0.5, dish_rings=8, dish_segments=8)
+    sc = ctx.scene(ents)
+    q = scenes.random_quaternions(3, seed=2)
+    f1, t1, _ = sc.srp([0.0, 0.0, 1.0], q, grid=256)
+    f2, t2, _ = sc.srp([0.0, 0.0, 1.0], q, grid=256)
+    np.testing.assert_array_equal(f1, f2)
+    np.testing.assert_array_equal(t1, t2)
