@@ -39,7 +39,7 @@ NODE_BYTES, TRI_BYTES, RAY_BYTES, HIT_BYTES = 80, 48, 32, 16
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--steps", type=int, default=500)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--faces", type=int, default=2_000_000)
@@ -48,7 +48,29 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--probe", type=int, default=0,
+                    help="profiling aid: only launch the primary-ray closest-hit kernel this many times")
     return ap.parse_args()
+
+
+def probe(args):
+    """Small profiling case: the 2M-triangle asteroid resident (about 330 MB with the rays, larger than
+    L2) and `--probe` launches of crt_trace_closest on the 2048^2 primary camera rays."""
+    import torch
+    from crt_gb300 import build, lib, workloads
+    build.build()
+    ents = workloads.asteroid_entities(args.faces)
+    cfg = workloads.asteroid_config(args.res, args.lidar)
+    ctx = lib.Context(0)
+    sc = ctx.scene(ents)
+    rays = torch.from_numpy(scenes_camera_rays(cfg["camera"])).cuda()
+    hits = torch.empty((rays.shape[0], 4), dtype=torch.float32, device="cuda")
+    for _ in range(args.probe):
+        sc.trace_closest(rays, out=hits)
+    ctx.synchronize()
+    miss = (hits[:, 3].view(torch.int32) == -1).float().mean().item()
+    print(json.dumps({"probe_launches": args.probe, "rays": int(rays.shape[0]), "miss_fraction": miss}))
+    ctx.close()
 
 
 def dist_info():
@@ -364,11 +386,16 @@ def gpu_arm(args):
 
 
 def scenes_camera_rays(cam):
-    """FP32 camera rays (as an [n, 8] float32 array) for the roofline probe."""
+    """FP32 camera rays in crt_ray layout (o.xyz, tmin, d.xyz, tmax) as an [n, 8] float32 array, for
+    the roofline probe (the oracle's FP64 rays are laid out o.xyz, d.xyz, tmin, tmax)."""
     import oracle
-    r = oracle.camera_rays(cam).astype(np.float32)
+    r64 = oracle.camera_rays(cam)
+    r = np.empty((r64.shape[0], 8), dtype=np.float32)
+    r[:, 0:3] = r64[:, 0:3]
+    r[:, 3] = 0.0
+    r[:, 4:7] = r64[:, 3:6]
     r[:, 7] = np.finfo(np.float32).max
-    return np.ascontiguousarray(r)
+    return r
 
 
 def e2e_measure(args, ents, cfg, rays_step):
@@ -409,7 +436,9 @@ def e2e_measure(args, ents, cfg, rays_step):
 
 def main():
     args = parse()
-    if args.impl == "reference":
+    if args.probe:
+        probe(args)
+    elif args.impl == "reference":
         reference_arm(args)
     else:
         gpu_arm(args)

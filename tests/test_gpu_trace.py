@@ -82,7 +82,8 @@ def camera_parity(ctx_scene, o, cam, ref=None):
     relx = np.linalg.norm(gx - ox, axis=-1)[ok] / scale[ok]
     assert relx.max() < DIST_REL, relx.max()
     assert np.abs(gn - on)[ok].max() < DIST_REL
-    assert (gx[oi == 0] == 0).all() and (gn[oi == 0] == 0).all()
+    both_miss = (oi == 0) & (gi == 0)
+    assert (gx[both_miss] == 0).all() and (gn[both_miss] == 0).all()
     return gi, oi
 
 
