@@ -101,6 +101,7 @@ SIGNATURES = {
     "crt_lidar_grid": ([vp, ctypes.POINTER(LidarGridDesc), vp, vp], i32),
     "crt_render": ([vp, ctypes.POINTER(CameraDesc), vp, u32, ctypes.POINTER(RenderParams), vp, vp], i32),
     "crt_srp": ([vp, ctypes.POINTER(SrpDesc), vp, sz, vp, vp, vp], i32),
+    "crt_srp_static": ([vp, ctypes.POINTER(SrpDesc), vp, sz, vp, vp], i32),
 }
 
 _lib = None

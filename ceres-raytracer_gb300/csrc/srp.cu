@@ -277,3 +277,151 @@ extern "C" int crt_srp(crt_scene* s, const crt_srp_desc* desc, const double* qua
         check_device_error(ctx, "crt_srp");
     });
 }
+
+// ---------------------------------------------------------------- allocation-free variant
+// crt_srp_static: the same force / torque computation with every piece of scratch (work counter,
+// attitude table, per-chunk FP64 partial sums, staging of host outputs) in the file-scope device
+// array below, so a call performs no device allocation.  It serves callers that must not allocate
+// device memory after start-up: flight-dynamics or attitude-control loops with a fixed memory
+// budget, and code that runs while another component owns the CUDA allocator.  Every GPU that loads
+// the library holds this array until the process exits.
+#define CRT_SRP_STATIC_BYTES (16u << 20)          // 16 MiB per device
+#define CRT_SRP_STATIC_MAX_ATT 4096u              // attitudes per call
+static __device__ __align__(256) unsigned char g_srp_static_scratch[CRT_SRP_STATIC_BYTES];
+
+namespace {
+
+constexpr size_t SS_COUNTER = 0;                                  // work counter (zeroed per launch)
+constexpr size_t SS_ATT = 256;                                    // SrpAtt table
+constexpr size_t SS_OUT = SS_ATT + sizeof(SrpAtt) * CRT_SRP_STATIC_MAX_ATT;    // force | torque staging
+constexpr size_t SS_PART = (SS_OUT + 48ull * CRT_SRP_STATIC_MAX_ATT + 255) & ~size_t(255);
+constexpr size_t SS_PART_BYTES = CRT_SRP_STATIC_BYTES - SS_PART;
+
+std::mutex g_static_mu;
+void* g_static_ptr[256] = {};
+
+// Device address of the scratch array on the current device; resolved once per device.
+void* static_scratch(int device) {
+    CRT_CHECK(device >= 0 && device < 256, CRT_ERR_INVALID, "device index out of range");
+    std::lock_guard<std::mutex> lk(g_static_mu);
+    if (!g_static_ptr[device]) {
+        void* p = nullptr;
+        CRT_CUDA(cudaGetSymbolAddress(&p, g_srp_static_scratch));
+        g_static_ptr[device] = p;
+    }
+    return g_static_ptr[device];
+}
+
+}  // namespace
+
+extern "C" int crt_srp_static(crt_scene* s, const crt_srp_desc* desc, const double* quats, size_t n_att,
+                              double* force, double* torque) {
+    if (!s || !desc) return CRT_ERR_INVALID;
+    crt_context* ctx = s->ctx;
+    return crt_guard(ctx, [&] {
+        CRT_CHECK(n_att == 0 || (quats && force && torque), CRT_ERR_INVALID, "null buffer");
+        CRT_CHECK(n_att <= CRT_SRP_STATIC_MAX_ATT, CRT_ERR_INVALID,
+                  "crt_srp_static: at most 4096 attitudes per call (static scratch limit)");
+        CRT_CHECK(desc->grid > 0 && desc->grid <= 65536, CRT_ERR_INVALID, "grid must be in [1, 65536]");
+        CRT_CHECK(desc->c > 0 && std::isfinite(desc->flux), CRT_ERR_INVALID, "bad flux or speed of light");
+        CRT_CHECK(desc->num_bounces <= 16, CRT_ERR_INVALID, "at most 16 specular bounces");
+        CRT_CHECK(!is_device_ptr(quats), CRT_ERR_INVALID, "crt_srp_static reads the quaternions from host memory");
+        const uint32_t G = desc->grid;
+        const uint32_t tiles = ((G + 7) / 8) * ((G + 3) / 4);
+        const uint32_t gpa = (tiles + CHUNK - 1) / CHUNK;
+        CRT_CHECK((size_t)gpa * 48 <= SS_PART_BYTES, CRT_ERR_INVALID,
+                  "crt_srp_static: grid too large for the 16 MiB static scratch (one attitude's partial sums "
+                  "must fit; grid <= 11585)");
+        if (!n_att) return;
+        CRT_CUDA(cudaSetDevice(ctx->device));
+        char* base = (char*)static_scratch(ctx->device);
+        uint32_t* queue = (uint32_t*)(base + SS_COUNTER);
+        SrpAtt* d_att = (SrpAtt*)(base + SS_ATT);
+        double* d_out = (double*)(base + SS_OUT);
+        double* d_partial = (double*)(base + SS_PART);
+        cudaStream_t st = ctx->stream;
+
+        const double sl = std::sqrt(desc->sun_dir_inertial[0] * desc->sun_dir_inertial[0] +
+                                    desc->sun_dir_inertial[1] * desc->sun_dir_inertial[1] +
+                                    desc->sun_dir_inertial[2] * desc->sun_dir_inertial[2]);
+        CRT_CHECK(sl > 0 && std::isfinite(sl), CRT_ERR_INVALID, "sun direction must be a non-zero vector");
+        const double si[3] = {desc->sun_dir_inertial[0] / sl, desc->sun_dir_inertial[1] / sl,
+                              desc->sun_dir_inertial[2] / sl};
+        double ctr[3], ext2 = 0;
+        for (int k = 0; k < 3; ++k) {
+            ctr[k] = 0.5 * ((double)s->bounds[k] + (double)s->bounds[3 + k]);
+            const double e = (double)s->bounds[3 + k] - (double)s->bounds[k];
+            ext2 += e * e;
+        }
+        const double Rb = 0.5 * std::sqrt(ext2);
+        const double h = 2.0 * Rb / G;
+        // attitude table: computed on the host in chunks held on the stack, copied into the scratch
+        SrpAtt chunk[64];
+        for (size_t a0 = 0; a0 < n_att; a0 += 64) {
+            const size_t na = std::min<size_t>(64, n_att - a0);
+            for (size_t j = 0; j < na; ++j) {
+                const double* q = quats + 4 * (a0 + j);
+                double w = q[0], x = q[1], y = q[2], z = q[3];
+                const double qn = std::sqrt(w * w + x * x + y * y + z * z);
+                CRT_CHECK(qn > 0 && std::isfinite(qn), CRT_ERR_INVALID, "attitude quaternion must be non-zero");
+                w /= qn; x /= qn; y /= qn; z /= qn;
+                const double R[9] = {1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y),
+                                     2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x),
+                                     2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)};
+                double sb[3];
+                for (int k = 0; k < 3; ++k) sb[k] = R[k] * si[0] + R[3 + k] * si[1] + R[6 + k] * si[2];
+                double ax[3] = {1, 0, 0};
+                if (std::fabs(sb[0]) >= 0.9) { ax[0] = 0; ax[1] = 1; }
+                double e1[3] = {sb[1] * ax[2] - sb[2] * ax[1], sb[2] * ax[0] - sb[0] * ax[2],
+                                sb[0] * ax[1] - sb[1] * ax[0]};
+                const double l1 = std::sqrt(e1[0] * e1[0] + e1[1] * e1[1] + e1[2] * e1[2]);
+                for (int k = 0; k < 3; ++k) e1[k] /= l1;
+                const double e2[3] = {sb[1] * e1[2] - sb[2] * e1[1], sb[2] * e1[0] - sb[0] * e1[2],
+                                      sb[0] * e1[1] - sb[1] * e1[0]};
+                for (int k = 0; k < 3; ++k) {
+                    const double o0 = ctr[k] + sb[k] * (2.0 * Rb + 1.0) + e1[k] * (-Rb + 0.5 * h) + e2[k] * (-Rb + 0.5 * h);
+                    chunk[j].org[k] = (float)o0;
+                    chunk[j].du[k] = (float)(e1[k] * h);
+                    chunk[j].dv[k] = (float)(e2[k] * h);
+                    chunk[j].dir[k] = (float)(-sb[k]);
+                }
+                chunk[j].E0 = (float)(desc->flux * h * h);
+                chunk[j].pad = 0.f;
+            }
+            CRT_CUDA(cudaMemcpyAsync(d_att + a0, chunk, sizeof(SrpAtt) * na, cudaMemcpyHostToDevice, st));
+            CRT_CUDA(cudaStreamSynchronize(st));   // the stack chunk is reused for the next attitudes
+        }
+        const bool host_out = !is_device_ptr(force) || !is_device_ptr(torque);
+        double* f_out = host_out ? d_out : force;
+        double* t_out = host_out ? d_out + 3 * CRT_SRP_STATIC_MAX_ATT : torque;
+        const size_t att_per_launch = std::max<size_t>(1, std::min<size_t>(n_att, SS_PART_BYTES / (48ull * gpa)));
+        const size_t smem = (size_t)CRT_STACK_SMEM * CRT_TRACE_BLOCK * sizeof(uint2);
+        const int grid = occupancy_grid(ctx, (const void*)k_srp, CRT_TRACE_BLOCK, smem);
+        const SceneView sv = scene_view(s);
+        for (size_t a0 = 0; a0 < n_att; a0 += att_per_launch) {
+            const size_t na = std::min(att_per_launch, n_att - a0);
+            SrpArgs A;
+            A.att = d_att + a0;
+            A.G = G;
+            A.tiles = tiles;
+            A.grabs_per_att = gpa;
+            A.n_att = (uint32_t)na;
+            A.inv_c = (float)(1.0 / desc->c);
+            for (int k = 0; k < 3; ++k) A.cm[k] = (float)desc->center_of_mass[k];
+            A.nb = desc->num_bounces;
+            A.partial = d_partial;
+            A.facet = nullptr;
+            A.n_tris = (uint32_t)s->n_tris;
+            CRT_CUDA(cudaMemsetAsync(queue, 0, sizeof(uint32_t), st));   // the counter must start at zero
+            k_srp<<<grid, CRT_TRACE_BLOCK, smem, st>>>(sv, A, queue, ctx->d_error);
+            check_launch(ctx, "k_srp");
+            k_srp_reduce<<<(uint32_t)na, 256, 0, st>>>(d_partial, gpa, f_out + 3 * a0, t_out + 3 * a0);
+            check_launch(ctx, "k_srp_reduce");
+        }
+        if (host_out) {
+            CRT_CUDA(cudaMemcpyAsync(force, f_out, n_att * 24, cudaMemcpyDeviceToHost, st));
+            CRT_CUDA(cudaMemcpyAsync(torque, t_out, n_att * 24, cudaMemcpyDeviceToHost, st));
+            check_device_error(ctx, "crt_srp_static");
+        }
+    });
+}

@@ -209,6 +209,18 @@ int crt_render(crt_scene* scene, const crt_camera_desc* camera, const crt_light_
  * is n_att * n_tris absorbed power per triangle (W).  No reference counterpart (README.md:9). */
 int crt_srp(crt_scene* scene, const crt_srp_desc* desc, const double* quaternions, size_t n_att, double* force,
             double* torque, double* facet_power);
+/* Allocation-free variant of crt_srp (no counterpart in the reference): the same force and torque,
+ * with all scratch (work counter, attitude table, per-chunk FP64 partial sums, staging of host
+ * outputs) in one 16 MiB file-scope device array instead of device allocations, for callers that
+ * must not allocate device memory once running (fixed-budget flight-dynamics or attitude loops,
+ * components that do not own the CUDA allocator).  Limits: n_att <= 4096 per call and
+ * grid <= 11585 (one attitude's partial sums must fit); quaternions are read from host memory;
+ * force / torque may be host or device memory; no per-facet output.  The first call on a device
+ * resolves the array's device address (cudaGetSymbolAddress) and should come before any stream
+ * capture.  All calls share the array: calls that overlap on the GPU (other streams or contexts)
+ * race.  Every GPU that loads the library keeps the 16 MiB until the process exits. */
+int crt_srp_static(crt_scene* scene, const crt_srp_desc* desc, const double* quaternions, size_t n_att,
+                   double* force, double* torque);
 
 #ifdef __cplusplus
 }
