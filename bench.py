@@ -48,6 +48,7 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--probe", type=int, default=0,
                     help="profiling aid: only launch the primary-ray closest-hit kernel this many times")
     return ap.parse_args()
@@ -147,9 +148,9 @@ def profiled_traffic():
     if not os.path.exists(path):
         return None
     for line in open(path):
-        if line.strip().startswith("dram_bytes_per_launch_full"):
+        if "dram_bytes_per_launch_full" in line and "=" in line:
             try:
-                return float(line.split("=")[1].split()[0])
+                return float(line.split("=")[1].replace("|", " ").split()[0])
             except (IndexError, ValueError):
                 return None
     return None
@@ -353,6 +354,11 @@ def gpu_arm(args):
             "bytes_per_ray": round(b_ray, 1), "nodes_per_ray": round(nodes_ray, 2), "tris_per_ray": round(tris_ray, 2),
             "kernel_ms": round(t_kernel * 1e3, 3), "kernel_mrays_s": round(cnt["rays"] / t_kernel / 1e6, 1)}
 
+    # ---- batched vs per-call on the config-3 request set
+    batched = None
+    if not args.no_batched and rank == 0:
+        batched = batched_measure(ctx, sc, stream)
+
     # ---- end to end through the public crt API (host numpy outputs)
     e2e = None
     if not args.no_e2e and rank == 0:
@@ -373,7 +379,7 @@ def gpu_arm(args):
                                "render_p99": round(percentile(lat_render, 99), 3),
                                "lidar_p50": round(percentile(lat_lidar, 50), 3),
                                "lidar_p99": round(percentile(lat_lidar, 99), 3)},
-                "roofline": roof, "gpu_launches": int(launches), "clocks": clk, "e2e": e2e}
+                "roofline": roof, "gpu_launches": int(launches), "clocks": clk, "e2e": e2e, "batched": batched}
         if world == 1 and not args.no_cpu:
             mr, det = cpu_measure(ents, cfg, args.cpu_seconds)
             line["cpu_baseline"] = {"value": round(mr, 3), "unit": UNIT, "cores": det["cores"], "kind": "port",
@@ -383,6 +389,81 @@ def gpu_arm(args):
         torch.distributed.barrier()
         torch.distributed.destroy_process_group()
     ctx.close()
+
+
+def batched_measure(ctx, sc, stream, reps=1):
+    """Config-3 workload on the resident asteroid: 64 requests (32 renders, 2 bounces, resolution
+    128^2..2048^2, 1..64 spp; 32 LiDAR scans 64^2..1024^2) as per-call GPU requests (one library call
+    each, in sequence) and as one crt_batch; device outputs in both cases.  Returns a dict."""
+    import torch
+    from crt_gb300 import workloads
+    reqs = workloads.batched_config(seed=1)
+    dev = torch.device("cuda", torch.cuda.current_device())
+    outs, breqs = [], []
+    for q in reqs:
+        if q["kind"] == "render":
+            W, H = q["camera"]["resolution"]
+            outs.append((torch.empty((H, W, 4), dtype=torch.uint8, device=dev), None))
+            breqs.append(dict(kind="render", scene=sc, camera=q["camera"], lights=q["lights"], min_samples=q["spp"],
+                              max_samples=q["spp"], noise_threshold=0.0, num_bounces=q["bounces"], seed=1,
+                              request=q["request"]))
+        else:
+            outs.append((torch.empty((q["ny"], q["nx"]), dtype=torch.float64, device=dev),
+                         torch.empty((q["ny"], q["nx"]), dtype=torch.int32, device=dev)))
+            breqs.append(dict(kind="lidar", scene=sc, position=q["position"], rotation=q["rotation"], nx=q["nx"],
+                              ny=q["ny"], half_x=q["half_x"], half_y=q["half_y"]))
+
+    def per_call(events=None):
+        for k, (q, o) in enumerate(zip(breqs, outs)):
+            if events is not None:
+                events[k][0].record(stream)
+            if q["kind"] == "render":
+                sc.render(q["camera"], q["lights"], q["min_samples"], q["max_samples"], 0.0, q["num_bounces"],
+                          seed=q["seed"], request=q["request"], want_radiance=False, out_rgba=o[0])
+            else:
+                sc.lidar_grid(q["position"], q["rotation"], q["nx"], q["ny"], q["half_x"], q["half_y"],
+                              out_range=o[0], out_prim=o[1])
+            if events is not None:
+                events[k][1].record(stream)
+
+    with torch.cuda.stream(stream):
+        # rays actually traced (counting build), identical for both paths
+        ctx.reset_counters()
+        ctx.set_counting(True)
+        ctx.batch(breqs, outputs=outs)
+        rays = ctx.counters()["rays"]
+        ctx.set_counting(False)
+        ctx.batch(breqs, outputs=outs)      # warm-up (scratch sized, graph path exercised)
+        per_call()
+        torch.cuda.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in breqs]
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        per_call(ev)
+        t1.record(stream)
+        b0 = torch.cuda.Event(enable_timing=True)
+        b1 = torch.cuda.Event(enable_timing=True)
+        b0.record(stream)
+        for _ in range(reps):
+            _, st = ctx.batch(breqs, outputs=outs)
+        b1.record(stream)
+    torch.cuda.synchronize()
+    pc_ms = t0.elapsed_time(t1)
+    bt_ms = b0.elapsed_time(b1) / reps
+    lat = [a.elapsed_time(b) for a, b in ev]
+    # per-call latency of a request submitted with the whole set: its completion time in the sequence
+    done = np.cumsum(lat)
+    return {"workload": "64 requests on the 2M asteroid: 32 renders (128^2..2048^2, 1..64 spp, 2 bounces, "
+                        "sun light) + 32 LiDAR scans (64^2..1024^2)",
+            "rays": int(rays), "per_call_mrays_s": round(rays / (pc_ms / 1e3) / 1e6, 1),
+            "batched_mrays_s": round(rays / (bt_ms / 1e3) / 1e6, 1), "speedup": round(pc_ms / bt_ms, 3),
+            "per_call_ms": round(pc_ms, 2), "batched_ms": round(bt_ms, 2), "waves": st["waves"],
+            "per_call_request_ms_p50": round(percentile(lat, 50), 3),
+            "per_call_request_ms_p99": round(percentile(lat, 99), 3),
+            "per_call_completion_ms_p50": round(percentile(list(done), 50), 2),
+            "per_call_completion_ms_p99": round(percentile(list(done), 99), 2),
+            "batched_completion_ms": round(bt_ms, 2)}
 
 
 def scenes_camera_rays(cam):

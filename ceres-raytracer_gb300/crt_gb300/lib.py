@@ -60,6 +60,41 @@ class SrpDesc(ctypes.Structure):
                 ("grid", u32), ("num_bounces", u32)]
 
 
+class Request(ctypes.Structure):
+    _fields_ = [("kind", i32), ("scene", vp), ("camera", ctypes.POINTER(CameraDesc)), ("lights", vp),
+                ("n_lights", u32), ("params", ctypes.POINTER(RenderParams)), ("rgba8", vp), ("radiance", vp),
+                ("lidar", ctypes.POINTER(LidarGridDesc)), ("range", vp), ("prim", vp)]
+
+
+class BatchStats(ctypes.Structure):
+    _fields_ = [("waves", sz), ("render_paths", ctypes.c_uint64), ("lidar_beams", ctypes.c_uint64)]
+
+
+class Tuning(ctypes.Structure):
+    _fields_ = [("queue_chunk", u32), ("wave_paths", u32), ("use_graphs", i32)]
+
+
+REQUEST_RENDER, REQUEST_LIDAR, REQUEST_SRP = 0, 1, 2
+
+
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("lanes", u32), ("lane_budget_bytes", sz), ("max_batch", u32)]
+
+
+class ServerRequest(ctypes.Structure):
+    _fields_ = [("base", Request), ("srp", ctypes.POINTER(SrpDesc)), ("quaternions", vp), ("n_att", sz),
+                ("force", vp), ("torque", vp)]
+
+
+class ServerResult(ctypes.Structure):
+    _fields_ = [("status", i32), ("submit_s", dbl), ("start_s", dbl), ("end_s", dbl), ("batch_size", u32)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_uint64), ("completed", ctypes.c_uint64), ("batches", ctypes.c_uint64),
+                ("failed", ctypes.c_uint64), ("rays", ctypes.c_uint64), ("busy_s", dbl)]
+
+
 class SceneStats(ctypes.Structure):
     _fields_ = [("n_tris", sz), ("n_nodes", sz), ("n_entities", sz), ("depth", u32), ("build_ms", dbl),
                 ("device_bytes", sz), ("bounds", ctypes.c_float * 6)]
@@ -102,6 +137,15 @@ SIGNATURES = {
     "crt_render": ([vp, ctypes.POINTER(CameraDesc), vp, u32, ctypes.POINTER(RenderParams), vp, vp], i32),
     "crt_srp": ([vp, ctypes.POINTER(SrpDesc), vp, sz, vp, vp, vp], i32),
     "crt_srp_static": ([vp, ctypes.POINTER(SrpDesc), vp, sz, vp, vp], i32),
+    "crt_batch": ([vp, vp, sz, ctypes.POINTER(BatchStats)], i32),
+    "crt_context_set_tuning": ([vp, ctypes.POINTER(Tuning)], i32),
+    "crt_context_get_tuning": ([vp, ctypes.POINTER(Tuning)], i32),
+    "crt_server_create": ([i32, ctypes.POINTER(ServerConfig), ctypes.POINTER(vp)], i32),
+    "crt_server_destroy": ([vp], i32),
+    "crt_server_last_error": ([], ctypes.c_char_p),
+    "crt_server_submit": ([vp, ctypes.POINTER(ServerRequest), ctypes.POINTER(ctypes.c_uint64)], i32),
+    "crt_server_wait": ([vp, ctypes.c_uint64, dbl, ctypes.POINTER(ServerResult)], i32),
+    "crt_server_get_stats": ([vp, ctypes.POINTER(ServerStats)], i32),
 }
 
 _lib = None
@@ -207,6 +251,66 @@ class Context:
 
     def scene(self, entities):
         return Scene(self, entities)
+
+    def set_tuning(self, queue_chunk=1, wave_paths=1 << 23, use_graphs=True):
+        t = Tuning(int(queue_chunk), int(wave_paths), int(bool(use_graphs)))
+        self._check(self.L.crt_context_set_tuning(self.h, ctypes.byref(t)))
+
+    def get_tuning(self):
+        t = Tuning()
+        self._check(self.L.crt_context_get_tuning(self.h, ctypes.byref(t)))
+        return dict(queue_chunk=t.queue_chunk, wave_paths=t.wave_paths, use_graphs=bool(t.use_graphs))
+
+    def batch(self, requests, outputs=None):
+        """Run render / LiDAR requests in one batch.  Each request is a dict:
+        {"kind": "render", "scene": Scene, "camera": cam, "lights": [...], "min_samples", "max_samples",
+         "noise_threshold", "num_bounces", "seed", "request", "radiance": bool}
+        {"kind": "lidar", "scene": Scene, "position", "rotation", "nx", "ny", "half_x", "half_y", "z_positive"}
+        Returns (outputs, stats): outputs[i] = (rgba, radiance) or (range, prim)."""
+        n = len(requests)
+        arr = (Request * max(1, n))()
+        keep, outs = [], []
+        for i, q in enumerate(requests):
+            r = arr[i]
+            r.scene = q["scene"].h
+            given = outputs[i] if outputs is not None else None
+            if q["kind"] == "render":
+                cam = q["camera"]
+                W, H = int(np.floor(cam["resolution"][0])), int(np.floor(cam["resolution"][1]))
+                c = fill_camera(cam)
+                L = fill_lights(q.get("lights", []))
+                p = RenderParams(int(q.get("min_samples", 1)), int(q.get("max_samples", 1)),
+                                 float(q.get("noise_threshold", 1.0)), int(q.get("num_bounces", 1)),
+                                 int(q.get("seed", 0)), int(q.get("request", 0)))
+                rgba, rad = given if given is not None else (
+                    np.empty((H, W, 4), np.uint8), np.empty((H, W, 4), np.float32) if q.get("radiance") else None)
+                keep += [c, L, p]
+                r.kind = REQUEST_RENDER
+                r.camera = ctypes.pointer(c)
+                r.lights = ctypes.cast(L, vp)
+                r.n_lights = len(q.get("lights", []))
+                r.params = ctypes.pointer(p)
+                r.rgba8 = ptr(rgba)
+                r.radiance = ptr(rad)
+                outs.append((rgba, rad))
+            else:
+                g = LidarGridDesc()
+                g.position[:] = [float(x) for x in np.asarray(q["position"], dtype=np.float64).ravel()]
+                g.rotation[:] = [float(x) for x in np.asarray(q["rotation"], dtype=np.float64).ravel()]
+                g.z_positive = int(bool(q.get("z_positive", False)))
+                g.nx, g.ny = int(q["nx"]), int(q["ny"])
+                g.half_angle_x, g.half_angle_y = float(q["half_x"]), float(q["half_y"])
+                rng, prim = given if given is not None else (np.empty((g.ny, g.nx)), np.empty((g.ny, g.nx), np.uint32))
+                keep.append(g)
+                r.kind = REQUEST_LIDAR
+                r.lidar = ctypes.pointer(g)
+                r.range = ptr(rng)
+                r.prim = ptr(prim)
+                outs.append((rng, prim))
+        st = BatchStats()
+        self._check(self.L.crt_batch(self.h, arr, n, ctypes.byref(st)))
+        del keep
+        return outs, dict(waves=st.waves, render_paths=st.render_paths, lidar_beams=st.lidar_beams)
 
 
 class Scene:
@@ -340,3 +444,104 @@ def make_rays(o, d, tmin=0.0, tmax=3.4e38):
     r["o"], r["d"] = o, d
     r["tmin"], r["tmax"] = tmin, tmax
     return r
+
+
+class Server:
+    """Continuous-batching request loop (crt_server_*).  Scenes are created with server.scene(...) on
+    a context of the server object's own (not a lane's), so they can also be called directly while
+    requests run; requests are dicts as for Context.batch plus {"kind": "srp", "scene", "sun_dir",
+    "quaternions", "grid", "num_bounces", "flux", "c", "center_of_mass"}.  submit() returns a ticket;
+    wait() returns (result dict, outputs)."""
+
+    def __init__(self, device=0, lanes=2, lane_budget_bytes=4 << 30, max_batch=64):
+        self.L = load()
+        self.h = None
+        self.ctx = Context(device)
+        cfg = ServerConfig(int(lanes), int(lane_budget_bytes), int(max_batch))
+        h = vp()
+        rc = self.L.crt_server_create(int(device), ctypes.byref(cfg), ctypes.byref(h))
+        if rc != CRT_OK:
+            self.ctx.close()
+            raise CrtError(rc, self.L.crt_status_string(rc).decode())
+        self.h = h
+        self._inflight = {}
+
+    def scene(self, entities):
+        return Scene(self.ctx, entities)
+
+    def submit(self, q, outputs=None):
+        sr = ServerRequest()
+        keep = []
+        r = sr.base
+        r.scene = q["scene"].h
+        if q["kind"] == "render":
+            cam = q["camera"]
+            W, H = int(np.floor(cam["resolution"][0])), int(np.floor(cam["resolution"][1]))
+            c, Ls = fill_camera(cam), fill_lights(q.get("lights", []))
+            p = RenderParams(int(q.get("min_samples", 1)), int(q.get("max_samples", 1)),
+                             float(q.get("noise_threshold", 1.0)), int(q.get("num_bounces", 1)), int(q.get("seed", 0)),
+                             int(q.get("request", 0)))
+            out = outputs or (np.empty((H, W, 4), np.uint8),
+                              np.empty((H, W, 4), np.float32) if q.get("radiance") else None)
+            keep += [c, Ls, p]
+            r.kind, r.camera, r.lights = REQUEST_RENDER, ctypes.pointer(c), ctypes.cast(Ls, vp)
+            r.n_lights, r.params = len(q.get("lights", [])), ctypes.pointer(p)
+            r.rgba8, r.radiance = ptr(out[0]), ptr(out[1])
+        elif q["kind"] == "lidar":
+            g = LidarGridDesc()
+            g.position[:] = [float(x) for x in np.asarray(q["position"], dtype=np.float64).ravel()]
+            g.rotation[:] = [float(x) for x in np.asarray(q["rotation"], dtype=np.float64).ravel()]
+            g.z_positive = int(bool(q.get("z_positive", False)))
+            g.nx, g.ny = int(q["nx"]), int(q["ny"])
+            g.half_angle_x, g.half_angle_y = float(q["half_x"]), float(q["half_y"])
+            out = outputs or (np.empty((g.ny, g.nx)), np.empty((g.ny, g.nx), np.uint32))
+            keep.append(g)
+            r.kind, r.lidar, r.range, r.prim = REQUEST_LIDAR, ctypes.pointer(g), ptr(out[0]), ptr(out[1])
+        else:
+            d = SrpDesc()
+            d.sun_dir_inertial[:] = [float(x) for x in q["sun_dir"]]
+            d.flux, d.c = float(q.get("flux", 1361.0)), float(q.get("c", 299792458.0))
+            d.center_of_mass[:] = [float(x) for x in q.get("center_of_mass", (0.0, 0.0, 0.0))]
+            d.grid, d.num_bounces = int(q["grid"]), int(q.get("num_bounces", 2))
+            quats = np.ascontiguousarray(q["quaternions"], dtype=np.float64).reshape(-1, 4)
+            out = outputs or (np.empty((len(quats), 3)), np.empty((len(quats), 3)))
+            keep += [d, quats]
+            r.kind = REQUEST_SRP
+            sr.srp, sr.quaternions, sr.n_att = ctypes.pointer(d), quats.ctypes.data, len(quats)
+            sr.force, sr.torque = ptr(out[0]), ptr(out[1])
+        t = ctypes.c_uint64()
+        rc = self.L.crt_server_submit(self.h, ctypes.byref(sr), ctypes.byref(t))
+        if rc != CRT_OK:
+            raise CrtError(rc, self.L.crt_server_last_error().decode())
+        self._inflight[t.value] = out
+        return t.value
+
+    def wait(self, ticket, timeout=-1.0):
+        res = ServerResult()
+        rc = self.L.crt_server_wait(self.h, ctypes.c_uint64(ticket), float(timeout), ctypes.byref(res))
+        if rc != CRT_OK:
+            raise CrtError(rc, "wait: " + self.L.crt_status_string(rc).decode())
+        out = self._inflight.pop(ticket, None)
+        return dict(status=res.status, submit_s=res.submit_s, start_s=res.start_s, end_s=res.end_s,
+                    latency_s=res.end_s - res.submit_s, batch_size=res.batch_size), out
+
+    def stats(self):
+        s = ServerStats()
+        self.L.crt_server_get_stats(self.h, ctypes.byref(s))
+        return dict(submitted=s.submitted, completed=s.completed, batches=s.batches, failed=s.failed, rays=s.rays,
+                    busy_s=s.busy_s)
+
+    def close(self):
+        """Finishes the queued requests, stops the lanes, then releases the scenes."""
+        if getattr(self, "h", None):
+            self.L.crt_server_destroy(self.h)
+            self.h = None
+        if getattr(self, "ctx", None) is not None:
+            self.ctx.close()
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -189,17 +189,16 @@ def asteroid(target_faces=2_000_000, level=None, radius=1000.0, amplitude=0.05, 
         target_faces = 0
     lib = _lib()
     nv, nf = ctypes.c_size_t(), ctypes.c_size_t()
-    rc = lib.crt_scene_asteroid(level, target_faces, radius, amplitude, octaves, seed, None, 0, None, 0,
-                                ctypes.byref(nv), ctypes.byref(nf))
+    # closed genus-0 triangle mesh: V - E + F = 2 with E = 3F/2, so V = F/2 + 2 (one generator call)
+    cap_f = target_faces or 20 * 4 ** level
+    cap_v = cap_f // 2 + 2
+    v = np.empty((cap_v, 3), dtype=F32)
+    f = np.empty((cap_f, 3), dtype=np.int32)
+    rc = lib.crt_scene_asteroid(level, target_faces, radius, amplitude, octaves, seed, v.ctypes.data, cap_v,
+                                f.ctypes.data, cap_f, ctypes.byref(nv), ctypes.byref(nf))
     if rc != 0:
         raise RuntimeError(f"crt_scene_asteroid failed ({rc})")
-    v = np.empty((nv.value, 3), dtype=F32)
-    f = np.empty((nf.value, 3), dtype=np.int32)
-    rc = lib.crt_scene_asteroid(level, target_faces, radius, amplitude, octaves, seed, v.ctypes.data, nv.value,
-                                f.ctypes.data, nf.value, ctypes.byref(nv), ctypes.byref(nf))
-    if rc != 0:
-        raise RuntimeError(f"crt_scene_asteroid failed ({rc})")
-    return Mesh(v, f)
+    return Mesh(np.ascontiguousarray(v[:nv.value]), np.ascontiguousarray(f[:nf.value]))
 
 
 def cached_asteroid(target_faces=2_000_000, seed=0, cache_dir=None, **kw):

@@ -73,3 +73,48 @@ def srp_config(n_att=256, grid=4096, seed=0):
     ents = scenes.spacecraft()
     q = scenes.random_quaternions(n_att, seed=seed)
     return dict(entities=ents, quaternions=q, grid=grid, num_bounces=2, sun=np.array([1.0, 0.0, 0.0]))
+
+
+SERVED_BODIES = ((100_000, 2), (500_000, 3), (2_000_000, 4), (8_000_000, 5))
+
+
+def served_bodies(bodies=SERVED_BODIES):
+    """Entity lists of the four resident asteroids of the served stream (faces, seed)."""
+    return [asteroid_entities(f, seed=s) for f, s in bodies]
+
+
+def served_stream(rate=200.0, seconds=60.0, seed=7, n_bodies=4):
+    """Poisson request stream over the resident bodies: arrival times (s) and request dicts.
+
+    50 % renders (resolution in {128..2048}^2, spp in {1, 2, 4, 8, 16}, primary + sun-shadow ray as
+    the asteroid render, poses on a 3-10 km shell), 30 % LiDAR scans ({64..1024}^2 beams over
+    +-5 deg) and 20 % SRP queries (one attitude, {512, 1024, 2048}^2 sun-ray grid, 2 bounces).
+    Each request names its body by index (`body`)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    n = int(rng.poisson(rate * seconds))
+    times = np.sort(rng.uniform(0.0, seconds, n))
+    sun = scenes.unit_vector(4000 + seed)
+    lights = [dict(type="point", intensity=SUN_DISTANCE ** 2, position=SUN_DISTANCE * sun)]
+    out = []
+    for i, t in enumerate(times):
+        body = int(rng.integers(n_bodies))
+        u = rng.uniform()
+        if u < 0.5:
+            res = int(rng.choice([128, 256, 512, 1024, 2048]))
+            spp = int(rng.choice([1, 2, 4, 8, 16]))
+            pos = pose_on_shell(rng, 3000.0, 10000.0)
+            cam = scenes.fov_camera(1100.0 / np.linalg.norm(pos), (res, res), pos, (0.0, 0.0, 0.0))
+            q = dict(kind="render", camera=cam, lights=lights, min_samples=spp, max_samples=spp,
+                     noise_threshold=0.0, num_bounces=1, seed=seed, request=i, size=res)
+        elif u < 0.8:
+            m = int(rng.choice([64, 128, 256, 512, 1024]))
+            pos = pose_on_shell(rng, 3000.0, 10000.0)
+            q = dict(kind="lidar", position=pos, rotation=scenes.look_at(pos, (0.0, 0.0, 0.0)), nx=m, ny=m,
+                     half_x=np.deg2rad(5.0), half_y=np.deg2rad(5.0), size=m)
+        else:
+            g = int(rng.choice([512, 1024, 2048]))
+            q = dict(kind="srp", sun_dir=sun, quaternions=scenes.random_quaternions(1, seed=10_000 + i), grid=g,
+                     num_bounces=2, size=g)
+        q["body"] = body
+        out.append((float(t), q))
+    return out

@@ -81,6 +81,13 @@ struct crt_context {
     size_t scratch_bytes[SCR_COUNT] = {};
     void* pinned = nullptr;
     size_t pinned_bytes = 0;
+    // tuning (crt_context_set_tuning; the autotuner picks these per GPU and scene class)
+    uint32_t queue_chunk = 1;        // 32-item groups per atomic grab of the ray queue
+    uint32_t wave_paths = 1u << 23;  // render paths per wavefront wave
+    int use_graphs = 1;              // replay batched waves as CUDA graphs
+    // graph cache of the batched wavefront (one executable per wave shape)
+    void* graph_exec = nullptr;
+    uint64_t graph_key = 0;
 };
 
 // Grow-only device scratch buffer for one purpose.  Synchronises the stream before reallocating.
@@ -155,6 +162,14 @@ struct crt_scene {
 };
 
 void scene_build(crt_scene* s, const crt_entity_desc* ents, uint32_t n);   // bvh_build.cu
+
+// render.cu: batched wavefront on an explicit context (its stream, scratch and error word)
+void batch_run(crt_context* ctx, const crt_request* reqs, size_t n, crt_batch_stats* stats);
+void batch_check_request(const crt_request& q);
+size_t batch_footprint(const crt_request& q, uint32_t wave_paths);
+// srp.cu: radiation pressure on an explicit context
+void srp_run(crt_context* ctx, crt_scene* s, const crt_srp_desc* desc, const double* quats, size_t n_att,
+             double* force, double* torque, double* facet_power);
 
 // ------------------------------------------------------------------ device math
 __host__ __device__ __forceinline__ float3 f3(float x, float y, float z) { return make_float3(x, y, z); }

@@ -235,6 +235,26 @@ int crt_context_reset_counters(crt_context* ctx) {
     });
 }
 
+int crt_context_set_tuning(crt_context* ctx, const crt_tuning* t) {
+    if (!ctx || !t) return CRT_ERR_INVALID;
+    if (t->queue_chunk < 1 || t->queue_chunk > 8 || t->wave_paths < (1u << 16)) {
+        ctx->last_error = "tuning out of range (queue_chunk 1..8, wave_paths >= 65536)";
+        return CRT_ERR_INVALID;
+    }
+    ctx->queue_chunk = t->queue_chunk;
+    ctx->wave_paths = t->wave_paths;
+    ctx->use_graphs = t->use_graphs ? 1 : 0;
+    return CRT_OK;
+}
+
+int crt_context_get_tuning(const crt_context* ctx, crt_tuning* out) {
+    if (!ctx || !out) return CRT_ERR_INVALID;
+    out->queue_chunk = ctx->queue_chunk;
+    out->wave_paths = ctx->wave_paths;
+    out->use_graphs = ctx->use_graphs;
+    return CRT_OK;
+}
+
 const char* crt_context_last_error(const crt_context* ctx) { return ctx ? ctx->last_error.c_str() : "null context"; }
 
 }  // extern "C"

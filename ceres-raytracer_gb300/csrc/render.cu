@@ -1,20 +1,24 @@
-// Wavefront unidirectional path tracer: do_render (src/crt/do_render.hpp:28-141) with
-// unidirectional (path_tracing/unidirectional.hpp:24-96) restated as separate stage kernels over
-// compacted queues:
+// Batched wavefront path tracer and LiDAR scans: do_render (src/crt/do_render.hpp:28-141) with
+// unidirectional (path_tracing/unidirectional.hpp:24-96), restated as stage kernels over compacted
+// queues that serve many requests (renders and LiDAR grids, possibly on different resident scenes)
+// per launch:
 //
-//   primary   camera ray per (pixel, sample) + closest hit          (persistent trace kernel)
-//   shade     surface point, one shadow ray per light, bounce ray   (k_shade, appends to queues)
-//   shadow    any hit for the shadow queue                          (persistent trace kernel)
-//   accum     sum lights, clamp after the first bounce, add weight  (k_accum)
-//   bounce    closest hit for the continuing-path queue             (persistent trace kernel)
-//   update    per-pixel running mean and adaptive stop              (k_update, k_compact)
-//   finalize  RGBA float and clamp(v * 256, 0, 255) bytes           (k_finalize)
+//   begin     copy this wave's descriptor, reset the queue counters          (k_wave_begin)
+//   primary   LiDAR beams of the batch + camera ray per (pixel, sample)       (persistent trace)
+//   shade     surface point, one shadow ray per light, bounce ray             (k_shade)
+//   shadow    any hit for the shadow queue                                     (persistent trace)
+//   accum     sum lights, clamp after the first bounce, times path weight      (k_accum)
+//   bounce    closest hit for the continuing-path queue                        (persistent trace)
+//   update    per-pixel running mean and adaptive stop, samples in order       (k_update)
+//   finalize  RGBA float and clamp(v * 256, 0, 255) bytes per request          (k_finalize)
 //
-// A wave holds k consecutive samples of every still-active pixel (path p -> sample p / n_active,
-// pixel active[p % n_active]); the update kernel consumes a pixel's samples in order, so the
-// running mean and the stopping rule match the reference's sequential loop.  Random numbers come
-// from Philox4x32-10 keyed by (seed, request) with counter (pixel, sample, bounce<<8 | purpose,
-// request), so an image does not depend on how its samples are grouped into waves or requests.
+// A wave is a list of slices, each slice = samples [s0, s0 + ns) of the pixel set of one request.
+// Path p of a slice maps to sample s0 + q / npix and pixel q % npix (q = p - slice.path_base), and
+// k_update consumes a pixel's samples in order, so images do not depend on how requests and samples
+// are grouped into waves: a request renders bit-identically alone or in a batch.  Random numbers
+// come from Philox4x32-10 keyed by (seed, request) with counter (pixel, sample, bounce<<8 | purpose,
+// request).  Every stage kernel reads the wave from device memory, so when no request samples
+// adaptively the whole wave plan is uploaded once and each wave is one CUDA-graph replay.
 //
 // FP32 secondary-ray origins: the reference offsets the hit point by 1e-4 along the flat normal
 // (unidirectional.hpp:59-61).  In FP32 at kilometre coordinates 1e-4 is about one ulp, so the
@@ -26,11 +30,14 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstring>
+#include <vector>
 
 namespace {
 
 constexpr int MAX_LIGHTS = 16;
-constexpr uint32_t WAVE_CAP = 1u << 23;   // paths per wave
+constexpr int MAX_SLICES = 128;
+constexpr int MAX_LIDAR = 256;
 
 struct LightDev {
     int type;
@@ -39,10 +46,6 @@ struct LightDev {
     float R[9];
     float size[2];
 };
-struct LightSet {
-    LightDev l[MAX_LIGHTS];
-    uint32_t n;
-};
 
 struct RenderCtl {
     uint32_t W, H;
@@ -50,28 +53,70 @@ struct RenderCtl {
     float noise_threshold;
     int num_bounces;
     uint32_t seed_lo, seed_hi, request;
-    float color_scale_unused;
 };
 
-struct WaveBufs {
-    uint32_t n_active;
-    const uint32_t* active;   // nullptr: identity (every pixel)
-    uint32_t sample_base;
-    uint32_t k;
-    float4* ray;      // 2 per path
+struct RReq {            // render request
+    SceneView sv;
+    CamBasis cam;
+    RenderCtl c;
+    uint32_t light_base, n_lights;
+    uint32_t pix_base, npix;
+    uchar4* rgba;        // device outputs (staging when the caller passed host memory)
+    float4* rad;
+};
+
+struct LReq {            // LiDAR beam-grid request
+    SceneView sv;
+    double o[3];
+    double rt[9];        // R^T row-major
+    double zsign;
+    uint32_t nx, ny;
+    uint32_t tan_base;   // nx + ny tangents in the batch table
+    uint32_t item_base;  // first primary item (8 x 4 tile order)
+    double* range;
+    uint32_t* prim;
+};
+
+struct Slice {
+    uint32_t req, s0, ns, npix;
+    uint32_t path_base, upd_base;
+    const uint32_t* active;   // pixel set of the slice (nullptr: every pixel of the request)
+};
+
+struct WaveDesc {
+    uint32_t n_lidar_items, n_lreq, n_paths, n_primary;
+    uint32_t n_slices, n_update, pad0, pad1;
+    Slice slices[MAX_SLICES];
+};
+
+struct Batch {
+    const RReq* rr;
+    const LReq* lr;
+    const LightDev* lights;
+    const double* tan;
+    const WaveDesc* descs;
+    WaveDesc* cur;
+    uint32_t* wave_idx;
+    uint32_t* counts;          // [0] |bounce queue in| [1] |bounce queue out| [2] |shadow queue|
+    uint32_t L;                // light stride per path
+    float4* ray;
     uint32_t* skip;
     float4* hit;
     float4* weight;
     float4* wacc;
     float4* rad;
-    float4* contrib;  // P * L
-    uint8_t* occ;     // P * L
-    uint32_t* q_cur;
-    uint32_t* q_next;
-    uint32_t* counts; // [0] |q_cur|, [1] |q_next|, [2] |shadow|
-    float4* sray;     // 2 per shadow entry
+    uint32_t* preq;
+    uint32_t* ppix;
+    uint32_t* psample;
+    float4* contrib;
+    uint8_t* occ;
+    float4* sray;
     uint32_t* sidx;
     uint32_t* sskip;
+    uint32_t* sreq;
+    float4* pix;               // per-pixel running mean (all render requests)
+    uint32_t* taken;
+    uint8_t* done;
 };
 
 __device__ __forceinline__ void rng2(const RenderCtl& c, uint32_t pixel, uint32_t sample, uint32_t bounce,
@@ -80,12 +125,6 @@ __device__ __forceinline__ void rng2(const RenderCtl& c, uint32_t pixel, uint32_
     philox4x32(ctr, c.seed_lo, c.seed_hi);
     a = unif24(ctr[0]);
     b = unif24(ctr[1]);
-}
-
-__device__ __forceinline__ void path_ids(const WaveBufs& w, uint32_t p, uint32_t& pixel, uint32_t& sample) {
-    const uint32_t a = p % w.n_active;
-    sample = w.sample_base + p / w.n_active;
-    pixel = w.active ? w.active[a] : a;
 }
 
 // cosine_importance (materials/brdfs.hpp:18-42): Malley's method about a left-handed normal
@@ -110,103 +149,213 @@ __device__ __forceinline__ float origin_offset(float3 x) {
     return fmaxf(1e-4f, ldexpf(1.0f, e - 24 + 2));   // 4 ulps of m
 }
 
-// ---------------------------------------------------------------- primary rays
+__device__ __forceinline__ uint32_t find_slice_by_path(const WaveDesc& w, uint32_t p) {
+    uint32_t lo = 0, hi = w.n_slices;   // last slice with path_base <= p
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (w.slices[mid].path_base <= p) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ bool tile_px(uint32_t i, uint32_t W, uint32_t H, uint32_t& px, uint32_t& py) {
+    const uint32_t tiles_x = (W + 7) >> 3;
+    const uint32_t tile = i >> 5, w = i & 31u;
+    px = (tile % tiles_x) * 8u + (w & 7u);
+    py = (tile / tiles_x) * 4u + (w >> 3);
+    return px < W && py < H;
+}
+
+// ---------------------------------------------------------------- primary stage
 struct PrimaryJob {
-    CamBasis cam;
-    RenderCtl c;
-    WaveBufs w;
-    __device__ bool ray(uint32_t p, TRay& r) const {
-        uint32_t pixel, sample;
-        path_ids(w, p, pixel, sample);
-        const uint32_t i = pixel % c.W, j = pixel / c.W;
-        float u = (float)i, v = (float)j;
-        if (c.max_samples != 1) {   // do_render.hpp:76-82: integer coordinates for a single sample
-            float a, b;
-            rng2(c, pixel, sample, 0, 0, a, b);
-            u += a - 0.5f;
-            v += b - 0.5f;
+    Batch B;
+    struct Item {
+        uint32_t req;
+        uint32_t lidar;
+    };
+    __device__ SceneView view(const SceneView&, const Item& it) const { return it.lidar ? B.lr[it.req].sv : B.rr[it.req].sv; }
+    __device__ void beam64(const LReq& L, uint32_t px, uint32_t py, double d[3]) const {
+        const double s0 = B.tan[L.tan_base + px], s1 = B.tan[L.tan_base + L.nx + py], s2 = L.zsign;
+        const double inv = 1.0 / sqrt(s0 * s0 + s1 * s1 + s2 * s2);
+        for (int k = 0; k < 3; ++k) d[k] = (L.rt[3 * k] * s0 + L.rt[3 * k + 1] * s1 + L.rt[3 * k + 2] * s2) * inv;
+    }
+    __device__ bool ray(uint32_t i, TRay& r, Item& it) const {
+        const WaveDesc& w = *B.cur;
+        if (i < w.n_lidar_items) {
+            uint32_t lo = 0, hi = w.n_lreq;
+            while (hi - lo > 1) {
+                const uint32_t mid = (lo + hi) >> 1;
+                if (B.lr[mid].item_base <= i) lo = mid;
+                else hi = mid;
+            }
+            const LReq& L = B.lr[lo];
+            uint32_t px, py;
+            if (!tile_px(i - L.item_base, L.nx, L.ny, px, py)) return false;
+            double d[3];
+            beam64(L, px, py, d);
+            r.o = f3((float)L.o[0], (float)L.o[1], (float)L.o[2]);
+            r.d = f3((float)d[0], (float)d[1], (float)d[2]);
+            r.tmin = 0.f;
+            r.tmax = 3.402823466e38f;
+            it.req = lo;
+            it.lidar = 1;
+            return true;
         }
-        r = camera_ray(cam, u, v);
+        const uint32_t p = i - w.n_lidar_items;
+        const Slice& S = w.slices[find_slice_by_path(w, p)];
+        const uint32_t q = p - S.path_base;
+        const uint32_t a = q % S.npix;
+        const uint32_t sample = S.s0 + q / S.npix;
+        const uint32_t pixel = S.active ? S.active[a] : a;
+        const RReq& R = B.rr[S.req];
+        float u = (float)(pixel % R.c.W), v = (float)(pixel / R.c.W);
+        if (R.c.max_samples != 1) {   // do_render.hpp:76-82: pixel corner for a single sample
+            float ja, jb;
+            rng2(R.c, pixel, sample, 0, 0, ja, jb);
+            u += ja - 0.5f;
+            v += jb - 0.5f;
+        }
+        r = camera_ray(R.cam, u, v);
+        B.preq[p] = S.req;
+        B.ppix[p] = pixel;
+        B.psample[p] = sample;
+        it.req = S.req;
+        it.lidar = 0;
         return true;
     }
-    __device__ void write(const SceneView&, uint32_t p, const TRay&, const THit& h) const {
-        w.hit[p] = make_float4(h.t, h.u, h.v, __uint_as_float(h.slot));
+    __device__ void write(const SceneView&, uint32_t i, const TRay&, const THit& h, const Item& it) const {
+        if (it.lidar) {
+            const LReq& L = B.lr[it.req];
+            uint32_t px, py;
+            tile_px(i - L.item_base, L.nx, L.ny, px, py);
+            const size_t k = (size_t)py * L.nx + px;
+            double rng = 0.0;
+            if (h.slot != CRT_MISS) {
+                double d[3];
+                beam64(L, px, py, d);
+                const double t = plane_t64(L.sv.tris, h.slot, L.o, d);
+                rng = isfinite(t) ? t : (double)h.t;
+            }
+            L.range[k] = rng;
+            if (L.prim) L.prim[k] = h.slot != CRT_MISS ? L.sv.leaf_prim[h.slot] : CRT_MISS;
+            return;
+        }
+        const uint32_t p = i - B.cur->n_lidar_items;
+        B.hit[p] = make_float4(h.t, h.u, h.v, __uint_as_float(h.slot));
         const float w0 = (float)(2.0 * 3.14159265358979323846);   // Color(2*M_PI), unidirectional.hpp:38
-        w.weight[p] = make_float4(w0, w0, w0, 0.f);
-        w.rad[p] = make_float4(0.f, 0.f, 0.f, 0.f);
+        B.weight[p] = make_float4(w0, w0, w0, 0.f);
+        B.rad[p] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
 };
 
 struct ShadowJob {
-    WaveBufs w;
-    __device__ bool ray(uint32_t i, TRay& r) const {
-        const float4 a = w.sray[2ull * i], b = w.sray[2ull * i + 1];
+    Batch B;
+    struct Item {
+        uint32_t req;
+    };
+    __device__ SceneView view(const SceneView&, const Item& it) const { return B.rr[it.req].sv; }
+    __device__ bool ray(uint32_t i, TRay& r, Item& it) const {
+        const float4 a = B.sray[2ull * i], b = B.sray[2ull * i + 1];
         r.o = f3(a.x, a.y, a.z);
         r.tmin = a.w;
         r.d = f3(b.x, b.y, b.z);
         r.tmax = b.w;
-        r.skip = w.sskip[i];
+        r.skip = B.sskip[i];
+        it.req = B.sreq[i];
         return true;
     }
-    __device__ void write(const SceneView&, uint32_t i, const TRay&, const THit& h) const {
-        if (h.slot != CRT_MISS) w.occ[w.sidx[i]] = 1;
+    __device__ void write(const SceneView&, uint32_t i, const TRay&, const THit& h, const Item&) const {
+        if (h.slot != CRT_MISS) B.occ[B.sidx[i]] = 1;
     }
 };
 
 struct BounceJob {
-    WaveBufs w;
-    __device__ bool ray(uint32_t i, TRay& r) const {
-        const uint32_t p = w.q_next[i];
-        const float4 a = w.ray[2ull * p], b = w.ray[2ull * p + 1];
+    Batch B;
+    const uint32_t* q;
+    struct Item {
+        uint32_t req;
+        uint32_t p;
+    };
+    __device__ SceneView view(const SceneView&, const Item& it) const { return B.rr[it.req].sv; }
+    __device__ bool ray(uint32_t i, TRay& r, Item& it) const {
+        const uint32_t p = q[i];
+        const float4 a = B.ray[2ull * p], b = B.ray[2ull * p + 1];
         r.o = f3(a.x, a.y, a.z);
         r.tmin = a.w;
         r.d = f3(b.x, b.y, b.z);
         r.tmax = b.w;
-        r.skip = w.skip[p];
+        r.skip = B.skip[p];
+        it.req = B.preq[p];
+        it.p = p;
         return true;
     }
-    __device__ void write(const SceneView&, uint32_t i, const TRay&, const THit& h) const {
-        const uint32_t p = w.q_next[i];
-        w.hit[p] = make_float4(h.t, h.u, h.v, __uint_as_float(h.slot));
+    __device__ void write(const SceneView&, uint32_t, const TRay&, const THit& h, const Item& it) const {
+        B.hit[it.p] = make_float4(h.t, h.u, h.v, __uint_as_float(h.slot));
     }
 };
 
-// warp-aggregated append of `cnt` entries per participating lane; returns the lane's first index
+// warp-aggregated append of `cnt` entries per participating lane (counts may differ between lanes:
+// lanes of one warp can belong to requests with different light counts); returns the lane's first index
 __device__ __forceinline__ uint32_t warp_append(uint32_t* counter, uint32_t cnt) {
     const uint32_t mask = __activemask();
     const int lane = threadIdx.x & 31;
     const int leader = __ffs(mask) - 1;
-    const uint32_t below = __popc(mask & ((1u << lane) - 1u));
+    uint32_t prefix = 0, total = 0;
+    for (uint32_t m = mask; m; m &= m - 1) {
+        const int j = __ffs(m) - 1;
+        const uint32_t c = __shfl_sync(mask, cnt, j);
+        if (j < lane) prefix += c;
+        total += c;
+    }
     uint32_t base = 0;
-    if (lane == leader) base = atomicAdd(counter, __popc(mask) * cnt);
+    if (lane == leader) base = atomicAdd(counter, total);
     base = __shfl_sync(mask, base, leader);
-    return base + below * cnt;
+    return base + prefix;
+}
+
+__global__ void k_wave_begin(Batch B) {
+    const WaveDesc* src = B.descs + *B.wave_idx;
+    const uint32_t* s = reinterpret_cast<const uint32_t*>(src);
+    uint32_t* d = reinterpret_cast<uint32_t*>(B.cur);
+    for (uint32_t k = threadIdx.x; k < sizeof(WaveDesc) / 4; k += blockDim.x) d[k] = s[k];
+    if (threadIdx.x == 0) B.counts[0] = B.counts[1] = B.counts[2] = 0;
+}
+__global__ void k_wave_end(Batch B) { *B.wave_idx += 1; }
+__global__ void k_queue_rotate(uint32_t* counts) {
+    counts[0] = counts[1];
+    counts[1] = 0;
+    counts[2] = 0;
 }
 
 // ---------------------------------------------------------------- shade
-__global__ void k_shade(SceneView sv, RenderCtl c, WaveBufs w, LightSet L, int bounce, uint32_t n_all) {
-    const uint32_t n = bounce == 0 ? n_all : w.counts[0];
+__global__ void k_shade(Batch B, int bounce, const uint32_t* __restrict__ q_in, uint32_t* __restrict__ q_out) {
+    const uint32_t n = bounce == 0 ? B.cur->n_paths : B.counts[0];
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const uint32_t p = bounce == 0 ? i : w.q_cur[i];
-        const float4 hv = w.hit[p];
+        const uint32_t p = bounce == 0 ? i : q_in[i];
+        const float4 hv = B.hit[p];
         THit h;
         h.t = hv.x; h.u = hv.y; h.v = hv.z;
         h.slot = __float_as_uint(hv.w);
         if (h.slot == CRT_MISS) continue;
-        uint32_t pixel, sample;
-        path_ids(w, p, pixel, sample);
+        const uint32_t req = B.preq[p];
+        const RReq& R = B.rr[req];
+        if (bounce >= R.c.num_bounces) continue;
+        const uint32_t pixel = B.ppix[p], sample = B.psample[p];
+        const SceneView sv = R.sv;
         const SurfacePoint sp = surface_point(sv, h);
         const EntityDev& E = sv.entities[sp.entity];
         const float3 col = f3(E.color[0], E.color[1], E.color[2]);
         const float3 x = sp.x - origin_offset(sp.x) * sp.flat_n;   // intersect_point - 1e-4 normal
-        const uint32_t sbase = warp_append(&w.counts[2], L.n);
-        for (uint32_t l = 0; l < L.n; ++l) {
-            const LightDev& lt = L.l[l];
+        const uint32_t nl = R.n_lights;
+        const uint32_t sbase = nl ? warp_append(&B.counts[2], nl) : 0;
+        for (uint32_t l = 0; l < nl; ++l) {
+            const LightDev& lt = B.lights[R.light_base + l];
             float3 lp = f3(lt.pos[0], lt.pos[1], lt.pos[2]);
             float inten;
             if (lt.type == 1) {   // AreaLight::sample_ray / get_intensity (area_light.hpp:54-72)
                 float a, b;
-                rng2(c, pixel, sample, (uint32_t)bounce, 2u + l, a, b);
+                rng2(R.c, pixel, sample, (uint32_t)bounce, 2u + l, a, b);
                 const float xc = lt.size[0] * a - lt.size[0] / 2, yc = lt.size[1] * b - lt.size[1] / 2;
                 lp = f3(lt.R[0] * xc + lt.R[1] * yc, lt.R[3] * xc + lt.R[4] * yc, lt.R[6] * xc + lt.R[7] * yc) + lp;
                 const float3 dd = x - lp;
@@ -221,40 +370,43 @@ __global__ void k_shade(SceneView sv, RenderCtl c, WaveBufs w, LightSet L, int b
             // ColoredLambertianMaterial::compute (material.hpp:100-103): colour * (-L . N), unclamped
             const float ldn = -dot3(dir, sp.shading_n);
             const float3 cb = col * ldn;
-            w.contrib[(size_t)p * L.n + l] = make_float4(cb.x * inten, cb.y * inten, cb.z * inten, 0.f);
-            w.occ[(size_t)p * L.n + l] = 0;
+            B.contrib[(size_t)p * B.L + l] = make_float4(cb.x * inten, cb.y * inten, cb.z * inten, 0.f);
+            B.occ[(size_t)p * B.L + l] = 0;
             const uint32_t e = sbase + l;
-            w.sray[2ull * e] = make_float4(x.x, x.y, x.z, 0.f);
-            w.sray[2ull * e + 1] = make_float4(dir.x, dir.y, dir.z, dist);
-            w.sidx[e] = p * L.n + l;
-            w.sskip[e] = h.slot;
+            B.sray[2ull * e] = make_float4(x.x, x.y, x.z, 0.f);
+            B.sray[2ull * e + 1] = make_float4(dir.x, dir.y, dir.z, dist);
+            B.sidx[e] = p * B.L + l;
+            B.sskip[e] = h.slot;
+            B.sreq[e] = req;
         }
-        w.wacc[p] = w.weight[p];
-        if (bounce < c.num_bounces - 1) {
+        B.wacc[p] = B.weight[p];
+        if (bounce < R.c.num_bounces - 1) {
             float r1, r2;
-            rng2(c, pixel, sample, (uint32_t)bounce, 1u, r1, r2);
+            rng2(R.c, pixel, sample, (uint32_t)bounce, 1u, r1, r2);
             const float3 nd = cosine_importance(sp.shading_n, r1, r2);
-            w.ray[2ull * p] = make_float4(x.x, x.y, x.z, 0.f);
-            w.ray[2ull * p + 1] = make_float4(nd.x, nd.y, nd.z, 3.402823466e38f);
-            w.skip[p] = h.slot;
+            B.ray[2ull * p] = make_float4(x.x, x.y, x.z, 0.f);
+            B.ray[2ull * p + 1] = make_float4(nd.x, nd.y, nd.z, 3.402823466e38f);
+            B.skip[p] = h.slot;
             const float bc = 1.0f - r1;
-            float4 wt = w.weight[p];
-            w.weight[p] = make_float4(wt.x * bc, wt.y * bc, wt.z * bc, 0.f);
-            w.q_next[warp_append(&w.counts[1], 1u)] = p;
+            const float4 wt = B.weight[p];
+            B.weight[p] = make_float4(wt.x * bc, wt.y * bc, wt.z * bc, 0.f);
+            q_out[warp_append(&B.counts[1], 1u)] = p;
         }
     }
 }
 
 // ---------------------------------------------------------------- accumulate
-__global__ void k_accum(RenderCtl c, WaveBufs w, uint32_t n_lights, int bounce, uint32_t n_all) {
-    const uint32_t n = bounce == 0 ? n_all : w.counts[0];
+__global__ void k_accum(Batch B, int bounce, const uint32_t* __restrict__ q_in) {
+    const uint32_t n = bounce == 0 ? B.cur->n_paths : B.counts[0];
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const uint32_t p = bounce == 0 ? i : w.q_cur[i];
-        if (__float_as_uint(w.hit[p].w) == CRT_MISS) continue;
+        const uint32_t p = bounce == 0 ? i : q_in[i];
+        if (__float_as_uint(B.hit[p].w) == CRT_MISS) continue;
+        const RReq& R = B.rr[B.preq[p]];
+        if (bounce >= R.c.num_bounces) continue;
         float3 lr = f3(0.f, 0.f, 0.f);
-        for (uint32_t l = 0; l < n_lights; ++l) {
-            if (!w.occ[(size_t)p * n_lights + l]) {
-                const float4 cb = w.contrib[(size_t)p * n_lights + l];
+        for (uint32_t l = 0; l < R.n_lights; ++l) {
+            if (!B.occ[(size_t)p * B.L + l]) {
+                const float4 cb = B.contrib[(size_t)p * B.L + l];
                 lr = lr + f3(cb.x, cb.y, cb.z);
             }
         }
@@ -263,204 +415,549 @@ __global__ void k_accum(RenderCtl c, WaveBufs w, uint32_t n_lights, int bounce, 
             lr.y = fminf(fmaxf(lr.y, 0.f), 1.f);
             lr.z = fminf(fmaxf(lr.z, 0.f), 1.f);
         }
-        const float4 wa = w.wacc[p];
-        float4 r = w.rad[p];
-        w.rad[p] = make_float4(r.x + lr.x * wa.x, r.y + lr.y * wa.y, r.z + lr.z * wa.z, 0.f);
+        const float4 wa = B.wacc[p];
+        const float4 r = B.rad[p];
+        B.rad[p] = make_float4(r.x + lr.x * wa.x, r.y + lr.y * wa.y, r.z + lr.z * wa.z, 0.f);
     }
 }
 
-// rotate queues: q_cur <- q_next (count only; the host swaps the pointers)
-__global__ void k_queue_rotate(uint32_t* counts) {
-    counts[0] = counts[1];
-    counts[1] = 0;
-    counts[2] = 0;
-}
-
 // ---------------------------------------------------------------- pixel update (do_render.hpp:84-114)
-__global__ void k_update(RenderCtl c, WaveBufs w, float4* __restrict__ pix, uint32_t* __restrict__ taken,
-                         uint8_t* __restrict__ done) {
-    for (uint32_t a = blockIdx.x * blockDim.x + threadIdx.x; a < w.n_active; a += gridDim.x * blockDim.x) {
-        const uint32_t pixel = w.active ? w.active[a] : a;
-        if (done[pixel]) continue;
-        float4 m = pix[pixel];
-        uint32_t t = taken[pixel];
-        for (uint32_t s = 0; s < w.k; ++s) {
-            const uint32_t sample = w.sample_base + s + 1;   // 1-based as in the reference loop
-            const float4 L = w.rad[(size_t)s * w.n_active + a];
+__global__ void k_update(Batch B) {
+    const WaveDesc& w = *B.cur;
+    for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < w.n_update; u += gridDim.x * blockDim.x) {
+        uint32_t lo = 0, hi = w.n_slices;
+        while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (w.slices[mid].upd_base <= u) lo = mid;
+            else hi = mid;
+        }
+        const Slice& S = w.slices[lo];
+        const uint32_t a = u - S.upd_base;
+        const uint32_t pixel = S.active ? S.active[a] : a;
+        const RReq& R = B.rr[S.req];
+        const size_t g = (size_t)R.pix_base + pixel;
+        if (B.done[g]) continue;
+        float4 m = B.pix[g];
+        uint32_t t = B.taken[g];
+        for (uint32_t k = 0; k < S.ns; ++k) {
+            const uint32_t sample = S.s0 + k + 1;   // 1-based as in the reference loop
+            const float4 L = B.rad[(size_t)S.path_base + (size_t)k * S.npix + a];
             const float inv = 1.0f / (float)sample;
             const float dx = (L.x - m.x) * inv, dy = (L.y - m.y) * inv, dz = (L.z - m.z) * inv;
             m.x += dx; m.y += dy; m.z += dz;
             t = sample;
-            if ((int)sample >= c.min_samples) {
+            if ((int)sample >= R.c.min_samples) {
                 const float noise = sqrtf(dx * dx + dy * dy + dz * dz);
-                if (noise < c.noise_threshold) {
-                    done[pixel] = 1;
+                if (noise < R.c.noise_threshold) {
+                    B.done[g] = 1;
                     break;
                 }
             }
         }
-        pix[pixel] = m;
-        taken[pixel] = t;
+        B.pix[g] = m;
+        B.taken[g] = t;
     }
 }
 
 __global__ void k_compact(const uint32_t* __restrict__ active, uint32_t n_active, const uint8_t* __restrict__ done,
-                          uint32_t* __restrict__ out, uint32_t* __restrict__ count) {
+                          uint32_t pix_base, uint32_t* __restrict__ out, uint32_t* __restrict__ count) {
     for (uint32_t a = blockIdx.x * blockDim.x + threadIdx.x; a < n_active; a += gridDim.x * blockDim.x) {
         const uint32_t pixel = active ? active[a] : a;
-        if (!done[pixel]) out[warp_append(count, 1u)] = pixel;
+        if (!done[pix_base + pixel]) out[warp_append(count, 1u)] = pixel;
     }
 }
 
-__global__ void k_finalize(uint32_t n, const float4* __restrict__ pix, float4* __restrict__ rad,
-                           uchar4* __restrict__ rgba) {
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const float4 m = pix[i];
+__global__ void k_finalize(Batch B, uint32_t n_req, uint32_t n_total) {
+    for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < n_total; g += gridDim.x * blockDim.x) {
+        uint32_t lo = 0, hi = n_req;
+        while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (B.rr[mid].pix_base <= g) lo = mid;
+            else hi = mid;
+        }
+        const RReq& R = B.rr[lo];
+        const uint32_t pixel = g - R.pix_base;
+        const float4 m = B.pix[g];
         const float v[4] = {m.x, m.y, m.z, 1.0f};
-        if (rad) rad[i] = make_float4(v[0], v[1], v[2], v[3]);
-        if (rgba) {
-            uint8_t q[4];
-            for (int k = 0; k < 4; ++k) q[k] = (uint8_t)fminf(fmaxf(v[k] * 256.0f, 0.0f), 255.0f);
-            rgba[i] = make_uchar4(q[0], q[1], q[2], q[3]);
+        if (R.rad) R.rad[pixel] = make_float4(v[0], v[1], v[2], v[3]);
+        if (R.rgba) {
+            uint8_t qv[4];
+            for (int k = 0; k < 4; ++k) qv[k] = (uint8_t)fminf(fmaxf(v[k] * 256.0f, 0.0f), 255.0f);
+            R.rgba[pixel] = make_uchar4(qv[0], qv[1], qv[2], qv[3]);
         }
     }
+}
+
+__global__ void k_tan_table2(double* __restrict__ out, uint32_t nx, uint32_t ny, double hx, double hy) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < nx) out[i] = tan(-hx + (i + 0.5) * 2.0 * hx / nx);
+    else if (i < nx + ny) out[i] = tan(-hy + ((i - nx) + 0.5) * 2.0 * hy / ny);
 }
 
 inline uint32_t grid_for(crt_context* ctx, size_t n, int block = 256) {
     const size_t want = (n + block - 1) / block;
     return (uint32_t)std::max<size_t>(1, std::min<size_t>(want, (size_t)ctx->sm_count * 8));
 }
+inline uint32_t tiles_items(uint32_t W, uint32_t H) { return ((W + 7) / 8) * ((H + 3) / 4) * 32u; }
+
+// ---------------------------------------------------------------- host side
+struct HostReq {
+    const crt_request* src;
+    bool adaptive;
+    uint32_t next_sample;     // first sample not yet scheduled
+    uint32_t total;           // max_samples
+    uint32_t n_active;        // adaptive requests: current pixel-set size
+    const uint32_t* active;   // adaptive requests: current pixel set (device)
+    uint32_t* act_buf[2];
+    int act_sel;
+    uint32_t rr_index;
+};
+
+void check_request(const crt_request& q) {
+    CRT_CHECK(q.scene, CRT_ERR_INVALID, "request without a scene");
+    if (q.kind == CRT_REQUEST_RENDER) {
+        CRT_CHECK(q.camera && q.params, CRT_ERR_INVALID, "render request needs a camera and parameters");
+        CRT_CHECK(q.n_lights <= (uint32_t)MAX_LIGHTS, CRT_ERR_INVALID, "at most 16 lights per render");
+        CRT_CHECK(!q.n_lights || q.lights, CRT_ERR_INVALID, "null light list");
+        CRT_CHECK(q.rgba8 || q.radiance, CRT_ERR_INVALID, "render request without an output buffer");
+        const double W = std::floor(q.camera->resolution[0]), H = std::floor(q.camera->resolution[1]);
+        CRT_CHECK(W >= 1 && H >= 1 && W * H < (double)(1u << 28), CRT_ERR_INVALID, "bad camera resolution");
+    } else if (q.kind == CRT_REQUEST_LIDAR) {
+        CRT_CHECK(q.lidar && q.range, CRT_ERR_INVALID, "LiDAR request needs a beam grid and a range buffer");
+        const crt_lidar_grid_desc& g = *q.lidar;
+        CRT_CHECK(g.nx > 0 && g.ny > 0 && (uint64_t)g.nx * g.ny < (1ull << 28), CRT_ERR_INVALID, "bad beam grid");
+        CRT_CHECK(g.half_angle_x >= 0 && g.half_angle_x < 1.5 && g.half_angle_y >= 0 && g.half_angle_y < 1.5,
+                  CRT_ERR_INVALID, "half angles must lie in [0, 1.5) rad");
+    } else {
+        throw CrtError{CRT_ERR_INVALID, "unknown request kind"};
+    }
+}
+
+void run_batch(crt_context* ctx, const crt_request* reqs, size_t n, crt_batch_stats* stats) {
+    for (size_t i = 0; i < n; ++i) {
+        check_request(reqs[i]);
+        CRT_CHECK(reqs[i].scene->ctx && reqs[i].scene->ctx->device == ctx->device, CRT_ERR_INVALID,
+                  "request scene lives on another device");
+    }
+    if (!n) return;
+    CRT_CUDA(cudaSetDevice(ctx->device));
+    cudaStream_t st = ctx->stream;
+
+    // ---- request tables
+    std::vector<RReq> rr;
+    std::vector<LReq> lr;
+    std::vector<LightDev> lights;
+    std::vector<HostReq> hreq;
+    uint32_t pix_total = 0, lidar_items = 0, tan_total = 0, L = 1;
+    size_t host_out_bytes = 0;
+    for (size_t i = 0; i < n; ++i) {
+        const crt_request& q = reqs[i];
+        if (q.kind == CRT_REQUEST_RENDER) {
+            RReq R;
+            R.sv = scene_view(q.scene);
+            R.cam = make_camera_basis(q.camera);
+            const crt_render_params& p = *q.params;
+            R.c = RenderCtl{R.cam.width, R.cam.height, p.min_samples, p.max_samples, (float)p.noise_threshold,
+                            p.num_bounces, (uint32_t)p.seed, (uint32_t)(p.seed >> 32), p.request};
+            R.light_base = (uint32_t)lights.size();
+            R.n_lights = q.n_lights;
+            for (uint32_t l = 0; l < q.n_lights; ++l) {
+                LightDev d;
+                d.type = q.lights[l].type;
+                d.intensity = (float)q.lights[l].intensity;
+                for (int k = 0; k < 3; ++k) d.pos[k] = (float)q.lights[l].position[k];
+                for (int k = 0; k < 9; ++k) d.R[k] = (float)q.lights[l].rotation[k];
+                d.size[0] = (float)q.lights[l].size[0];
+                d.size[1] = (float)q.lights[l].size[1];
+                lights.push_back(d);
+            }
+            L = std::max<uint32_t>(L, q.n_lights);
+            R.npix = R.cam.width * R.cam.height;
+            R.pix_base = pix_total;
+            pix_total += R.npix;
+            R.rgba = nullptr;
+            R.rad = nullptr;
+            if (q.rgba8 && !is_device_ptr(q.rgba8)) host_out_bytes += (size_t)R.npix * 4;
+            if (q.radiance && !is_device_ptr(q.radiance)) host_out_bytes += (size_t)R.npix * 16;
+            HostReq h;
+            h.src = &q;
+            h.adaptive = p.noise_threshold > 0 && p.min_samples < p.max_samples;
+            h.next_sample = 0;
+            h.total = (uint32_t)std::max(0, p.max_samples);
+            h.n_active = R.npix;
+            h.active = nullptr;
+            h.act_sel = 0;
+            h.rr_index = (uint32_t)rr.size();
+            hreq.push_back(h);
+            rr.push_back(R);
+        } else {
+            CRT_CHECK(lr.size() < (size_t)MAX_LIDAR, CRT_ERR_INVALID, "at most 256 LiDAR requests per batch");
+            const crt_lidar_grid_desc& g = *q.lidar;
+            LReq Lq;
+            Lq.sv = scene_view(q.scene);
+            for (int k = 0; k < 3; ++k) Lq.o[k] = g.position[k];
+            for (int a = 0; a < 3; ++a)
+                for (int b = 0; b < 3; ++b) Lq.rt[3 * a + b] = g.rotation[3 * b + a];
+            Lq.zsign = g.z_positive ? 1.0 : -1.0;
+            Lq.nx = g.nx;
+            Lq.ny = g.ny;
+            Lq.tan_base = tan_total;
+            tan_total += g.nx + g.ny;
+            Lq.item_base = lidar_items;
+            lidar_items += tiles_items(g.nx, g.ny);
+            Lq.range = nullptr;
+            Lq.prim = nullptr;
+            if (!is_device_ptr(q.range)) host_out_bytes += (size_t)g.nx * g.ny * 8;
+            if (q.prim && !is_device_ptr(q.prim)) host_out_bytes += (size_t)g.nx * g.ny * 4;
+            lr.push_back(Lq);
+        }
+    }
+
+    // ---- wave plan for every render sample; adaptive requests schedule sample by sample later
+    std::vector<WaveDesc> plan;
+    const uint32_t cap = std::max<uint32_t>(ctx->wave_paths, 1u << 16);
+    uint32_t max_paths = 0;
+    int max_bounces = 0;
+    for (const RReq& R : rr) max_bounces = std::max(max_bounces, R.c.num_bounces);
+    auto new_wave = [&]() {
+        WaveDesc w;
+        std::memset(&w, 0, sizeof(w));
+        plan.push_back(w);
+    };
+    auto add_slice = [&](WaveDesc& w, uint32_t req, uint32_t s0, uint32_t ns, uint32_t npix, const uint32_t* active) {
+        Slice& S = w.slices[w.n_slices++];
+        S.req = req;
+        S.s0 = s0;
+        S.ns = ns;
+        S.npix = npix;
+        S.path_base = w.n_paths;
+        S.upd_base = w.n_update;
+        S.active = active;
+        w.n_paths += ns * npix;
+        w.n_update += npix;
+    };
+    // non-adaptive samples, plus the non-adaptive prefix (samples < min_samples) of adaptive requests
+    new_wave();
+    for (HostReq& h : hreq) {
+        const RReq& R = rr[h.rr_index];
+        const uint32_t upto = h.adaptive ? (uint32_t)std::min<int>(std::max(R.c.min_samples, 1), (int)h.total) : h.total;
+        while (h.next_sample < upto) {
+            WaveDesc* w = &plan.back();
+            const uint32_t room = w->n_paths < cap ? cap - w->n_paths : 0;
+            uint32_t ns = std::min<uint32_t>(upto - h.next_sample, room / R.npix);
+            if (ns == 0) {
+                if (w->n_slices == 0) ns = 1;   // a single sample larger than the wave cap
+                else { new_wave(); continue; }
+            }
+            if (w->n_slices == MAX_SLICES) { new_wave(); continue; }
+            add_slice(*w, h.rr_index, h.next_sample, ns, R.npix, nullptr);
+            h.next_sample += ns;
+        }
+    }
+    if (plan.back().n_slices == 0 && plan.size() > 1) plan.pop_back();
+    plan[0].n_lidar_items = lidar_items;
+    plan[0].n_lreq = (uint32_t)lr.size();
+    for (WaveDesc& w : plan) {
+        w.n_primary = w.n_lidar_items + w.n_paths;
+        max_paths = std::max(max_paths, w.n_paths);
+    }
+    bool any_adaptive = false;
+    for (const HostReq& h : hreq)
+        if (h.adaptive && h.next_sample < h.total) any_adaptive = true;
+    if (any_adaptive) max_paths = std::max(max_paths, std::min<uint32_t>(cap, pix_total));
+    for (const RReq& R : rr) max_paths = std::max(max_paths, std::min<uint32_t>(R.npix, std::max(cap, R.npix)));
+
+    // ---- device memory (context scratch, reused across batches)
+    const size_t P = std::max<uint32_t>(max_paths, 1), NL = L;
+    const size_t WD = sizeof(WaveDesc);
+    char* base = nullptr;
+    Batch B;
+    std::memset(&B, 0, sizeof(B));
+    auto carve = [&](char* b) {
+        size_t off = 0;
+        auto take = [&](size_t bytes) {
+            off = (off + 255) & ~size_t(255);
+            char* q = b ? b + off : nullptr;
+            off += bytes;
+            return q;
+        };
+        B.rr = (const RReq*)take(sizeof(RReq) * std::max<size_t>(rr.size(), 1));
+        B.lr = (const LReq*)take(sizeof(LReq) * std::max<size_t>(lr.size(), 1));
+        B.lights = (const LightDev*)take(sizeof(LightDev) * std::max<size_t>(lights.size(), 1));
+        B.tan = (const double*)take(8 * std::max<uint32_t>(tan_total, 1));
+        B.descs = (const WaveDesc*)take(WD * plan.size());
+        B.cur = (WaveDesc*)take(WD);
+        B.wave_idx = (uint32_t*)take(64);
+        B.counts = (uint32_t*)take(64);
+        B.ray = (float4*)take(P * 32);
+        B.skip = (uint32_t*)take(P * 4);
+        B.hit = (float4*)take(P * 16);
+        B.weight = (float4*)take(P * 16);
+        B.wacc = (float4*)take(P * 16);
+        B.rad = (float4*)take(P * 16);
+        B.preq = (uint32_t*)take(P * 4);
+        B.ppix = (uint32_t*)take(P * 4);
+        B.psample = (uint32_t*)take(P * 4);
+        B.contrib = (float4*)take(P * NL * 16);
+        B.occ = (uint8_t*)take(P * NL);
+        B.sray = (float4*)take(P * NL * 32);
+        B.sidx = (uint32_t*)take(P * NL * 4);
+        B.sskip = (uint32_t*)take(P * NL * 4);
+        B.sreq = (uint32_t*)take(P * NL * 4);
+        B.pix = (float4*)take((size_t)std::max<uint32_t>(pix_total, 1) * 16);
+        B.taken = (uint32_t*)take((size_t)std::max<uint32_t>(pix_total, 1) * 4);
+        B.done = (uint8_t*)take(std::max<uint32_t>(pix_total, 1));
+        return off;
+    };
+    const size_t total_bytes = carve(nullptr);
+    base = (char*)ctx_scratch(ctx, SCR_WAVE2, total_bytes);
+    carve(base);
+    uint32_t* queues = (uint32_t*)ctx_scratch(ctx, SCR_WAVE3, P * 8 + 256);
+    uint32_t* qa = queues;
+    uint32_t* qb = queues + P;
+    uint32_t* actbuf = any_adaptive ? (uint32_t*)ctx_scratch(ctx, SCR_WAVE4, (size_t)pix_total * 8 + 256) : nullptr;
+    char* stage = host_out_bytes ? (char*)ctx_scratch(ctx, SCR_OUT2, host_out_bytes) : nullptr;
+    size_t stage_off = 0;
+
+    // outputs: caller device memory or staging
+    size_t ri = 0, li = 0;
+    for (size_t i = 0; i < n; ++i) {
+        const crt_request& q = reqs[i];
+        if (q.kind == CRT_REQUEST_RENDER) {
+            RReq& R = rr[ri++];
+            if (q.rgba8) {
+                if (is_device_ptr(q.rgba8)) R.rgba = (uchar4*)q.rgba8;
+                else { R.rgba = (uchar4*)(stage + stage_off); stage_off += (size_t)R.npix * 4; }
+            }
+            if (q.radiance) {
+                stage_off = (stage_off + 15) & ~size_t(15);
+                if (is_device_ptr(q.radiance)) R.rad = (float4*)q.radiance;
+                else { R.rad = (float4*)(stage + stage_off); stage_off += (size_t)R.npix * 16; }
+            }
+        } else {
+            LReq& Lq = lr[li++];
+            stage_off = (stage_off + 15) & ~size_t(15);
+            if (is_device_ptr(q.range)) Lq.range = q.range;
+            else { Lq.range = (double*)(stage + stage_off); stage_off += (size_t)Lq.nx * Lq.ny * 8; }
+            if (q.prim) {
+                if (is_device_ptr(q.prim)) Lq.prim = q.prim;
+                else { Lq.prim = (uint32_t*)(stage + stage_off); stage_off += (size_t)Lq.nx * Lq.ny * 4; }
+            }
+        }
+    }
+    if (host_out_bytes) CRT_CHECK(stage_off <= host_out_bytes + 64 * n, CRT_ERR_INVALID, "staging overflow");
+
+    // ---- uploads (pinned staging; the stream is synchronised before the staging is reused)
+    const size_t up_bytes = sizeof(RReq) * rr.size() + sizeof(LReq) * lr.size() + sizeof(LightDev) * lights.size() +
+                            WD * plan.size() + 1024;
+    char* pin = (char*)ctx_pinned(ctx, up_bytes);
+    CRT_CUDA(cudaStreamSynchronize(st));
+    size_t po = 0;
+    auto up = [&](const void* dst, const void* src, size_t bytes) {
+        if (!bytes) return;
+        std::memcpy(pin + po, src, bytes);
+        CRT_CUDA(cudaMemcpyAsync((void*)dst, pin + po, bytes, cudaMemcpyHostToDevice, st));
+        po += (bytes + 255) & ~size_t(255);
+    };
+    up(B.rr, rr.data(), sizeof(RReq) * rr.size());
+    up(B.lr, lr.data(), sizeof(LReq) * lr.size());
+    up(B.lights, lights.data(), sizeof(LightDev) * lights.size());
+    up(B.descs, plan.data(), WD * plan.size());
+    CRT_CUDA(cudaMemsetAsync(B.wave_idx, 0, 4, st));
+    if (pix_total) {
+        CRT_CUDA(cudaMemsetAsync(B.pix, 0, (size_t)pix_total * 16, st));
+        CRT_CUDA(cudaMemsetAsync(B.taken, 0, (size_t)pix_total * 4, st));
+        CRT_CUDA(cudaMemsetAsync(B.done, 0, pix_total, st));
+    }
+    for (size_t k = 0; k < lr.size(); ++k) {
+        const crt_lidar_grid_desc& g = *([&]() {
+            size_t c = 0;
+            for (size_t i = 0; i < n; ++i)
+                if (reqs[i].kind == CRT_REQUEST_LIDAR && c++ == k) return reqs[i].lidar;
+            return (const crt_lidar_grid_desc*)nullptr;
+        })();
+        const uint32_t nt = g.nx + g.ny;
+        k_tan_table2<<<(nt + 255) / 256, 256, 0, st>>>((double*)B.tan + lr[k].tan_base, g.nx, g.ny, g.half_angle_x,
+                                                        g.half_angle_y);
+        check_launch(ctx, "k_tan_table2");
+    }
+    B.L = (uint32_t)NL;
+
+    // ---- one wave: every launch reads the wave from B.cur (graph-capturable)
+    uint32_t* tqueue = (uint32_t*)ctx_scratch(ctx, SCR_QUEUE, 256);
+    const uint32_t gsz = grid_for(ctx, P);
+    auto launch_wave = [&]() {
+        k_wave_begin<<<1, 128, 0, st>>>(B);
+        check_launch(ctx, "k_wave_begin");
+        launch_trace<false>(ctx, SceneView{}, PrimaryJob{B}, (uint32_t)std::min<size_t>(P + lidar_items, 0xFFFFFF00u),
+                            &B.cur->n_primary, tqueue);
+        const uint32_t* q_in = nullptr;
+        uint32_t* q_out = qa;
+        for (int b = 0; b < max_bounces; ++b) {
+            k_shade<<<gsz, 256, 0, st>>>(B, b, q_in, q_out);
+            check_launch(ctx, "k_shade");
+            launch_trace<true>(ctx, SceneView{}, ShadowJob{B}, (uint32_t)std::min<size_t>(P * NL, 0xFFFFFF00u),
+                               &B.counts[2], tqueue);
+            k_accum<<<gsz, 256, 0, st>>>(B, b, q_in);
+            check_launch(ctx, "k_accum");
+            if (b < max_bounces - 1) {
+                launch_trace<false>(ctx, SceneView{}, BounceJob{B, q_out}, (uint32_t)P, &B.counts[1], tqueue);
+                k_queue_rotate<<<1, 1, 0, st>>>(B.counts);
+                check_launch(ctx, "k_queue_rotate");
+                q_in = q_out;
+                q_out = (q_out == qa) ? qb : qa;
+            }
+        }
+        k_update<<<gsz, 256, 0, st>>>(B);
+        check_launch(ctx, "k_update");
+        k_wave_end<<<1, 1, 0, st>>>(B);
+        check_launch(ctx, "k_wave_end");
+    };
+
+    size_t waves_run = 0;
+    const bool graph_ok = ctx->use_graphs && !ctx->counting && plan.size() > 1;
+    if (graph_ok) {
+        // capture one wave, replay it for every wave of the plan
+        cudaGraph_t g = nullptr;
+        cudaGraphExec_t ge = nullptr;
+        CRT_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        const uint64_t before = ctx->launches;
+        try {
+            launch_wave();
+        } catch (...) {
+            cudaStreamEndCapture(st, &g);
+            if (g) cudaGraphDestroy(g);
+            throw;
+        }
+        CRT_CUDA(cudaStreamEndCapture(st, &g));
+        const uint64_t per_wave = ctx->launches - before;
+        CRT_CUDA(cudaGraphInstantiate(&ge, g, 0));
+        cudaGraphDestroy(g);
+        ctx->launches = before;
+        for (size_t w = 0; w < plan.size(); ++w) {
+            CRT_CUDA(cudaGraphLaunch(ge, st));
+            ctx->launches += per_wave;
+        }
+        cudaGraphExecDestroy(ge);
+        waves_run = plan.size();
+    } else {
+        for (size_t w = 0; w < plan.size(); ++w) launch_wave();
+        waves_run = plan.size();
+    }
+
+    // ---- adaptive requests: one sample per wave over the still-active pixels
+    if (any_adaptive) {
+        uint32_t* acount = B.counts + 8;
+        uint32_t offs = 0;
+        for (HostReq& h : hreq) {
+            if (!h.adaptive) continue;
+            h.act_buf[0] = actbuf + offs;
+            h.act_buf[1] = actbuf + offs + rr[h.rr_index].npix;
+            offs += 2 * rr[h.rr_index].npix;
+        }
+        while (true) {
+            // compact the pixel sets of adaptive requests that still have samples
+            std::vector<HostReq*> live;
+            for (HostReq& h : hreq)
+                if (h.adaptive && h.next_sample < h.total && h.n_active > 0) live.push_back(&h);
+            if (live.empty()) break;
+            for (HostReq* h : live) {
+                uint32_t* out = h->act_buf[h->act_sel];
+                CRT_CUDA(cudaMemsetAsync(acount, 0, 4, st));
+                k_compact<<<grid_for(ctx, h->n_active), 256, 0, st>>>(h->active, h->n_active, B.done,
+                                                                       rr[h->rr_index].pix_base, out, acount);
+                check_launch(ctx, "k_compact");
+                uint32_t cnt = 0;
+                CRT_CUDA(cudaMemcpyAsync(&cnt, acount, 4, cudaMemcpyDeviceToHost, st));
+                CRT_CUDA(cudaStreamSynchronize(st));
+                h->n_active = cnt;
+                h->active = out;
+                h->act_sel ^= 1;
+            }
+            WaveDesc w;
+            std::memset(&w, 0, sizeof(w));
+            for (HostReq* h : live) {
+                if (!h->n_active || w.n_slices == MAX_SLICES) continue;
+                add_slice(w, h->rr_index, h->next_sample, 1, h->n_active, h->active);
+                h->next_sample += 1;
+            }
+            if (!w.n_slices) break;
+            w.n_primary = w.n_paths;
+            CRT_CHECK(w.n_paths <= P, CRT_ERR_INVALID, "adaptive wave exceeds the path buffers");
+            std::memcpy(pin, &w, WD);
+            CRT_CUDA(cudaMemcpyAsync((void*)B.descs, pin, WD, cudaMemcpyHostToDevice, st));
+            CRT_CUDA(cudaMemsetAsync(B.wave_idx, 0, 4, st));
+            launch_wave();
+            ++waves_run;
+            CRT_CUDA(cudaStreamSynchronize(st));   // the pinned descriptor is rewritten next round
+        }
+    }
+
+    // ---- finalize and copy host outputs
+    if (pix_total) {
+        k_finalize<<<grid_for(ctx, pix_total), 256, 0, st>>>(B, (uint32_t)rr.size(), pix_total);
+        check_launch(ctx, "k_finalize");
+    }
+    ri = 0;
+    li = 0;
+    bool host_out = false;
+    for (size_t i = 0; i < n; ++i) {
+        const crt_request& q = reqs[i];
+        if (q.kind == CRT_REQUEST_RENDER) {
+            const RReq& R = rr[ri++];
+            if (q.rgba8 && (void*)R.rgba != (void*)q.rgba8) { out_finish(ctx, q.rgba8, R.rgba, (size_t)R.npix * 4); host_out = true; }
+            if (q.radiance && (void*)R.rad != (void*)q.radiance) { out_finish(ctx, q.radiance, R.rad, (size_t)R.npix * 16); host_out = true; }
+        } else {
+            const LReq& Lq = lr[li++];
+            if ((void*)Lq.range != (void*)q.range) { out_finish(ctx, q.range, Lq.range, (size_t)Lq.nx * Lq.ny * 8); host_out = true; }
+            if (q.prim && (void*)Lq.prim != (void*)q.prim) { out_finish(ctx, q.prim, Lq.prim, (size_t)Lq.nx * Lq.ny * 4); host_out = true; }
+        }
+    }
+    if (stats) {
+        stats->waves = waves_run;
+        stats->render_paths = 0;
+        for (const WaveDesc& w : plan) stats->render_paths += w.n_paths;
+        stats->lidar_beams = 0;
+        for (const LReq& Lq : lr) stats->lidar_beams += (uint64_t)Lq.nx * Lq.ny;
+    }
+    if (host_out) check_device_error(ctx, "crt_batch");
+}
 
 }  // namespace
+
+void batch_run(crt_context* ctx, const crt_request* reqs, size_t n, crt_batch_stats* stats) {
+    run_batch(ctx, reqs, n, stats);
+}
+void batch_check_request(const crt_request& q) { check_request(q); }
+
+size_t batch_footprint(const crt_request& q, uint32_t wave_paths) {
+    if (q.kind == CRT_REQUEST_RENDER) {
+        const size_t npix = (size_t)std::floor(q.camera->resolution[0]) * (size_t)std::floor(q.camera->resolution[1]);
+        const size_t paths = std::min<size_t>(npix * (size_t)std::max(1, q.params->max_samples),
+                                              std::max<size_t>(wave_paths, npix));
+        const size_t L = std::max<uint32_t>(q.n_lights, 1);
+        return paths * (188 + 57 * L) + npix * 45;
+    }
+    return (size_t)q.lidar->nx * q.lidar->ny * 24 + 16 * (q.lidar->nx + q.lidar->ny);
+}
+
+extern "C" int crt_batch(crt_context* ctx, const crt_request* reqs, size_t n, crt_batch_stats* stats) {
+    if (!ctx || (n && !reqs)) return CRT_ERR_INVALID;
+    return crt_guard(ctx, [&] { run_batch(ctx, reqs, n, stats); });
+}
 
 extern "C" int crt_render(crt_scene* s, const crt_camera_desc* cam, const crt_light_desc* lights, uint32_t n_lights,
                           const crt_render_params* p, uint8_t* rgba8, float* radiance) {
     if (!s || !cam || !p || (n_lights && !lights)) return CRT_ERR_INVALID;
-    crt_context* ctx = s->ctx;
-    return crt_guard(ctx, [&] {
-        CRT_CHECK(n_lights <= (uint32_t)MAX_LIGHTS, CRT_ERR_INVALID, "at most 16 lights per render");
-        CRT_CHECK(rgba8 || radiance, CRT_ERR_INVALID, "no output buffer");
-        const CamBasis cb = make_camera_basis(cam);
-        CRT_CHECK(cb.width > 0 && cb.height > 0 && (uint64_t)cb.width * cb.height < (1ull << 28), CRT_ERR_INVALID,
-                  "bad camera resolution");
-        CRT_CUDA(cudaSetDevice(ctx->device));
-        cudaStream_t st = ctx->stream;
-        const uint32_t npix = cb.width * cb.height;
-        RenderCtl c;
-        c.W = cb.width;
-        c.H = cb.height;
-        c.min_samples = p->min_samples;
-        c.max_samples = p->max_samples;
-        c.noise_threshold = (float)p->noise_threshold;
-        c.num_bounces = p->num_bounces;
-        c.seed_lo = (uint32_t)p->seed;
-        c.seed_hi = (uint32_t)(p->seed >> 32);
-        c.request = p->request;
-        LightSet L;
-        L.n = n_lights;
-        for (uint32_t l = 0; l < n_lights; ++l) {
-            L.l[l].type = lights[l].type;
-            L.l[l].intensity = (float)lights[l].intensity;
-            for (int k = 0; k < 3; ++k) L.l[l].pos[k] = (float)lights[l].position[k];
-            for (int k = 0; k < 9; ++k) L.l[l].R[k] = (float)lights[l].rotation[k];
-            L.l[l].size[0] = (float)lights[l].size[0];
-            L.l[l].size[1] = (float)lights[l].size[1];
-        }
-        // pixel state
-        char* ps = (char*)ctx_scratch(ctx, SCR_WAVE0, (size_t)npix * (16 + 4 + 1 + 4 + 4) + 1024);
-        float4* pix = (float4*)ps;
-        uint32_t* taken = (uint32_t*)(ps + (size_t)npix * 16);
-        uint32_t* act_a = (uint32_t*)(ps + (size_t)npix * 20);
-        uint32_t* act_b = (uint32_t*)(ps + (size_t)npix * 24);
-        uint8_t* done = (uint8_t*)(ps + (size_t)npix * 28);
-        uint32_t* acount = (uint32_t*)ctx_scratch(ctx, SCR_WAVE1, 64);
-        CRT_CUDA(cudaMemsetAsync(pix, 0, (size_t)npix * 16, st));
-        CRT_CUDA(cudaMemsetAsync(taken, 0, (size_t)npix * 4, st));
-        CRT_CUDA(cudaMemsetAsync(done, 0, npix, st));
-
-        const bool adaptive = p->noise_threshold > 0 && p->min_samples < p->max_samples;
-        const uint32_t nl = std::max<uint32_t>(n_lights, 1);
-        uint32_t n_active = npix;
-        const uint32_t* active = nullptr;
-        int sample_base = 0;
-        const int total = std::max(0, p->max_samples);
-        const SceneView sv = scene_view(s);
-        while (sample_base < total && n_active > 0) {
-            int k;
-            if (!adaptive) k = total - sample_base;
-            else if (sample_base == 0) k = std::max(1, std::min(p->min_samples, total));
-            else k = 1;
-            k = (int)std::min<uint64_t>((uint64_t)k, std::max<uint64_t>(1, WAVE_CAP / n_active));
-            const uint32_t P = n_active * (uint32_t)k;
-            // wave buffers
-            const size_t per = 32 + 4 + 16 + 16 + 16 + 16 + (size_t)nl * (16 + 1) + 8 + (size_t)nl * (32 + 8);
-            char* wb = (char*)ctx_scratch(ctx, SCR_WAVE2, (size_t)P * per + 4096);
-            WaveBufs w;
-            size_t off = 0;
-            auto take = [&](size_t bytes) {
-                off = (off + 255) & ~size_t(255);
-                char* q = wb + off;
-                off += bytes;
-                return q;
-            };
-            w.n_active = n_active;
-            w.active = active;
-            w.sample_base = (uint32_t)sample_base;
-            w.k = (uint32_t)k;
-            w.ray = (float4*)take((size_t)P * 32);
-            w.skip = (uint32_t*)take((size_t)P * 4);
-            w.hit = (float4*)take((size_t)P * 16);
-            w.weight = (float4*)take((size_t)P * 16);
-            w.wacc = (float4*)take((size_t)P * 16);
-            w.rad = (float4*)take((size_t)P * 16);
-            w.contrib = (float4*)take((size_t)P * nl * 16);
-            w.occ = (uint8_t*)take((size_t)P * nl);
-            w.q_cur = (uint32_t*)take((size_t)P * 4);
-            w.q_next = (uint32_t*)take((size_t)P * 4);
-            w.sray = (float4*)take((size_t)P * nl * 32);
-            w.sidx = (uint32_t*)take((size_t)P * nl * 4);
-            w.sskip = (uint32_t*)take((size_t)P * nl * 4);
-            w.counts = acount + 4;
-            CRT_CUDA(cudaMemsetAsync(w.counts, 0, 3 * sizeof(uint32_t), st));
-
-            launch_trace<false>(s, PrimaryJob{cb, c, w}, P);
-            for (int b = 0; b < p->num_bounces; ++b) {
-                k_shade<<<grid_for(ctx, P), 256, 0, st>>>(sv, c, w, L, b, P);
-                check_launch(ctx, "k_shade");
-                if (n_lights) {
-                    launch_trace<true>(s, ShadowJob{w}, P * n_lights, w.counts + 2);
-                }
-                k_accum<<<grid_for(ctx, P), 256, 0, st>>>(c, w, n_lights, b, P);
-                check_launch(ctx, "k_accum");
-                if (b < p->num_bounces - 1) {
-                    launch_trace<false>(s, BounceJob{w}, P, w.counts + 1);
-                    k_queue_rotate<<<1, 1, 0, st>>>(w.counts);
-                    check_launch(ctx, "k_queue_rotate");
-                    std::swap(w.q_cur, w.q_next);
-                }
-            }
-            k_update<<<grid_for(ctx, n_active), 256, 0, st>>>(c, w, pix, taken, done);
-            check_launch(ctx, "k_update");
-            sample_base += k;
-            if (adaptive && sample_base < total) {
-                uint32_t* out = active == act_a ? act_b : act_a;
-                CRT_CUDA(cudaMemsetAsync(acount, 0, sizeof(uint32_t), st));
-                k_compact<<<grid_for(ctx, n_active), 256, 0, st>>>(active, n_active, done, out, acount);
-                check_launch(ctx, "k_compact");
-                uint32_t h = 0;
-                CRT_CUDA(cudaMemcpyAsync(&h, acount, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
-                CRT_CUDA(cudaStreamSynchronize(st));
-                n_active = h;
-                active = out;
-            }
-        }
-        float4* d_rad = (float4*)out_device(ctx, radiance, (size_t)npix * 16, SCR_OUT0);
-        uchar4* d_rgba = (uchar4*)out_device(ctx, rgba8, (size_t)npix * 4, SCR_OUT1);
-        k_finalize<<<grid_for(ctx, npix), 256, 0, st>>>(npix, pix, d_rad, d_rgba);
-        check_launch(ctx, "k_finalize");
-        out_finish(ctx, radiance, d_rad, (size_t)npix * 16);
-        out_finish(ctx, rgba8, d_rgba, (size_t)npix * 4);
-        if ((radiance && (void*)d_rad != (void*)radiance) || (rgba8 && (void*)d_rgba != (void*)rgba8))
-            check_device_error(ctx, "crt_render");
-    });
+    crt_request q;
+    std::memset(&q, 0, sizeof(q));
+    q.kind = CRT_REQUEST_RENDER;
+    q.scene = s;
+    q.camera = cam;
+    q.lights = lights;
+    q.n_lights = n_lights;
+    q.params = p;
+    q.rgba8 = rgba8;
+    q.radiance = radiance;
+    return crt_guard(s->ctx, [&] { run_batch(s->ctx, &q, 1, nullptr); });
 }

@@ -172,11 +172,11 @@ __global__ void k_srp_reduce(const double* __restrict__ partial, uint32_t grabs_
 
 }  // namespace
 
-extern "C" int crt_srp(crt_scene* s, const crt_srp_desc* desc, const double* quats, size_t n_att, double* force,
-                       double* torque, double* facet_power) {
-    if (!s || !desc) return CRT_ERR_INVALID;
-    crt_context* ctx = s->ctx;
-    return crt_guard(ctx, [&] {
+// Runs on `ctx` (stream, scratch, error word), which may differ from the scene's own context on the
+// same device (serving lanes).  Throws CrtError.
+void srp_run(crt_context* ctx, crt_scene* s, const crt_srp_desc* desc, const double* quats, size_t n_att,
+             double* force, double* torque, double* facet_power) {
+    [&] {
         CRT_CHECK(n_att == 0 || (quats && force && torque), CRT_ERR_INVALID, "null buffer");
         CRT_CHECK(desc->grid > 0 && desc->grid <= 65536, CRT_ERR_INVALID, "grid must be in [1, 65536]");
         CRT_CHECK(desc->c > 0 && std::isfinite(desc->flux), CRT_ERR_INVALID, "bad flux or speed of light");
@@ -275,7 +275,13 @@ extern "C" int crt_srp(crt_scene* s, const crt_srp_desc* desc, const double* qua
         out_finish(ctx, torque, d_torque, n_att * 24);
         if (facet_power) out_finish(ctx, facet_power, d_facet, n_att * s->n_tris * 8);
         check_device_error(ctx, "crt_srp");
-    });
+    }();
+}
+
+extern "C" int crt_srp(crt_scene* s, const crt_srp_desc* desc, const double* quats, size_t n_att, double* force,
+                       double* torque, double* facet_power) {
+    if (!s || !desc) return CRT_ERR_INVALID;
+    return crt_guard(s->ctx, [&] { srp_run(s->ctx, s, desc, quats, n_att, force, torque, facet_power); });
 }
 
 // ---------------------------------------------------------------- allocation-free variant

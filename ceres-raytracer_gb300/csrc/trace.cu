@@ -14,10 +14,10 @@
 namespace {
 
 // ---------------------------------------------------------------- jobs
-struct RayClosestJob {
+struct RayClosestJob : JobBase {
     const float4* rays;   // crt_ray as 2 x float4
     crt_hit* hits;
-    __device__ bool ray(uint32_t i, TRay& r) const {
+    __device__ bool ray(uint32_t i, TRay& r, Item&) const {
         const float4 a = __ldg(rays + 2ull * i), b = __ldg(rays + 2ull * i + 1);
         r.o = f3(a.x, a.y, a.z);
         r.tmin = a.w;
@@ -25,7 +25,7 @@ struct RayClosestJob {
         r.tmax = b.w;
         return true;
     }
-    __device__ void write(const SceneView& sv, uint32_t i, const TRay&, const THit& h) const {
+    __device__ void write(const SceneView& sv, uint32_t i, const TRay&, const THit& h, const Item&) const {
         crt_hit o;
         if (h.slot != CRT_MISS) {
             o.t = h.t; o.u = h.u; o.v = h.v;
@@ -38,10 +38,10 @@ struct RayClosestJob {
     }
 };
 
-struct RayAnyJob {
+struct RayAnyJob : JobBase {
     const float4* rays;
     uint8_t* occluded;
-    __device__ bool ray(uint32_t i, TRay& r) const {
+    __device__ bool ray(uint32_t i, TRay& r, Item&) const {
         const float4 a = __ldg(rays + 2ull * i), b = __ldg(rays + 2ull * i + 1);
         r.o = f3(a.x, a.y, a.z);
         r.tmin = a.w;
@@ -49,7 +49,7 @@ struct RayAnyJob {
         r.tmax = b.w;
         return true;
     }
-    __device__ void write(const SceneView&, uint32_t i, const TRay&, const THit& h) const {
+    __device__ void write(const SceneView&, uint32_t i, const TRay&, const THit& h, const Item&) const {
         occluded[i] = h.slot != CRT_MISS ? 1 : 0;
     }
 };
@@ -62,18 +62,18 @@ __device__ __forceinline__ bool tile_pixel(uint32_t i, uint32_t W, uint32_t H, u
     return px < W && py < H;
 }
 
-struct PassJob {
+struct PassJob : JobBase {
     CamBasis cam;
     double* xyz;
     uint32_t* ids;
     double* normals;
-    __device__ bool ray(uint32_t i, TRay& r) const {
+    __device__ bool ray(uint32_t i, TRay& r, Item&) const {
         uint32_t px, py;
         if (!tile_pixel(i, cam.width, cam.height, px, py)) return false;
         r = camera_ray(cam, (float)px, (float)py);
         return true;
     }
-    __device__ void write(const SceneView& sv, uint32_t i, const TRay&, const THit& h) const {
+    __device__ void write(const SceneView& sv, uint32_t i, const TRay&, const THit& h, const Item&) const {
         uint32_t px, py;
         tile_pixel(i, cam.width, cam.height, px, py);
         const size_t pix = (size_t)py * cam.width + px;
@@ -132,13 +132,13 @@ struct PassJob {
     }
 };
 
-struct LidarBatchJob {
+struct LidarBatchJob : JobBase {
     const double* pos;
     const double* rot;
     float zsign;
     double* range;
     uint32_t* prim;
-    __device__ bool ray(uint32_t i, TRay& r) const {
+    __device__ bool ray(uint32_t i, TRay& r, Item&) const {
         // SimpleLidar::batch_cast_rays: direction R^T (0, 0, +-1) = +-(R[2][0], R[2][1], R[2][2])
         r.o = f3((float)pos[3ull * i], (float)pos[3ull * i + 1], (float)pos[3ull * i + 2]);
         r.d = f3((float)(zsign * rot[9ull * i + 6]), (float)(zsign * rot[9ull * i + 7]), (float)(zsign * rot[9ull * i + 8]));
@@ -146,7 +146,7 @@ struct LidarBatchJob {
         r.tmax = 3.402823466e38f;
         return true;
     }
-    __device__ void write(const SceneView& sv, uint32_t i, const TRay&, const THit& h) const {
+    __device__ void write(const SceneView& sv, uint32_t i, const TRay&, const THit& h, const Item&) const {
         // do_lidar.hpp:49-59: |hit - position|, 0 on a miss; evaluated along the FP64 pose ray
         double rng = 0.0;
         if (h.slot != CRT_MISS) {
@@ -160,7 +160,7 @@ struct LidarBatchJob {
     }
 };
 
-struct LidarGridJob {
+struct LidarGridJob : JobBase {
     double o[3];
     double rt[9];         // R^T row-major (world = rt * sensor direction)
     double zsign;
@@ -174,7 +174,7 @@ struct LidarGridJob {
         const double inv = 1.0 / sqrt(s0 * s0 + s1 * s1 + s2 * s2);
         for (int k = 0; k < 3; ++k) d[k] = (rt[3 * k] * s0 + rt[3 * k + 1] * s1 + rt[3 * k + 2] * s2) * inv;
     }
-    __device__ bool ray(uint32_t i, TRay& r) const {
+    __device__ bool ray(uint32_t i, TRay& r, Item&) const {
         uint32_t px, py;
         if (!tile_pixel(i, nx, ny, px, py)) return false;
         double d[3];
@@ -185,7 +185,7 @@ struct LidarGridJob {
         r.tmax = 3.402823466e38f;
         return true;
     }
-    __device__ void write(const SceneView& sv, uint32_t i, const TRay&, const THit& h) const {
+    __device__ void write(const SceneView& sv, uint32_t i, const TRay&, const THit& h, const Item&) const {
         uint32_t px, py;
         tile_pixel(i, nx, ny, px, py);
         const size_t k = (size_t)py * nx + px;
@@ -230,7 +230,7 @@ int crt_trace_closest(crt_scene* s, const crt_ray* rays, size_t n, crt_hit* hits
         CRT_CUDA(cudaSetDevice(ctx->device));
         const float4* d_rays = (const float4*)to_device(ctx, rays, n * sizeof(crt_ray), SCR_IN0);
         crt_hit* d_hits = (crt_hit*)out_device(ctx, hits, n * sizeof(crt_hit), SCR_OUT0);
-        launch_trace<false>(s, RayClosestJob{d_rays, d_hits}, (uint32_t)n);
+        launch_trace<false>(s, RayClosestJob{{}, d_rays, d_hits}, (uint32_t)n);
         out_finish(ctx, hits, d_hits, n * sizeof(crt_hit));
         finish(ctx, d_hits != (void*)hits, "crt_trace_closest");
     });
@@ -246,7 +246,7 @@ int crt_trace_any(crt_scene* s, const crt_ray* rays, size_t n, uint8_t* occluded
         CRT_CUDA(cudaSetDevice(ctx->device));
         const float4* d_rays = (const float4*)to_device(ctx, rays, n * sizeof(crt_ray), SCR_IN0);
         uint8_t* d_occ = (uint8_t*)out_device(ctx, occluded, n, SCR_OUT0);
-        launch_trace<true>(s, RayAnyJob{d_rays, d_occ}, (uint32_t)n);
+        launch_trace<true>(s, RayAnyJob{{}, d_rays, d_occ}, (uint32_t)n);
         out_finish(ctx, occluded, d_occ, n);
         finish(ctx, d_occ != occluded, "crt_trace_any");
     });
@@ -266,7 +266,7 @@ int crt_passes(crt_scene* s, const crt_camera_desc* cam, double* xyz, uint32_t* 
         double* d_xyz = (double*)out_device(ctx, xyz, np * 24, SCR_OUT0);
         uint32_t* d_ids = (uint32_t*)out_device(ctx, ids, np * 4, SCR_OUT1);
         double* d_nrm = (double*)out_device(ctx, normals, np * 24, SCR_OUT2);
-        launch_trace<false>(s, PassJob{cb, d_xyz, d_ids, d_nrm}, tiles_items(cb.width, cb.height));
+        launch_trace<false>(s, PassJob{{}, cb, d_xyz, d_ids, d_nrm}, tiles_items(cb.width, cb.height));
         out_finish(ctx, xyz, d_xyz, np * 24);
         out_finish(ctx, ids, d_ids, np * 4);
         out_finish(ctx, normals, d_nrm, np * 24);
@@ -287,7 +287,7 @@ int crt_lidar_batch(crt_scene* s, const double* positions, const double* rotatio
         const double* d_rot = (const double*)to_device(ctx, rotations, n * 72, SCR_IN1);
         double* d_rng = (double*)out_device(ctx, range, n * 8, SCR_OUT0);
         uint32_t* d_prim = (uint32_t*)out_device(ctx, prim, n * 4, SCR_OUT1);
-        launch_trace<false>(s, LidarBatchJob{d_pos, d_rot, z_positive ? 1.0f : -1.0f, d_rng, d_prim}, (uint32_t)n);
+        launch_trace<false>(s, LidarBatchJob{{}, d_pos, d_rot, z_positive ? 1.0f : -1.0f, d_rng, d_prim}, (uint32_t)n);
         out_finish(ctx, range, d_rng, n * 8);
         out_finish(ctx, prim, d_prim, n * 4);
         finish(ctx, d_rng != range || (prim && d_prim != prim), "crt_lidar_batch");

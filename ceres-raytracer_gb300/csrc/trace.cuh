@@ -63,11 +63,20 @@ __device__ __forceinline__ SurfacePoint surface_point(const SceneView& sv, const
     return sp;
 }
 
+// Jobs: ray(i, r, item) builds the ray of work item i (false: nothing to trace), view(sv, item)
+// names the scene to traverse (requests of one launch may use different resident scenes), and
+// write(sv, i, r, hit, item) stores the result.  JobBase supplies the single-scene defaults.
+struct JobBase {
+    struct Item {};
+    __device__ __forceinline__ const SceneView& view(const SceneView& sv, const Item&) const { return sv; }
+};
+
+// Persistent ray-queue kernel: each warp takes `chunk` x 32 consecutive items per atomic grab.
 template <bool ANY, bool COUNT, class Job>
-__global__ void __launch_bounds__(CRT_TRACE_BLOCK) k_trace(SceneView sv, Job job, uint32_t n_items,
+__global__ void __launch_bounds__(CRT_TRACE_BLOCK, 8) k_trace(SceneView sv, Job job, uint32_t n_items,
                                                             const uint32_t* __restrict__ n_dev,
                                                             uint32_t* __restrict__ queue, uint32_t* __restrict__ err,
-                                                            unsigned long long* __restrict__ counters) {
+                                                            unsigned long long* __restrict__ counters, uint32_t chunk) {
     extern __shared__ uint2 sstack[];
     if (n_dev) n_items = *n_dev;   // item count produced by an earlier kernel on the stream
     const int lane = threadIdx.x & 31;
@@ -75,15 +84,18 @@ __global__ void __launch_bounds__(CRT_TRACE_BLOCK) k_trace(SceneView sv, Job job
     uint32_t nrays = 0;
     while (true) {
         uint32_t base = 0;
-        if (lane == 0) base = atomicAdd(queue, 32u);
+        if (lane == 0) base = atomicAdd(queue, 32u * chunk);
         base = __shfl_sync(0xffffffffu, base, 0);
         if (base >= n_items) break;
-        const uint32_t i = base + lane;
-        TRay r;
-        if (i < n_items && job.ray(i, r)) {
-            const THit h = traverse<ANY, COUNT>(sv, r, sstack + threadIdx.x, CRT_TRACE_BLOCK, st, err);
-            job.write(sv, i, r, h);
-            if (COUNT) ++nrays;
+        for (uint32_t c = 0; c < chunk; ++c) {
+            const uint32_t i = base + 32u * c + lane;
+            TRay r;
+            typename Job::Item it;
+            if (i < n_items && job.ray(i, r, it)) {
+                const THit h = traverse<ANY, COUNT>(job.view(sv, it), r, sstack + threadIdx.x, CRT_TRACE_BLOCK, st, err);
+                job.write(sv, i, r, h, it);
+                if (COUNT) ++nrays;
+            }
         }
     }
     if (COUNT) {
@@ -104,9 +116,8 @@ __global__ void __launch_bounds__(CRT_TRACE_BLOCK) k_trace(SceneView sv, Job job
 // Launches the persistent trace kernel over n_items work items (or over *n_dev items when n_dev is
 // given: n_items is then the upper bound used to size the grid).
 template <bool ANY, class Job>
-void launch_trace(crt_scene* s, const Job& job, uint32_t n_items, const uint32_t* n_dev = nullptr,
-                  uint32_t* queue = nullptr) {
-    crt_context* ctx = s->ctx;
+void launch_trace(crt_context* ctx, const SceneView& sv, const Job& job, uint32_t n_items,
+                  const uint32_t* n_dev = nullptr, uint32_t* queue = nullptr) {
     if (!queue) queue = (uint32_t*)ctx_scratch(ctx, SCR_QUEUE, 256);
     CRT_CUDA(cudaMemsetAsync(queue, 0, sizeof(uint32_t), ctx->stream));
     const size_t smem = (size_t)CRT_STACK_SMEM * CRT_TRACE_BLOCK * sizeof(uint2);
@@ -114,12 +125,18 @@ void launch_trace(crt_scene* s, const Job& job, uint32_t n_items, const uint32_t
     int grid = occupancy_grid(ctx, kfn, CRT_TRACE_BLOCK, smem);
     const uint32_t need = (n_items + CRT_TRACE_BLOCK - 1) / CRT_TRACE_BLOCK;
     if ((uint32_t)grid > need) grid = (int)std::max<uint32_t>(need, 1u);
-    const SceneView sv = scene_view(s);
+    const uint32_t chunk = ctx->queue_chunk ? ctx->queue_chunk : 1u;
     if (ctx->counting)
         k_trace<ANY, true, Job><<<grid, CRT_TRACE_BLOCK, smem, ctx->stream>>>(sv, job, n_items, n_dev, queue,
-                                                                             ctx->d_error, ctx->d_counters);
+                                                                             ctx->d_error, ctx->d_counters, chunk);
     else
         k_trace<ANY, false, Job><<<grid, CRT_TRACE_BLOCK, smem, ctx->stream>>>(sv, job, n_items, n_dev, queue,
-                                                                              ctx->d_error, ctx->d_counters);
+                                                                              ctx->d_error, ctx->d_counters, chunk);
     check_launch(ctx, "k_trace");
+}
+
+template <bool ANY, class Job>
+void launch_trace(crt_scene* s, const Job& job, uint32_t n_items, const uint32_t* n_dev = nullptr,
+                  uint32_t* queue = nullptr) {
+    launch_trace<ANY>(s->ctx, scene_view(s), job, n_items, n_dev, queue);
 }

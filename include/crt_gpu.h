@@ -130,6 +130,37 @@ typedef struct {
     uint32_t num_bounces;         /* specular continuation segments after the primary hit */
 } crt_srp_desc;
 
+/* One request of a batch (crt_batch).  kind selects which fields are used. */
+enum { CRT_REQUEST_RENDER = 0, CRT_REQUEST_LIDAR = 1 };
+typedef struct {
+    int kind;
+    crt_scene* scene;                     /* resident scene (requests of a batch may use different ones) */
+    /* CRT_REQUEST_RENDER: as crt_render */
+    const crt_camera_desc* camera;
+    const crt_light_desc* lights;
+    uint32_t n_lights;
+    const crt_render_params* params;
+    uint8_t* rgba8;                       /* [H][W][4] or NULL */
+    float* radiance;                      /* [H][W][4] or NULL */
+    /* CRT_REQUEST_LIDAR: as crt_lidar_grid */
+    const crt_lidar_grid_desc* lidar;
+    double* range;                        /* [ny][nx] */
+    uint32_t* prim;                       /* [ny][nx] or NULL */
+} crt_request;
+
+typedef struct {
+    size_t waves;                         /* wavefront waves executed */
+    uint64_t render_paths;                /* camera paths (pixels x samples) */
+    uint64_t lidar_beams;
+} crt_batch_stats;
+
+/* Tuning knobs of the persistent kernels and the batched wavefront (chosen by the autotuner). */
+typedef struct {
+    uint32_t queue_chunk;                 /* 32-ray groups a warp takes per atomic grab (1..8) */
+    uint32_t wave_paths;                  /* camera paths per wave (>= 65536) */
+    int use_graphs;                       /* replay batched waves as CUDA graphs */
+} crt_tuning;
+
 typedef struct {
     size_t n_tris;
     size_t n_nodes;           /* 8-wide compressed nodes */
@@ -158,6 +189,8 @@ int crt_context_synchronize(crt_context* ctx);
 int crt_context_set_counting(crt_context* ctx, int enabled);
 int crt_context_get_counters(crt_context* ctx, crt_counters* out);
 int crt_context_reset_counters(crt_context* ctx);
+int crt_context_set_tuning(crt_context* ctx, const crt_tuning* tuning);
+int crt_context_get_tuning(const crt_context* ctx, crt_tuning* out);
 const char* crt_context_last_error(const crt_context* ctx);
 const char* crt_status_string(int status);
 int crt_abi_version(void);
@@ -204,6 +237,13 @@ int crt_lidar_grid(crt_scene* scene, const crt_lidar_grid_desc* desc, double* ra
  * rgba8 is [H][W][4] (clamp(v*256, 0, 255)), radiance (optional) the float RGBA before quantisation. */
 int crt_render(crt_scene* scene, const crt_camera_desc* camera, const crt_light_desc* lights, uint32_t n_lights,
                const crt_render_params* params, uint8_t* rgba8, float* radiance);
+/* Many render and LiDAR requests in one set of persistent launches: do_render / do_batch_lidar
+ * called once per request in the reference become one wavefront over every request's rays (one
+ * shared ray queue per stage).  Each request's outputs are identical to its own crt_render /
+ * crt_lidar_grid call: random streams are keyed by (seed, request) and pixels consume their samples
+ * in order.  Requests with adaptive sampling (noise_threshold > 0, min < max) advance one sample
+ * per wave after their first min_samples. */
+int crt_batch(crt_context* ctx, const crt_request* requests, size_t n, crt_batch_stats* stats);
 /* Solar radiation pressure for n_att attitudes (unit quaternions w,x,y,z rotating body vectors into the
  * inertial frame).  force and torque are n_att*3 in the body frame (N, N m); facet_power (optional)
  * is n_att * n_tris absorbed power per triangle (W).  No reference counterpart (README.md:9). */
@@ -221,6 +261,53 @@ int crt_srp(crt_scene* scene, const crt_srp_desc* desc, const double* quaternion
  * race.  Every GPU that loads the library keeps the 16 MiB until the process exits. */
 int crt_srp_static(crt_scene* scene, const crt_srp_desc* desc, const double* quaternions, size_t n_att,
                    double* force, double* torque);
+
+/* ---------------------------------------------------------------- serving
+ * A request loop over resident scenes (no counterpart in the reference, which renders one camera per
+ * call): requests are submitted from any thread, queued, admitted FIFO into batches while their
+ * estimated device-memory footprint fits a lane's budget, and run as crt_batch on one of `lanes`
+ * concurrent lanes (each with its own stream and scratch), so batches formed while others run
+ * overlap on the device.  Results equal the same requests run alone (crt_batch guarantee). */
+typedef struct crt_server crt_server;
+enum { CRT_REQUEST_SRP = 2 };
+typedef struct {
+    uint32_t lanes;                       /* concurrent batches, >= 1 */
+    size_t lane_budget_bytes;             /* admission budget per batch (device scratch) */
+    uint32_t max_batch;                   /* requests per batch */
+} crt_server_config;
+typedef struct {
+    crt_request base;                     /* kind RENDER or LIDAR: as for crt_batch; kind SRP: below */
+    const crt_srp_desc* srp;
+    const double* quaternions;            /* n_att * 4, host memory */
+    size_t n_att;
+    double* force;                        /* n_att * 3 */
+    double* torque;                       /* n_att * 3 */
+} crt_server_request;
+typedef struct {
+    int status;                           /* CRT_OK or the failure of the batch that ran it */
+    double submit_s, start_s, end_s;      /* steady-clock seconds */
+    uint32_t batch_size;                  /* requests in the batch that ran it */
+} crt_server_result;
+typedef struct {
+    uint64_t submitted, completed, batches, failed;
+    uint64_t rays;                        /* rays traced by completed batches */
+    double busy_s;                        /* summed lane time */
+} crt_server_stats;
+
+/* Lanes own their contexts.  Requests name scenes built on any context of the same device (the
+ * lanes only read a scene's arrays), so the caller can keep using those scenes directly; scenes
+ * must outlive every request that names them. */
+int crt_server_create(int device, const crt_server_config* config, crt_server** out);
+/* Stops the lanes after the queued requests finish. */
+int crt_server_destroy(crt_server* server);
+/* Copies the request's descriptors; outputs must stay valid until the request completes.  Rejects
+ * malformed requests at once (CRT_ERR_INVALID); crt_server_last_error then holds the reason. */
+int crt_server_submit(crt_server* server, const crt_server_request* request, uint64_t* ticket);
+/* Message of the calling thread's last failed crt_server_submit. */
+const char* crt_server_last_error(void);
+/* Waits up to timeout_s (negative: forever) for a ticket; CRT_ERR_TIMEOUT when it has not finished. */
+int crt_server_wait(crt_server* server, uint64_t ticket, double timeout_s, crt_server_result* out);
+int crt_server_get_stats(crt_server* server, crt_server_stats* out);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,128 @@
+"""Serving loop (crt_server_*): continuous batching over resident scenes.
+
+* every result equals the same request run alone (bit for bit), whatever batch it landed in;
+* admission by memory budget: with a budget smaller than any request each request runs alone;
+* malformed requests are refused at submission and the server keeps serving;
+* waits are bounded (CRT_ERR_TIMEOUT), no GPU-side waiting is involved.
+"""
+import threading
+import time
+
+import numpy as np
+import pytest
+
+from crt_gb300 import lib, scenes
+from helpers import camera_from, entities_from, lights_from, load_golden
+
+pytestmark = pytest.mark.gpu
+
+
+def request_mix(d, cornell, ast, n=14, seed=3):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    cam = camera_from(d, "rcam")
+    reqs = []
+    for k in range(n):
+        kind = ["render", "lidar", "srp"][k % 3]
+        if kind == "render":
+            res = int(rng.choice([8, 16, 32]))
+            reqs.append(dict(kind="render", scene=cornell, camera=dict(cam, resolution=[res, res]),
+                             lights=lights_from(d["lights"]), min_samples=2, max_samples=2, noise_threshold=0.0,
+                             num_bounces=2, seed=k, request=k, radiance=True))
+        elif kind == "lidar":
+            pos = 3000.0 * scenes.unit_vector(70 + k)
+            reqs.append(dict(kind="lidar", scene=ast, position=pos, rotation=scenes.look_at(pos, (0, 0, 0)),
+                             nx=int(rng.integers(8, 40)), ny=int(rng.integers(8, 40)), half_x=0.1, half_y=0.08))
+        else:
+            reqs.append(dict(kind="srp", scene=ast, sun_dir=scenes.unit_vector(90 + k),
+                             quaternions=scenes.random_quaternions(2, seed=k), grid=96, num_bounces=1))
+    return reqs
+
+
+def alone(q):
+    sc = q["scene"]
+    if q["kind"] == "render":
+        return sc.render(q["camera"], q["lights"], q["min_samples"], q["max_samples"], q["noise_threshold"],
+                         q["num_bounces"], seed=q["seed"], request=q["request"])
+    if q["kind"] == "lidar":
+        return sc.lidar_grid(q["position"], q["rotation"], q["nx"], q["ny"], q["half_x"], q["half_y"])
+    f, t, _ = sc.srp(q["sun_dir"], q["quaternions"], q["grid"], num_bounces=q["num_bounces"])
+    return f, t
+
+
+@pytest.fixture(scope="module")
+def server():
+    srv = lib.Server(0, lanes=2, lane_budget_bytes=64 << 20, max_batch=8)
+    d = load_golden("cornell")
+    cornell = srv.scene(entities_from(d))
+    ast = srv.scene([scenes.EntitySpec("a", scenes.asteroid(20_000, seed=6), (0.2, 0.2, 0.2), rho_s=0.2,
+                                       rho_d=0.3)])
+    yield srv, d, cornell, ast
+    srv.close()
+
+
+def test_results_same_alone_and_in_the_mix(server):
+    srv, d, cornell, ast = server
+    reqs = request_mix(d, cornell, ast)
+    expected = [alone(q) for q in reqs]
+    tickets = [None] * len(reqs)
+
+    def client(idx):
+        for i in idx:
+            tickets[i] = srv.submit(reqs[i])
+            time.sleep(0.001 * (i % 3))
+
+    threads = [threading.Thread(target=client, args=(range(k, len(reqs), 2),)) for k in range(2)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    sizes = []
+    for q, e, tk in zip(reqs, expected, tickets):
+        res, out = srv.wait(tk, timeout=60.0)
+        assert res["status"] == 0
+        assert res["end_s"] >= res["start_s"] >= res["submit_s"]
+        sizes.append(res["batch_size"])
+        for a, b in zip(out, e):
+            if b is not None:
+                np.testing.assert_array_equal(a, b)
+    st = srv.stats()
+    assert st["completed"] >= len(reqs) and st["failed"] == 0 and st["rays"] > 0
+
+
+def test_admission_budget_runs_large_requests_alone():
+    srv = lib.Server(0, lanes=1, lane_budget_bytes=1, max_batch=64)
+    try:
+        d = load_golden("cornell")
+        cornell = srv.scene(entities_from(d))
+        cam = camera_from(d, "rcam")
+        reqs = [dict(kind="render", scene=cornell, camera=dict(cam, resolution=[16, 16]),
+                     lights=lights_from(d["lights"]), min_samples=1, max_samples=1, noise_threshold=0.0,
+                     num_bounces=1, seed=1, request=k) for k in range(5)]
+        tickets = [srv.submit(q) for q in reqs]
+        for q, tk in zip(reqs, tickets):
+            res, out = srv.wait(tk, timeout=60.0)
+            assert res["status"] == 0 and res["batch_size"] == 1
+            np.testing.assert_array_equal(out[0], alone(q)[0])
+        assert srv.stats()["batches"] == 5
+    finally:
+        srv.close()
+
+
+def test_malformed_request_refused_and_service_continues(server):
+    srv, d, cornell, ast = server
+    bad = dict(kind="lidar", scene=ast, position=[0, 0, 3000.0], rotation=np.eye(3), nx=0, ny=4, half_x=0.1,
+               half_y=0.1)
+    with pytest.raises(lib.CrtError):
+        srv.submit(bad)
+    good = dict(bad, nx=4)
+    res, out = srv.wait(srv.submit(good), timeout=60.0)
+    assert res["status"] == 0
+    np.testing.assert_array_equal(out[0], alone(good)[0])
+
+
+def test_wait_is_bounded(server):
+    srv, *_ = server
+    t = time.perf_counter()
+    with pytest.raises(lib.CrtError) as e:
+        srv.wait(10 ** 9, timeout=0.05)
+    assert e.value.status == -4 and time.perf_counter() - t < 5.0
