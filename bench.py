@@ -49,6 +49,14 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-served", action="store_true")
+    ap.add_argument("--served-seconds", type=float, default=10.0,
+                    help="length of the Poisson request stream (the configuration states 60 s)")
+    ap.add_argument("--served-rate", type=float, default=200.0)
+    ap.add_argument("--served-lanes", type=int, default=2)
+    ap.add_argument("--served-budget-mib", type=int, default=4096)
+    ap.add_argument("--no-srp", action="store_true")
+    ap.add_argument("--srp-attitudes", type=int, default=256)
     ap.add_argument("--probe", type=int, default=0,
                     help="profiling aid: only launch the primary-ray closest-hit kernel this many times")
     return ap.parse_args()
@@ -91,7 +99,7 @@ class ClockSampler:
     """nvidia-smi clock / throttle sampling during the timed region."""
     FIELDS = "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown," \
              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown," \
-             "clocks_event_reasons.sw_power_cap"
+             "clocks_event_reasons.sw_power_cap,utilization.gpu"
 
     def __init__(self, device):
         self.device = device
@@ -129,8 +137,10 @@ class ClockSampler:
         mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower().startswith("active")})
+        util = [float(r[9]) for r in rows if len(r) > 9 and r[9].replace(".", "").isdigit()]
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(rows)}
+                "reasons": reasons, "samples": len(rows),
+                "gpu_busy_pct": round(statistics.mean(util), 1) if util else None}
 
 
 def measured_peak():
@@ -359,6 +369,14 @@ def gpu_arm(args):
     if not args.no_batched and rank == 0:
         batched = batched_measure(ctx, sc, stream)
 
+    srp = None
+    if not args.no_srp and rank == 0:
+        srp = srp_measure(args, ctx, stream)
+
+    served = None
+    if not args.no_served and rank == 0:
+        served = served_measure(args, local)
+
     # ---- end to end through the public crt API (host numpy outputs)
     e2e = None
     if not args.no_e2e and rank == 0:
@@ -379,7 +397,8 @@ def gpu_arm(args):
                                "render_p99": round(percentile(lat_render, 99), 3),
                                "lidar_p50": round(percentile(lat_lidar, 50), 3),
                                "lidar_p99": round(percentile(lat_lidar, 99), 3)},
-                "roofline": roof, "gpu_launches": int(launches), "clocks": clk, "e2e": e2e, "batched": batched}
+                "roofline": roof, "gpu_launches": int(launches), "clocks": clk, "e2e": e2e, "batched": batched,
+                "served": served, "srp": srp}
         if world == 1 and not args.no_cpu:
             mr, det = cpu_measure(ents, cfg, args.cpu_seconds)
             line["cpu_baseline"] = {"value": round(mr, 3), "unit": UNIT, "cores": det["cores"], "kind": "port",
@@ -426,7 +445,12 @@ def batched_measure(ctx, sc, stream, reps=1):
             if events is not None:
                 events[k][1].record(stream)
 
+    from crt_gb300 import autotune
     with torch.cuda.stream(stream):
+        # wave size and queue chunk picked by the autotuner on this request set (both paths use them)
+        knobs, rep = autotune.tune(ctx, lambda: ctx.batch(breqs, outputs=outs), "batched-64", sc.stats()["n_tris"],
+                                   grid={"queue_chunk": (1, 2), "wave_paths": (1 << 22, 1 << 23, 1 << 24),
+                                         "use_graphs": (True,)}, use_cache=False)
         # rays actually traced (counting build), identical for both paths
         ctx.reset_counters()
         ctx.set_counting(True)
@@ -463,7 +487,167 @@ def batched_measure(ctx, sc, stream, reps=1):
             "per_call_request_ms_p99": round(percentile(lat, 99), 3),
             "per_call_completion_ms_p50": round(percentile(list(done), 50), 2),
             "per_call_completion_ms_p99": round(percentile(list(done), 99), 2),
-            "batched_completion_ms": round(bt_ms, 2)}
+            "batched_completion_ms": round(bt_ms, 2),
+            "tuning": knobs, "tuning_trials_ms": [[t[0]["queue_chunk"], t[0]["wave_paths"], round(t[1], 2)]
+                                                  for t in rep["trials"]]}
+
+
+def served_measure(args, device):
+    """Served stream: Poisson arrivals (200 req/s by default) over four resident asteroids (100k, 500k,
+    2M, 8M triangles), 50 % renders / 30 % LiDAR / 20 % SRP, host (numpy) outputs as a user gets them.
+
+    open loop   requests are submitted at their arrival times; latency = completion - arrival.  The
+                server (continuous batching over `lanes` concurrent lanes) and the per-call drop-in
+                (one blocking library call per request, in arrival order) serve the same stream.
+    closed loop every request is submitted at once: makespan throughput of both paths.
+    Rays come from a counting pass over the same requests (identical for both paths)."""
+    import threading
+    from crt_gb300 import lib, workloads
+    stream = workloads.served_stream(args.served_rate, args.served_seconds)
+    srv = lib.Server(device, lanes=args.served_lanes, lane_budget_bytes=args.served_budget_mib << 20, max_batch=256)
+    t0 = time.perf_counter()
+    ents = workloads.served_bodies()
+    t_gen = time.perf_counter() - t0
+    bodies = [srv.scene(e) for e in ents]
+    items = [(t, dict(q, scene=bodies[q["body"]])) for t, q in stream]
+
+    def call(q):
+        sc = q["scene"]
+        if q["kind"] == "render":
+            sc.render(q["camera"], q["lights"], q["min_samples"], q["max_samples"], 0.0, q["num_bounces"],
+                      seed=q["seed"], request=q["request"], want_radiance=False)
+        elif q["kind"] == "lidar":
+            sc.lidar_grid(q["position"], q["rotation"], q["nx"], q["ny"], q["half_x"], q["half_y"])
+        else:
+            sc.srp(q["sun_dir"], q["quaternions"], q["grid"], num_bounces=q["num_bounces"])
+
+    # rays of the whole stream (counting build, context of the scenes)
+    srv.ctx.reset_counters()
+    srv.ctx.set_counting(True)
+    for _, q in items:
+        call(q)
+    rays = int(srv.ctx.counters()["rays"])
+    srv.ctx.set_counting(False)
+    for _, q in items[:64]:                       # warm-up of both paths
+        call(q)
+    for tk in [srv.submit(q) for _, q in items[:64]]:
+        srv.wait(tk)
+
+    def served(open_loop):
+        tickets = [None] * len(items)
+        start = time.perf_counter() + 0.05
+
+        def submitter():
+            for i, (t, q) in enumerate(items):
+                if open_loop:
+                    d = start + t - time.perf_counter()
+                    if d > 0:
+                        time.sleep(d)
+                tickets[i] = srv.submit(q)
+
+        s0 = srv.stats()
+        th = threading.Thread(target=submitter)
+        th.start()
+        res = []
+        for i in range(len(items)):
+            while tickets[i] is None:
+                time.sleep(0.0002)
+            res.append(srv.wait(tickets[i])[0])
+        th.join()
+        s1 = srv.stats()
+        lat = [1e3 * (r["end_s"] - r["submit_s"]) for r in res]
+        span = max(r["end_s"] for r in res) - min(r["submit_s"] for r in res)
+        return lat, span, (s1["batches"] - s0["batches"]), res
+
+    def per_call(open_loop):
+        lat = []
+        start = time.perf_counter() + 0.05
+        t_first = None
+        for t, q in items:
+            arrive = start + t if open_loop else None
+            if open_loop:
+                d = arrive - time.perf_counter()
+                if d > 0:
+                    time.sleep(d)
+            a = time.perf_counter()
+            t_first = t_first or a
+            call(q)
+            e = time.perf_counter()
+            lat.append(1e3 * (e - (arrive if open_loop else t_first)))
+        return lat, time.perf_counter() - t_first
+
+    small = [q.get("size", 0) <= 1024 for _, q in items]
+
+    def summary(lat, span):
+        ls = [x for x, f in zip(lat, small) if f]
+        return {"mrays_s": round(rays / span / 1e6, 1), "span_s": round(span, 3),
+                "p50_ms": round(percentile(lat, 50), 2), "p99_ms": round(percentile(lat, 99), 2),
+                "p50_ms_le1024": round(percentile(ls, 50), 2), "p99_ms_le1024": round(percentile(ls, 99), 2)}
+
+    def clocked(fn, *a):
+        cs = ClockSampler(device)
+        cs.start()
+        r = fn(*a)
+        return r, cs.stop()
+
+    (lat_s, span_s, nb_s, res_s), clk_s = clocked(served, True)
+    (lat_p, span_p), clk_p = clocked(per_call, True)
+    (clat_s, cspan_s, cnb_s, _), cclk_s = clocked(served, False)
+    (clat_p, cspan_p), cclk_p = clocked(per_call, False)
+    out = {"workload": "served stream: Poisson %.0f req/s for %.0f s (%d requests) over 4 resident asteroids "
+                       "(100k/500k/2M/8M triangles); 50%% renders 128^2..2048^2 x 1..16 spp (primary + sun "
+                       "shadow), 30%% LiDAR 64^2..1024^2, 20%% SRP 512^2..2048^2 x 2 bounces; host outputs"
+                       % (args.served_rate, args.served_seconds, len(items)),
+           "rays": rays, "offered_mrays_s": round(rays / args.served_seconds / 1e6, 1),
+           "lanes": args.served_lanes, "lane_budget_mib": args.served_budget_mib,
+           "open_loop": {"served": dict(summary(lat_s, span_s), waves=nb_s, clocks=clk_s),
+                         "per_call": dict(summary(lat_p, span_p), clocks=clk_p)},
+           "closed_loop": {"served": dict(summary(clat_s, cspan_s), waves=cnb_s, clocks=cclk_s),
+                           "per_call": dict(summary(clat_p, cspan_p), clocks=cclk_p),
+                           "speedup": round(cspan_p / cspan_s, 3)},
+           "body_generation_s": round(t_gen, 1)}
+    srv.close()
+    return out
+
+
+def srp_measure(args, ctx, stream):
+    """SRP batch: spacecraft (box bus, two panels, parabolic dish), N random attitudes, 4096^2 parallel
+    sun rays each, 2 specular bounces, FP64 force / torque and per-facet absorbed power on the device."""
+    import torch
+    from crt_gb300 import workloads
+    cfg = workloads.srp_config(n_att=args.srp_attitudes)
+    sc = ctx.scene(cfg["entities"])
+    n_tris = sc.stats()["n_tris"]
+    q = torch.from_numpy(np.ascontiguousarray(cfg["quaternions"])).cuda()
+    n = q.shape[0]
+    f = torch.empty((n, 3), dtype=torch.float64, device=q.device)
+    t = torch.empty((n, 3), dtype=torch.float64, device=q.device)
+    fp = torch.empty((n, n_tris), dtype=torch.float64, device=q.device)
+
+    def run(facet):
+        sc.srp_into(cfg["sun"], q, cfg["grid"], f, t, fp if facet else None, num_bounces=cfg["num_bounces"])
+
+    with torch.cuda.stream(stream):
+        ctx.reset_counters()
+        ctx.set_counting(True)
+        run(True)
+        cnt = ctx.counters()
+        ctx.set_counting(False)
+        run(True)
+        res = {}
+        for facet in (False, True):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            run(facet)
+            b.record(stream)
+            torch.cuda.synchronize()
+            res[facet] = a.elapsed_time(b) / 1e3
+    sc.close()
+    return {"workload": "SRP batch: spacecraft %d triangles, %d attitudes x %d^2 sun rays, %d bounces"
+                        % (n_tris, n, cfg["grid"], cfg["num_bounces"]),
+            "rays": int(cnt["rays"]), "mrays_s": round(cnt["rays"] / res[True] / 1e6, 1),
+            "ms": round(res[True] * 1e3, 2), "ms_without_facet_power": round(res[False] * 1e3, 2),
+            "ms_per_attitude": round(res[True] * 1e3 / n, 3), "nodes_per_ray": round(cnt["nodes"] / cnt["rays"], 2)}
 
 
 def scenes_camera_rays(cam):

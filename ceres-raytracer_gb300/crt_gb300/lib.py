@@ -78,7 +78,8 @@ REQUEST_RENDER, REQUEST_LIDAR, REQUEST_SRP = 0, 1, 2
 
 
 class ServerConfig(ctypes.Structure):
-    _fields_ = [("lanes", u32), ("lane_budget_bytes", sz), ("max_batch", u32)]
+    _fields_ = [("lanes", u32), ("lane_budget_bytes", sz), ("max_batch", u32), ("count_rays", u32),
+                ("wave_paths", u32)]
 
 
 class ServerRequest(ctypes.Structure):
@@ -234,6 +235,10 @@ class Context:
 
     def set_stream(self, stream_handle):
         self._check(self.L.crt_context_set_stream(self.h, stream_handle))
+
+    def stream_handle(self):
+        """cudaStream_t of the context (an integer), e.g. for torch.cuda.ExternalStream."""
+        return self.L.crt_context_get_stream(self.h) or 0
 
     def synchronize(self):
         self._check(self.L.crt_context_synchronize(self.h))
@@ -436,6 +441,19 @@ class Scene:
         self.ctx._check(self.ctx.L.crt_srp(self.h, ctypes.byref(d), ptr(q), n, ptr(f), ptr(t), ptr(fp)))
         return f, t, fp
 
+    def srp_into(self, sun_dir, quaternions, grid, force, torque, facet_power=None, num_bounces=2, flux=1361.0,
+                 c=299792458.0, center_of_mass=(0, 0, 0)):
+        """crt_srp with caller buffers (host arrays or device tensors): quaternions [n, 4] float64,
+        force / torque [n, 3] float64, facet_power [n, n_tris] float64 or None."""
+        d = SrpDesc()
+        d.sun_dir_inertial[:] = [float(x) for x in sun_dir]
+        d.flux, d.c = float(flux), float(c)
+        d.center_of_mass[:] = [float(x) for x in center_of_mass]
+        d.grid, d.num_bounces = int(grid), int(num_bounces)
+        n = int(quaternions.shape[0])
+        self.ctx._check(self.ctx.L.crt_srp(self.h, ctypes.byref(d), ptr(quaternions), n, ptr(force), ptr(torque),
+                                           ptr(facet_power)))
+
 
 def make_rays(o, d, tmin=0.0, tmax=3.4e38):
     """Structured FP32 ray array from [n, 3] origins and directions."""
@@ -453,11 +471,11 @@ class Server:
     "quaternions", "grid", "num_bounces", "flux", "c", "center_of_mass"}.  submit() returns a ticket;
     wait() returns (result dict, outputs)."""
 
-    def __init__(self, device=0, lanes=2, lane_budget_bytes=4 << 30, max_batch=64):
+    def __init__(self, device=0, lanes=2, lane_budget_bytes=4 << 30, max_batch=256, count_rays=False, wave_paths=0):
         self.L = load()
         self.h = None
         self.ctx = Context(device)
-        cfg = ServerConfig(int(lanes), int(lane_budget_bytes), int(max_batch))
+        cfg = ServerConfig(int(lanes), int(lane_budget_bytes), int(max_batch), int(bool(count_rays)), int(wave_paths))
         h = vp()
         rc = self.L.crt_server_create(int(device), ctypes.byref(cfg), ctypes.byref(h))
         if rc != CRT_OK:

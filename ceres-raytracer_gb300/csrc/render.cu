@@ -29,6 +29,7 @@
 #include "trace.cuh"
 
 #include <algorithm>
+#include <map>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -488,6 +489,21 @@ __global__ void k_finalize(Batch B, uint32_t n_req, uint32_t n_total) {
     }
 }
 
+// finalize of one request (the serving engine completes requests one by one)
+__global__ void k_finalize_one(Batch B, uint32_t slot) {
+    const RReq& R = B.rr[slot];
+    for (uint32_t pixel = blockIdx.x * blockDim.x + threadIdx.x; pixel < R.npix; pixel += gridDim.x * blockDim.x) {
+        const float4 m = B.pix[(size_t)R.pix_base + pixel];
+        const float v[4] = {m.x, m.y, m.z, 1.0f};
+        if (R.rad) R.rad[pixel] = make_float4(v[0], v[1], v[2], v[3]);
+        if (R.rgba) {
+            uint8_t qv[4];
+            for (int k = 0; k < 4; ++k) qv[k] = (uint8_t)fminf(fmaxf(v[k] * 256.0f, 0.0f), 255.0f);
+            R.rgba[pixel] = make_uchar4(qv[0], qv[1], qv[2], qv[3]);
+        }
+    }
+}
+
 __global__ void k_tan_table2(double* __restrict__ out, uint32_t nx, uint32_t ny, double hx, double hy) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < nx) out[i] = tan(-hx + (i + 0.5) * 2.0 * hx / nx);
@@ -501,6 +517,40 @@ inline uint32_t grid_for(crt_context* ctx, size_t n, int block = 256) {
 inline uint32_t tiles_items(uint32_t W, uint32_t H) { return ((W + 7) / 8) * ((H + 3) / 4) * 32u; }
 
 // ---------------------------------------------------------------- host side
+// The stage sequence of one wave on the context stream.  Every launch reads the wave from B.cur
+// (filled by k_wave_begin from B.descs[*B.wave_idx]), so the sequence can be captured once and
+// replayed.  P: path capacity, NL: light stride, lidar_items: bound on the wave's LiDAR items.
+void launch_wave_kernels(crt_context* ctx, const Batch& B, size_t P, size_t NL, uint32_t lidar_items,
+                         int max_bounces, uint32_t* qa, uint32_t* qb, uint32_t* tqueue) {
+    cudaStream_t st = ctx->stream;
+    const uint32_t gsz = grid_for(ctx, P);
+    k_wave_begin<<<1, 128, 0, st>>>(B);
+    check_launch(ctx, "k_wave_begin");
+    launch_trace<false>(ctx, SceneView{}, PrimaryJob{B}, (uint32_t)std::min<size_t>(P + lidar_items, 0xFFFFFF00u),
+                        &B.cur->n_primary, tqueue);
+    const uint32_t* q_in = nullptr;
+    uint32_t* q_out = qa;
+    for (int b = 0; b < max_bounces; ++b) {
+        k_shade<<<gsz, 256, 0, st>>>(B, b, q_in, q_out);
+        check_launch(ctx, "k_shade");
+        launch_trace<true>(ctx, SceneView{}, ShadowJob{B}, (uint32_t)std::min<size_t>(P * NL, 0xFFFFFF00u),
+                           &B.counts[2], tqueue);
+        k_accum<<<gsz, 256, 0, st>>>(B, b, q_in);
+        check_launch(ctx, "k_accum");
+        if (b < max_bounces - 1) {
+            launch_trace<false>(ctx, SceneView{}, BounceJob{B, q_out}, (uint32_t)P, &B.counts[1], tqueue);
+            k_queue_rotate<<<1, 1, 0, st>>>(B.counts);
+            check_launch(ctx, "k_queue_rotate");
+            q_in = q_out;
+            q_out = (q_out == qa) ? qb : qa;
+        }
+    }
+    k_update<<<gsz, 256, 0, st>>>(B);
+    check_launch(ctx, "k_update");
+    k_wave_end<<<1, 1, 0, st>>>(B);
+    check_launch(ctx, "k_wave_end");
+}
+
 struct HostReq {
     const crt_request* src;
     bool adaptive;
@@ -785,34 +835,7 @@ void run_batch(crt_context* ctx, const crt_request* reqs, size_t n, crt_batch_st
 
     // ---- one wave: every launch reads the wave from B.cur (graph-capturable)
     uint32_t* tqueue = (uint32_t*)ctx_scratch(ctx, SCR_QUEUE, 256);
-    const uint32_t gsz = grid_for(ctx, P);
-    auto launch_wave = [&]() {
-        k_wave_begin<<<1, 128, 0, st>>>(B);
-        check_launch(ctx, "k_wave_begin");
-        launch_trace<false>(ctx, SceneView{}, PrimaryJob{B}, (uint32_t)std::min<size_t>(P + lidar_items, 0xFFFFFF00u),
-                            &B.cur->n_primary, tqueue);
-        const uint32_t* q_in = nullptr;
-        uint32_t* q_out = qa;
-        for (int b = 0; b < max_bounces; ++b) {
-            k_shade<<<gsz, 256, 0, st>>>(B, b, q_in, q_out);
-            check_launch(ctx, "k_shade");
-            launch_trace<true>(ctx, SceneView{}, ShadowJob{B}, (uint32_t)std::min<size_t>(P * NL, 0xFFFFFF00u),
-                               &B.counts[2], tqueue);
-            k_accum<<<gsz, 256, 0, st>>>(B, b, q_in);
-            check_launch(ctx, "k_accum");
-            if (b < max_bounces - 1) {
-                launch_trace<false>(ctx, SceneView{}, BounceJob{B, q_out}, (uint32_t)P, &B.counts[1], tqueue);
-                k_queue_rotate<<<1, 1, 0, st>>>(B.counts);
-                check_launch(ctx, "k_queue_rotate");
-                q_in = q_out;
-                q_out = (q_out == qa) ? qb : qa;
-            }
-        }
-        k_update<<<gsz, 256, 0, st>>>(B);
-        check_launch(ctx, "k_update");
-        k_wave_end<<<1, 1, 0, st>>>(B);
-        check_launch(ctx, "k_wave_end");
-    };
+    auto launch_wave = [&]() { launch_wave_kernels(ctx, B, P, NL, lidar_items, max_bounces, qa, qb, tqueue); };
 
     size_t waves_run = 0;
     const bool graph_ok = ctx->use_graphs && !ctx->counting && plan.size() > 1;
@@ -923,6 +946,556 @@ void run_batch(crt_context* ctx, const crt_request* reqs, size_t n, crt_batch_st
     if (host_out) check_device_error(ctx, "crt_batch");
 }
 
+// ---------------------------------------------------------------- serving engine
+// Continuous batching at wave granularity: requests join a lane's engine while others are on the
+// GPU and leave it as soon as their last wave has run.  Per-request pixel state (running mean,
+// sample count, done flag) lives in a unit arena (one unit per pixel), host-output staging,
+// adaptive pixel sets and LiDAR tangent tables in a byte arena; both are first-fit allocators over
+// fixed device buffers sized from the lane budget, so admission is by free memory.  Each step plans
+// one wave shortest-remaining-work first (LiDAR scans first: one launch finishes them), runs the
+// same stage kernels as crt_batch, finalizes the requests whose work is complete and synchronises.
+// Random streams and per-pixel sample order are those of crt_render, so results do not depend on
+// what else shares the waves.
+
+class Ranges {   // first-fit allocator over [0, cap)
+  public:
+    void reset(size_t cap) {
+        free_.clear();
+        cap_ = cap;
+        if (cap) free_[0] = cap;
+    }
+    size_t cap() const { return cap_; }
+    bool alloc(size_t n, size_t& off) {
+        for (auto it = free_.begin(); it != free_.end(); ++it) {
+            if (it->second < n) continue;
+            off = it->first;
+            const size_t rest = it->second - n;
+            free_.erase(it);
+            if (rest) free_[off + n] = rest;
+            return true;
+        }
+        return false;
+    }
+    void release(size_t off, size_t n) {
+        if (!n) return;
+        auto it = free_.emplace(off, n).first;
+        auto nx = std::next(it);
+        if (nx != free_.end() && it->first + it->second == nx->first) {
+            it->second += nx->second;
+            free_.erase(nx);
+        }
+        if (it != free_.begin()) {
+            auto pv = std::prev(it);
+            if (pv->first + pv->second == it->first) {
+                pv->second += it->second;
+                free_.erase(it);
+            }
+        }
+    }
+
+  private:
+    std::map<size_t, size_t> free_;
+    size_t cap_ = 0;
+};
+
+constexpr uint32_t ENGINE_SLOTS = 1024;      // resident render requests per engine
+constexpr size_t UNIT_BYTES = 16 + 4 + 1;    // pix, taken, done
+inline size_t up256(size_t n) { return (n + 255) & ~size_t(255); }
+
+struct EReq {
+    uint64_t tag = 0, seq = 0;
+    crt_request q;
+    bool lidar = false, finished = false;
+    uint32_t slot = 0, npix = 0;
+    size_t unit_off = 0, units = 0, byte_off = 0, bytes = 0;
+    bool adaptive = false;
+    uint32_t next_sample = 0, upto = 0, total = 0, n_active = 0;
+    const uint32_t* active = nullptr;
+    uint32_t* act_buf[2] = {nullptr, nullptr};
+    int act_sel = 0;
+    int num_bounces = 0;
+    uint32_t n_lights = 0, skipped = 0;
+    uchar4* rgba = nullptr;
+    float4* rad = nullptr;
+    double* range = nullptr;
+    uint32_t* prim = nullptr;
+    double* tan = nullptr;
+    uint64_t remaining() const {
+        if (lidar) return 0;
+        return (uint64_t)(total - next_sample) * (adaptive && next_sample >= upto ? n_active : npix);
+    }
+};
+
+}  // namespace
+
+struct WaveEngine {
+    crt_context* ctx = nullptr;
+    size_t budget = 0;
+    uint32_t P = 0, NL = 0, want_P = 0, want_NL = 1;
+    char* paths = nullptr;
+    char* units_mem = nullptr;
+    char* bytes_mem = nullptr;
+    char* fixed = nullptr;           // request tables, wave descriptor, counters
+    Ranges units, bytes;
+    std::vector<uint32_t> free_slots;
+    std::vector<EReq> res;
+    uint64_t seq = 0;
+    struct Up {
+        void* dst;
+        size_t off, n;
+    };
+    std::vector<char> up_data;
+    std::vector<Up> ups;
+    char* pinned = nullptr;
+    size_t pinned_bytes = 0;
+    // fixed device tables
+    RReq* d_rr = nullptr;
+    LightDev* d_lights = nullptr;
+    LReq* d_lr = nullptr;
+    WaveDesc* d_desc = nullptr;
+    WaveDesc* d_cur = nullptr;
+    uint32_t* d_wave_idx = nullptr;
+    uint32_t* d_counts = nullptr;
+    uint32_t* d_acount = nullptr;
+    uint32_t* d_tqueue = nullptr;
+
+    float4* pix() const { return (float4*)units_mem; }
+    uint32_t* taken() const { return (uint32_t*)(units_mem + up256(units.cap() * 16)); }
+    uint8_t* done() const { return (uint8_t*)(units_mem + up256(units.cap() * 16) + up256(units.cap() * 4)); }
+    static size_t path_bytes(size_t P, size_t NL) {
+        return P * (32 + 4 + 16 * 5 + 12 + 8) + P * NL * (16 + 1 + 32 + 12) + 64 * 256;
+    }
+};
+
+namespace {
+
+void engine_alloc_units(WaveEngine* e, size_t cap) {
+    CRT_CHECK(cap < (1ull << 32), CRT_ERR_OOM, "serving pixel arena limited to 2^32 pixels");
+    if (e->units_mem) CRT_CUDA(cudaFree(e->units_mem));
+    e->units_mem = nullptr;
+    e->units.reset(0);
+    const size_t b = up256(cap * 16) + up256(cap * 4) + up256(cap);
+    CRT_CUDA(cudaMalloc(&e->units_mem, b));
+    e->units.reset(cap);
+}
+
+void engine_alloc_bytes(WaveEngine* e, size_t cap) {
+    CRT_CHECK(cap < (32ull << 30), CRT_ERR_OOM, "serving byte arena limited to 32 GiB");
+    if (e->bytes_mem) CRT_CUDA(cudaFree(e->bytes_mem));
+    e->bytes_mem = nullptr;
+    e->bytes.reset(0);
+    cap = up256(cap);
+    CRT_CUDA(cudaMalloc(&e->bytes_mem, cap));
+    e->bytes.reset(cap);
+}
+
+void engine_upload(WaveEngine* e, void* dst, const void* src, size_t n) {
+    const size_t off = e->up_data.size();
+    e->up_data.resize(off + up256(n));
+    std::memcpy(e->up_data.data() + off, src, n);
+    e->ups.push_back({dst, off, n});
+}
+
+void engine_flush_uploads(WaveEngine* e) {
+    if (e->ups.empty()) return;
+    const size_t need = e->up_data.size();
+    if (e->pinned_bytes < need) {   // no copy from the pinned buffer is in flight between steps
+        if (e->pinned) CRT_CUDA(cudaFreeHost(e->pinned));
+        e->pinned = nullptr;
+        e->pinned_bytes = 0;
+        const size_t cap = (need + need / 2 + 4095) & ~size_t(4095);
+        CRT_CUDA(cudaMallocHost(&e->pinned, cap));
+        e->pinned_bytes = cap;
+    }
+    std::memcpy(e->pinned, e->up_data.data(), need);
+    for (const WaveEngine::Up& u : e->ups)
+        CRT_CUDA(cudaMemcpyAsync(u.dst, e->pinned + u.off, u.n, cudaMemcpyHostToDevice, e->ctx->stream));
+    e->ups.clear();
+    e->up_data.clear();
+}
+
+void engine_release(WaveEngine* e, EReq& r) {
+    if (r.units) e->units.release(r.unit_off, r.units);
+    if (r.bytes) e->bytes.release(r.byte_off, r.bytes);
+    if (!r.lidar) e->free_slots.push_back(r.slot);
+    r.units = r.bytes = 0;
+}
+
+}  // namespace
+
+WaveEngine* engine_create(crt_context* ctx, size_t budget_bytes) {
+    WaveEngine* e = new WaveEngine();
+    e->ctx = ctx;
+    e->budget = budget_bytes;
+    try {
+        CRT_CUDA(cudaSetDevice(ctx->device));
+        const size_t fixed = up256(sizeof(RReq) * ENGINE_SLOTS) + up256(sizeof(LightDev) * ENGINE_SLOTS * MAX_LIGHTS) +
+                             up256(sizeof(LReq) * MAX_LIDAR) + 2 * up256(sizeof(WaveDesc)) + 4 * 256 +
+                             up256(4 * ENGINE_SLOTS);
+        CRT_CUDA(cudaMalloc(&e->fixed, fixed));
+        char* f = e->fixed;
+        auto take = [&](size_t n) { char* q = f; f += up256(n); return q; };
+        e->d_rr = (RReq*)take(sizeof(RReq) * ENGINE_SLOTS);
+        e->d_lights = (LightDev*)take(sizeof(LightDev) * ENGINE_SLOTS * MAX_LIGHTS);
+        e->d_lr = (LReq*)take(sizeof(LReq) * MAX_LIDAR);
+        e->d_desc = (WaveDesc*)take(sizeof(WaveDesc));
+        e->d_cur = (WaveDesc*)take(sizeof(WaveDesc));
+        e->d_wave_idx = (uint32_t*)take(256);
+        e->d_counts = (uint32_t*)take(256);
+        e->d_tqueue = (uint32_t*)take(256);
+        take(256);
+        e->d_acount = (uint32_t*)take(4 * ENGINE_SLOTS);
+        for (uint32_t s = ENGINE_SLOTS; s > 0; --s) e->free_slots.push_back(s - 1);
+        // budget: path buffers for one wave, then pixel state and staging (2 : 3)
+        e->want_P = std::max<uint32_t>(ctx->wave_paths, 1u << 16);
+        // (a request larger than what is left runs alone, its arena growing to fit it)
+        const size_t pb = WaveEngine::path_bytes(e->want_P, 1);
+        const size_t rest = budget_bytes > pb ? budget_bytes - pb : 0;
+        engine_alloc_units(e, std::max<size_t>(rest * 2 / 5 / UNIT_BYTES, 1));
+        engine_alloc_bytes(e, std::max<size_t>(rest * 3 / 5, 256));
+    } catch (...) {
+        engine_destroy(e);
+        throw;
+    }
+    return e;
+}
+
+void engine_destroy(WaveEngine* e) {
+    if (!e) return;
+    cudaSetDevice(e->ctx->device);
+    cudaStreamSynchronize(e->ctx->stream);
+    cudaFree(e->paths);
+    cudaFree(e->units_mem);
+    cudaFree(e->bytes_mem);
+    cudaFree(e->fixed);
+    if (e->pinned) cudaFreeHost(e->pinned);
+    delete e;
+}
+
+size_t engine_resident(const WaveEngine* e) { return e->res.size(); }
+
+// Admits a request when its state fits the free arenas now (false: retry after requests finish).
+// A request larger than an arena is admitted alone, the arena growing to fit it.
+bool engine_admit(WaveEngine* e, const crt_request& q, uint64_t tag) {
+    check_request(q);
+    CRT_CHECK(q.scene->ctx && q.scene->ctx->device == e->ctx->device, CRT_ERR_INVALID,
+              "request scene lives on another device");
+    crt_context* ctx = e->ctx;
+    cudaStream_t st = ctx->stream;
+    EReq r;
+    std::memset(&r.q, 0, sizeof(r.q));
+    r.q = q;
+    r.tag = tag;
+    if (q.kind == CRT_REQUEST_RENDER) {
+        if (e->free_slots.empty()) return false;
+        const CamBasis cam = make_camera_basis(q.camera);
+        const crt_render_params& p = *q.params;
+        r.npix = cam.width * cam.height;
+        const bool host_rgba = q.rgba8 && !is_device_ptr(q.rgba8);
+        const bool host_rad = q.radiance && !is_device_ptr(q.radiance);
+        r.adaptive = p.noise_threshold > 0 && p.min_samples < p.max_samples;
+        r.total = (uint32_t)std::max(0, p.max_samples);
+        r.upto = r.adaptive ? (uint32_t)std::min<int>(std::max(p.min_samples, 1), (int)r.total) : r.total;
+        r.n_active = r.npix;
+        r.num_bounces = p.num_bounces;
+        r.n_lights = q.n_lights;
+        const size_t b_rgba = host_rgba ? up256((size_t)r.npix * 4) : 0;
+        const size_t b_rad = host_rad ? up256((size_t)r.npix * 16) : 0;
+        const size_t b_act = r.adaptive ? 2 * up256((size_t)r.npix * 4) : 0;
+        r.units = r.npix;
+        r.bytes = b_rgba + b_rad + b_act;
+        const bool alone = e->res.empty();
+        if (r.units > e->units.cap() && alone) engine_alloc_units(e, r.units + r.units / 4);
+        if (r.bytes > e->bytes.cap() && alone) engine_alloc_bytes(e, r.bytes + r.bytes / 4);
+        if (!e->units.alloc(r.units, r.unit_off)) return false;
+        if (r.bytes && !e->bytes.alloc(r.bytes, r.byte_off)) {
+            e->units.release(r.unit_off, r.units);
+            return false;
+        }
+        r.slot = e->free_slots.back();
+        e->free_slots.pop_back();
+        char* b = e->bytes_mem + r.byte_off;
+        r.rgba = q.rgba8 ? (host_rgba ? (uchar4*)b : (uchar4*)q.rgba8) : nullptr;
+        b += b_rgba;
+        r.rad = q.radiance ? (host_rad ? (float4*)b : (float4*)q.radiance) : nullptr;
+        b += b_rad;
+        if (r.adaptive) {
+            r.act_buf[0] = (uint32_t*)b;
+            r.act_buf[1] = (uint32_t*)(b + up256((size_t)r.npix * 4));
+        }
+        RReq R;
+        std::memset(&R, 0, sizeof(R));
+        R.sv = scene_view(q.scene);
+        R.cam = cam;
+        R.c = RenderCtl{cam.width, cam.height, p.min_samples, p.max_samples, (float)p.noise_threshold, p.num_bounces,
+                        (uint32_t)p.seed, (uint32_t)(p.seed >> 32), p.request};
+        R.light_base = r.slot * MAX_LIGHTS;
+        R.n_lights = q.n_lights;
+        R.pix_base = (uint32_t)r.unit_off;
+        R.npix = r.npix;
+        R.rgba = r.rgba;
+        R.rad = r.rad;
+        LightDev lights[MAX_LIGHTS];
+        for (uint32_t l = 0; l < q.n_lights; ++l) {
+            LightDev& d = lights[l];
+            d.type = q.lights[l].type;
+            d.intensity = (float)q.lights[l].intensity;
+            for (int k = 0; k < 3; ++k) d.pos[k] = (float)q.lights[l].position[k];
+            for (int k = 0; k < 9; ++k) d.R[k] = (float)q.lights[l].rotation[k];
+            d.size[0] = (float)q.lights[l].size[0];
+            d.size[1] = (float)q.lights[l].size[1];
+        }
+        engine_upload(e, e->d_rr + r.slot, &R, sizeof(R));
+        if (q.n_lights) engine_upload(e, e->d_lights + R.light_base, lights, sizeof(LightDev) * q.n_lights);
+        CRT_CUDA(cudaMemsetAsync(e->pix() + r.unit_off, 0, (size_t)r.npix * 16, st));
+        CRT_CUDA(cudaMemsetAsync(e->taken() + r.unit_off, 0, (size_t)r.npix * 4, st));
+        CRT_CUDA(cudaMemsetAsync(e->done() + r.unit_off, 0, r.npix, st));
+        e->want_P = std::max(e->want_P, r.npix);
+        e->want_NL = std::max(e->want_NL, std::max<uint32_t>(q.n_lights, 1));
+    } else {
+        r.lidar = true;
+        const crt_lidar_grid_desc& g = *q.lidar;
+        const size_t n = (size_t)g.nx * g.ny;
+        const bool host_range = !is_device_ptr(q.range);
+        const bool host_prim = q.prim && !is_device_ptr(q.prim);
+        const size_t b_tan = up256(8 * ((size_t)g.nx + g.ny));
+        const size_t b_range = host_range ? up256(n * 8) : 0;
+        const size_t b_prim = host_prim ? up256(n * 4) : 0;
+        r.bytes = b_tan + b_range + b_prim;
+        if (r.bytes > e->bytes.cap() && e->res.empty()) engine_alloc_bytes(e, r.bytes + r.bytes / 4);
+        if (!e->bytes.alloc(r.bytes, r.byte_off)) return false;
+        char* b = e->bytes_mem + r.byte_off;
+        r.tan = (double*)b;
+        b += b_tan;
+        r.range = host_range ? (double*)b : q.range;
+        b += b_range;
+        r.prim = q.prim ? (host_prim ? (uint32_t*)b : q.prim) : nullptr;
+        const uint32_t nt = g.nx + g.ny;
+        k_tan_table2<<<(nt + 255) / 256, 256, 0, st>>>(r.tan, g.nx, g.ny, g.half_angle_x, g.half_angle_y);
+        check_launch(ctx, "k_tan_table2");
+    }
+    r.seq = e->seq++;
+    e->res.push_back(r);
+    return true;
+}
+
+// Drops every resident request (after a failed step); returns their tags.
+void engine_abort(WaveEngine* e, std::vector<uint64_t>& dropped) {
+    cudaStreamSynchronize(e->ctx->stream);
+    for (EReq& r : e->res) {
+        engine_release(e, r);
+        dropped.push_back(r.tag);
+    }
+    e->res.clear();
+    e->ups.clear();
+    e->up_data.clear();
+}
+
+// Runs one wave over the resident requests and appends the tags of the requests it completed.
+void engine_step(WaveEngine* e, std::vector<uint64_t>& completed) {
+    crt_context* ctx = e->ctx;
+    cudaStream_t st = ctx->stream;
+    CRT_CUDA(cudaSetDevice(ctx->device));
+    if (e->res.empty()) return;
+    // path buffers (wave-local state only, so they can be resized between waves)
+    if (e->want_P > e->P || e->want_NL > e->NL) {
+        CRT_CUDA(cudaStreamSynchronize(st));
+        if (e->paths) CRT_CUDA(cudaFree(e->paths));
+        e->paths = nullptr;
+        e->P = e->NL = 0;
+        CRT_CUDA(cudaMalloc(&e->paths, WaveEngine::path_bytes(e->want_P, e->want_NL)));
+        e->P = e->want_P;
+        e->NL = e->want_NL;
+    }
+    const size_t P = e->P, NL = e->NL;
+    Batch B;
+    std::memset(&B, 0, sizeof(B));
+    {
+        char* b = e->paths;
+        auto take = [&](size_t n) { char* q = b; b += up256(n); return q; };
+        B.ray = (float4*)take(P * 32);
+        B.skip = (uint32_t*)take(P * 4);
+        B.hit = (float4*)take(P * 16);
+        B.weight = (float4*)take(P * 16);
+        B.wacc = (float4*)take(P * 16);
+        B.rad = (float4*)take(P * 16);
+        B.preq = (uint32_t*)take(P * 4);
+        B.ppix = (uint32_t*)take(P * 4);
+        B.psample = (uint32_t*)take(P * 4);
+        B.contrib = (float4*)take(P * NL * 16);
+        B.occ = (uint8_t*)take(P * NL);
+        B.sray = (float4*)take(P * NL * 32);
+        B.sidx = (uint32_t*)take(P * NL * 4);
+        B.sskip = (uint32_t*)take(P * NL * 4);
+        B.sreq = (uint32_t*)take(P * NL * 4);
+    }
+    // the two path queues follow the path buffers (path_bytes reserves 8 bytes per path for them)
+    uint32_t* qa = (uint32_t*)((char*)B.sreq + up256(P * NL * 4));
+    uint32_t* qb = qa + P;
+    B.rr = e->d_rr;
+    B.lr = e->d_lr;
+    B.lights = e->d_lights;
+    B.tan = (const double*)e->bytes_mem;
+    B.descs = e->d_desc;
+    B.cur = e->d_cur;
+    B.wave_idx = e->d_wave_idx;
+    B.counts = e->d_counts;
+    B.L = (uint32_t)NL;
+    B.pix = e->pix();
+    B.taken = e->taken();
+    B.done = e->done();
+    for (EReq& r : e->res)
+        if (!r.lidar && r.next_sample >= r.total && (!r.adaptive || r.next_sample >= r.upto)) r.finished = true;
+
+    // adaptive requests past their fixed prefix: compact the still-active pixels
+    std::vector<EReq*> compacting;
+    for (EReq& r : e->res)
+        if (!r.lidar && r.adaptive && r.next_sample >= r.upto && r.next_sample < r.total && r.n_active > 0)
+            compacting.push_back(&r);
+    if (!compacting.empty()) {
+        CRT_CUDA(cudaMemsetAsync(e->d_acount, 0, 4 * compacting.size(), st));
+        for (size_t k = 0; k < compacting.size(); ++k) {
+            EReq& r = *compacting[k];
+            k_compact<<<grid_for(ctx, r.n_active), 256, 0, st>>>(r.active, r.n_active, B.done, (uint32_t)r.unit_off,
+                                                                 r.act_buf[r.act_sel], e->d_acount + k);
+            check_launch(ctx, "k_compact");
+        }
+        std::vector<uint32_t> cnt(compacting.size());
+        CRT_CUDA(cudaMemcpyAsync(cnt.data(), e->d_acount, 4 * cnt.size(), cudaMemcpyDeviceToHost, st));
+        CRT_CUDA(cudaStreamSynchronize(st));
+        for (size_t k = 0; k < compacting.size(); ++k) {
+            EReq& r = *compacting[k];
+            r.n_active = cnt[k];
+            r.active = r.act_buf[r.act_sel];
+            r.act_sel ^= 1;
+            if (r.n_active == 0) r.finished = true;
+        }
+    }
+
+    // plan one wave: LiDAR scans, then renders by least remaining work
+    WaveDesc w;
+    std::memset(&w, 0, sizeof(w));
+    std::vector<LReq> lreqs;
+    std::vector<EReq*> wave_lidar;
+    uint32_t lidar_items = 0;
+    for (EReq& r : e->res) {
+        if (!r.lidar || lreqs.size() == (size_t)MAX_LIDAR) continue;
+        const crt_lidar_grid_desc& g = *r.q.lidar;
+        LReq L;
+        std::memset(&L, 0, sizeof(L));
+        L.sv = scene_view(r.q.scene);
+        for (int k = 0; k < 3; ++k) L.o[k] = g.position[k];
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) L.rt[3 * a + b] = g.rotation[3 * b + a];
+        L.zsign = g.z_positive ? 1.0 : -1.0;
+        L.nx = g.nx;
+        L.ny = g.ny;
+        L.tan_base = (uint32_t)(r.byte_off / 8);   // byte arena < 32 GiB (checked at creation)
+        L.item_base = lidar_items;
+        L.range = r.range;
+        L.prim = r.prim;
+        const uint32_t items = tiles_items(g.nx, g.ny);
+        if ((uint64_t)lidar_items + items > 0xF0000000ull) break;
+        lidar_items += items;
+        lreqs.push_back(L);
+        wave_lidar.push_back(&r);
+    }
+    w.n_lidar_items = lidar_items;
+    w.n_lreq = (uint32_t)lreqs.size();
+    std::vector<EReq*> order;
+    for (EReq& r : e->res)
+        if (!r.lidar && !r.finished && r.next_sample < r.total) order.push_back(&r);
+    // least remaining work first; a request passed over for 4 waves goes first (no starvation)
+    std::stable_sort(order.begin(), order.end(), [](const EReq* a, const EReq* b) {
+        const bool sa = a->skipped >= 4, sb = b->skipped >= 4;
+        if (sa != sb) return sa;
+        if (sa) return a->seq < b->seq;
+        const uint64_t ra = a->remaining(), rb = b->remaining();
+        return ra != rb ? ra < rb : a->seq < b->seq;
+    });
+    int max_bounces = 0;
+    for (EReq* rp : order) {
+        EReq& r = *rp;
+        if (w.n_slices == MAX_SLICES) break;
+        const uint32_t room = (uint32_t)(P - w.n_paths);
+        Slice& S = w.slices[w.n_slices];
+        if (r.next_sample < r.upto) {
+            const uint32_t ns = std::min<uint32_t>(r.upto - r.next_sample, room / r.npix);
+            if (ns == 0) {
+                ++r.skipped;
+                continue;
+            }
+            S.req = r.slot;
+            S.s0 = r.next_sample;
+            S.ns = ns;
+            S.npix = r.npix;
+            S.active = nullptr;
+        } else {
+            if (r.n_active > room) {
+                ++r.skipped;
+                continue;
+            }
+            S.req = r.slot;
+            S.s0 = r.next_sample;
+            S.ns = 1;
+            S.npix = r.n_active;
+            S.active = r.active;
+        }
+        S.path_base = w.n_paths;
+        S.upd_base = w.n_update;
+        w.n_paths += S.ns * S.npix;
+        w.n_update += S.npix;
+        w.n_slices++;
+        r.next_sample += S.ns;
+        r.skipped = 0;
+        max_bounces = std::max(max_bounces, r.num_bounces);
+        if (r.next_sample >= r.total) r.finished = true;
+    }
+    w.n_primary = w.n_lidar_items + w.n_paths;
+
+    // run it
+    // one flush per step: the pinned buffer is reused only after the step's closing synchronise
+    const bool any_work = w.n_primary > 0;
+    if (any_work) {
+        if (lreqs.size()) engine_upload(e, e->d_lr, lreqs.data(), sizeof(LReq) * lreqs.size());
+        engine_upload(e, e->d_desc, &w, sizeof(WaveDesc));
+    }
+    engine_flush_uploads(e);
+    if (any_work) {
+        CRT_CUDA(cudaMemsetAsync(e->d_wave_idx, 0, 4, st));
+        launch_wave_kernels(ctx, B, P, NL, lidar_items, max_bounces, qa, qb, e->d_tqueue);
+    }
+    // completions: finalize renders, copy host outputs
+    std::vector<EReq*> done_now;
+    for (EReq* r : wave_lidar) {
+        const crt_lidar_grid_desc& g = *r->q.lidar;
+        const size_t n = (size_t)g.nx * g.ny;
+        out_finish(ctx, r->q.range, r->range, n * 8);
+        if (r->q.prim) out_finish(ctx, r->q.prim, r->prim, n * 4);
+        r->finished = true;
+    }
+    for (EReq& r : e->res) {
+        if (r.lidar || !r.finished) continue;
+        k_finalize_one<<<grid_for(ctx, r.npix), 256, 0, st>>>(B, r.slot);
+        check_launch(ctx, "k_finalize_one");
+        if (r.q.rgba8) out_finish(ctx, r.q.rgba8, r.rgba, (size_t)r.npix * 4);
+        if (r.q.radiance) out_finish(ctx, r.q.radiance, r.rad, (size_t)r.npix * 16);
+    }
+    check_device_error(ctx, "serving wave");   // synchronises the stream
+    std::vector<EReq> keep;
+    keep.reserve(e->res.size());
+    for (EReq& r : e->res) {
+        if (r.finished) {
+            engine_release(e, r);
+            completed.push_back(r.tag);
+        } else {
+            keep.push_back(r);
+        }
+    }
+    e->res.swap(keep);
+}
+
+namespace {
 }  // namespace
 
 void batch_run(crt_context* ctx, const crt_request* reqs, size_t n, crt_batch_stats* stats) {

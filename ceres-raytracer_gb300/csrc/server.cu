@@ -1,10 +1,11 @@
 // Serving loop: continuous batching of render / LiDAR / SRP requests over resident scenes.
 //
-// Each lane owns a context (stream, scratch, counters, error word) and a host thread.  A lane takes
-// the oldest queued requests while their estimated device footprint fits its budget (a request
-// larger than the budget runs alone), runs the render and LiDAR requests as one crt_batch and the
-// SRP requests one by one, then publishes per-request timings.  With two or more lanes, a batch is
-// formed and launched while the previous one is still on the GPU, so their work overlaps.
+// Each lane owns a context (stream, scratch, counters, error word), a wave engine and a host
+// thread.  Between waves a lane admits queued requests in arrival order while their per-request
+// state (pixel accumulators, staging, LiDAR tables) fits the engine's free memory, runs the SRP
+// queries, then runs one wave over everything resident; a request leaves as soon as its last wave
+// has run.  Requests that arrive while others are on the GPU therefore join the next wave, and
+// with two or more lanes one lane plans and launches while the other's wave is on the GPU.
 #include "common.cuh"
 
 #include <chrono>
@@ -49,6 +50,7 @@ struct crt_server {
     int device = 0;
     crt_server_config cfg;
     std::vector<crt_context*> lanes;
+    std::vector<WaveEngine*> engines;
     std::vector<std::thread> threads;
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
@@ -61,71 +63,108 @@ struct crt_server {
 
 namespace {
 
+void publish(crt_server* S, Pending* p, int status, double start_s, double end_s, uint32_t batch_size) {
+    crt_server_result r;
+    r.status = status;
+    r.submit_s = p->submit_s;
+    r.start_s = start_s;
+    r.end_s = end_s;
+    r.batch_size = batch_size;
+    S->done[p->ticket] = r;
+    S->stats.completed++;
+    if (status != CRT_OK) S->stats.failed++;
+    delete p;
+}
+
+// One lane: admits queued requests into its wave engine whenever their state fits (FIFO), runs SRP
+// queries between waves, and runs one wave per iteration.  Requests leave when their last wave is done.
 void lane_loop(crt_server* S, size_t lane) {
     crt_context* ctx = S->lanes[lane];
+    WaveEngine* E = S->engines[lane];
     cudaSetDevice(S->device);
+    std::unordered_map<uint64_t, std::pair<Pending*, double>> resident;   // tag -> (request, admitted at)
+    std::vector<uint64_t> finished;
     while (true) {
-        std::vector<Pending*> batch;
+        std::vector<Pending*> srp;
         {
             std::unique_lock<std::mutex> lk(S->mu);
-            S->cv_work.wait(lk, [&] { return S->stop || !S->queue.empty(); });
-            if (S->queue.empty()) return;   // stopping and drained
-            size_t used = 0;
-            while (!S->queue.empty() && batch.size() < S->cfg.max_batch) {
+            S->cv_work.wait(lk, [&] { return S->stop || !S->queue.empty() || !resident.empty(); });
+            if (S->stop && S->queue.empty() && resident.empty()) return;
+            const double now = now_s();
+            while (!S->queue.empty() && resident.size() < S->cfg.max_batch) {
                 Pending* p = S->queue.front();
-                if (!batch.empty() && used + p->footprint > S->cfg.lane_budget_bytes) break;
-                used += p->footprint;
-                batch.push_back(p);
+                if (p->srp) {
+                    srp.push_back(p);
+                    S->queue.pop_front();
+                    continue;
+                }
+                bool ok = false;
+                const int rc = crt_guard(ctx, [&] { ok = engine_admit(E, p->req, p->ticket); });
+                if (rc != CRT_OK) {   // validated at submission, so only a CUDA failure gets here
+                    S->queue.pop_front();
+                    publish(S, p, rc, now, now_s(), 0);
+                    continue;
+                }
+                if (!ok) break;       // head of the queue waits for memory (FIFO admission)
                 S->queue.pop_front();
+                resident[p->ticket] = {p, now};
             }
+        }
+        S->cv_done.notify_all();
+        crt_counters c0{}, c1{};
+        if (S->cfg.count_rays) crt_context_get_counters(ctx, &c0);
+        for (Pending* p : srp) {
+            const double t0 = now_s();
+            int rc = crt_guard(ctx, [&] {
+                srp_run(ctx, p->req.scene, &p->srp_desc, p->quats.data(), p->quats.size() / 4, p->force, p->torque,
+                        nullptr);
+            });
+            const int sync = crt_context_synchronize(ctx);
+            if (rc == CRT_OK) rc = sync;
+            const double t1 = now_s();
+            std::lock_guard<std::mutex> lk(S->mu);
+            publish(S, p, rc, t0, t1, 1);
+            S->stats.batches++;
+            S->stats.busy_s += t1 - t0;
+        }
+        if (!srp.empty()) S->cv_done.notify_all();
+        if (resident.empty()) {
+            if (S->cfg.count_rays && !srp.empty()) {
+                crt_context_get_counters(ctx, &c1);
+                std::lock_guard<std::mutex> lk(S->mu);
+                S->stats.rays += c1.rays - c0.rays;
+            }
+            continue;
         }
         const double t0 = now_s();
-        int status = CRT_OK;
-        std::vector<int> srp_status(batch.size(), CRT_OK);
-        uint64_t rays = 0;
-        {
-            std::vector<crt_request> reqs;
-            for (Pending* p : batch)
-                if (!p->srp) reqs.push_back(p->req);
-            crt_counters c0{}, c1{};
-            crt_context_get_counters(ctx, &c0);
-            if (!reqs.empty())
-                status = crt_guard(ctx, [&] { batch_run(ctx, reqs.data(), reqs.size(), nullptr); });
-            for (size_t k = 0; k < batch.size(); ++k) {
-                Pending* p = batch[k];
-                if (!p->srp) continue;
-                srp_status[k] = crt_guard(ctx, [&] {
-                    srp_run(ctx, p->req.scene, &p->srp_desc, p->quats.data(), p->quats.size() / 4, p->force,
-                            p->torque, nullptr);
-                });
-            }
-            const int sync = crt_context_synchronize(ctx);
-            if (status == CRT_OK) status = sync;
-            crt_context_get_counters(ctx, &c1);
-            rays = c1.rays - c0.rays;
+        const size_t sharing = resident.size();
+        finished.clear();
+        int rc = crt_guard(ctx, [&] { engine_step(E, finished); });
+        if (rc != CRT_OK) {
+            finished.clear();
+            engine_abort(E, finished);
         }
         const double t1 = now_s();
+        if (S->cfg.count_rays) crt_context_get_counters(ctx, &c1);
         {
             std::lock_guard<std::mutex> lk(S->mu);
-            for (size_t k = 0; k < batch.size(); ++k) {
-                Pending* p = batch[k];
-                crt_server_result r;
-                r.status = p->srp ? srp_status[k] : status;
-                r.submit_s = p->submit_s;
-                r.start_s = t0;
-                r.end_s = t1;
-                r.batch_size = (uint32_t)batch.size();
-                S->done[p->ticket] = r;
-                S->stats.completed++;
-                if (r.status != CRT_OK) S->stats.failed++;
-                delete p;
+            for (uint64_t tag : finished) {
+                auto it = resident.find(tag);
+                if (it == resident.end()) continue;
+                publish(S, it->second.first, rc, it->second.second, t1, (uint32_t)sharing);
+                resident.erase(it);
             }
             S->stats.batches++;
-            S->stats.rays += rays;
             S->stats.busy_s += t1 - t0;
+            if (S->cfg.count_rays) S->stats.rays += c1.rays - c0.rays;
         }
         S->cv_done.notify_all();
     }
+}
+
+size_t srp_footprint(const crt_srp_desc& d, size_t n_att) {
+    const size_t tiles = ((size_t)(d.grid + 7) / 8) * ((d.grid + 3) / 4);
+    return (tiles / 16 + 1) * 48 * std::max<size_t>(n_att, 1) + n_att * 112;
 }
 
 thread_local std::string t_submit_error;
@@ -149,10 +188,6 @@ int submit_guard(F&& f) {
     }
 }
 
-size_t srp_footprint(const crt_srp_desc& d, size_t n_att) {
-    const size_t tiles = ((size_t)(d.grid + 7) / 8) * ((d.grid + 3) / 4);
-    return (tiles / 16 + 1) * 48 * std::max<size_t>(n_att, 1) + n_att * 112;
-}
 
 }  // namespace
 
@@ -161,22 +196,30 @@ extern "C" {
 int crt_server_create(int device, const crt_server_config* cfg, crt_server** out) {
     if (!out) return CRT_ERR_INVALID;
     *out = nullptr;
-    crt_server_config c = cfg ? *cfg : crt_server_config{2, (size_t)4 << 30, 64};
-    if (c.lanes < 1 || c.lanes > 8 || c.max_batch < 1) return CRT_ERR_INVALID;
+    crt_server_config c = cfg ? *cfg : crt_server_config{2, (size_t)4 << 30, 256, 0, 0};
+    if (c.wave_paths == 0) c.wave_paths = 1u << 22;
+    if (c.lanes < 1 || c.lanes > 8 || c.max_batch < 1 || c.wave_paths < (1u << 16)) return CRT_ERR_INVALID;
     crt_server* S = new crt_server();
     S->device = device;
     S->cfg = c;
     std::memset(&S->stats, 0, sizeof(S->stats));
+    auto unwind = [&](int rc) {
+        for (WaveEngine* e : S->engines) engine_destroy(e);
+        for (crt_context* x : S->lanes) crt_context_destroy(x);
+        delete S;
+        return rc;
+    };
     for (uint32_t l = 0; l < c.lanes; ++l) {
         crt_context* ctx = nullptr;
         int rc = crt_context_create(device, &ctx);
-        if (rc != CRT_OK) {
-            for (crt_context* x : S->lanes) crt_context_destroy(x);
-            delete S;
-            return rc;
-        }
-        crt_context_set_counting(ctx, 1);   // per-batch ray counts (a few integer adds per node visit)
+        if (rc != CRT_OK) return unwind(rc);
         S->lanes.push_back(ctx);
+        ctx->wave_paths = c.wave_paths;
+        if (c.count_rays) crt_context_set_counting(ctx, 1);   // per-wave ray counts
+        WaveEngine* e = nullptr;
+        rc = crt_guard(ctx, [&] { e = engine_create(ctx, c.lane_budget_bytes); });
+        if (rc != CRT_OK) return unwind(rc);
+        S->engines.push_back(e);
     }
     for (uint32_t l = 0; l < c.lanes; ++l) S->threads.emplace_back(lane_loop, S, (size_t)l);
     *out = S;
@@ -191,6 +234,7 @@ int crt_server_destroy(crt_server* S) {
     }
     S->cv_work.notify_all();
     for (std::thread& t : S->threads) t.join();
+    for (WaveEngine* e : S->engines) engine_destroy(e);
     for (crt_context* c : S->lanes) crt_context_destroy(c);
     delete S;
     return CRT_OK;

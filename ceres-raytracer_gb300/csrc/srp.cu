@@ -15,8 +15,9 @@
 // Reduction: each persistent warp takes CHUNK tiles (8 x 4 rays each) of one attitude at a time;
 // lanes accumulate force and torque in FP64, the warp reduces them with shuffles, and lane 0 writes
 // the chunk's partial sums to a slot indexed by the chunk, so the per-attitude totals (summed by
-// k_srp_reduce in a fixed order) are bitwise reproducible.  Facet powers use warp-aggregated FP64
-// atomics (reproducible up to the order of additions).
+// k_srp_reduce in a fixed order) are bitwise reproducible.  Facet powers are summed per facet within
+// a warp (FP32, at most 32 terms) and added with FP64 atomics (reproducible up to the order of
+// additions); warps whose rays all missed skip that step.
 #include "common.cuh"
 #include "trace.cuh"
 
@@ -50,13 +51,16 @@ struct SrpArgs {
     uint32_t n_tris;
 };
 
+template <bool COUNT>
 __global__ void __launch_bounds__(CRT_TRACE_BLOCK) k_srp(SceneView sv, SrpArgs A, uint32_t* __restrict__ queue,
-                                                         uint32_t* __restrict__ err) {
+                                                         uint32_t* __restrict__ err,
+                                                         unsigned long long* __restrict__ counters) {
     extern __shared__ uint2 sstack[];
     const int lane = threadIdx.x & 31;
     const uint32_t tiles_x = (A.G + 7) >> 3;
     const uint32_t total = A.n_att * A.grabs_per_att;
     TravStats st{0u, 0u};
+    uint32_t nrays = 0;
     while (true) {
         uint32_t g = 0;
         if (lane == 0) g = atomicAdd(queue, 1u);
@@ -81,7 +85,8 @@ __global__ void __launch_bounds__(CRT_TRACE_BLOCK) k_srp(SceneView sv, SrpArgs A
                 THit h;
                 h.slot = CRT_MISS;
                 if (alive) {
-                    h = traverse<false, false>(sv, r, sstack + threadIdx.x, CRT_TRACE_BLOCK, st, err);
+                    h = traverse<false, COUNT>(sv, r, sstack + threadIdx.x, CRT_TRACE_BLOCK, st, err);
+                    if (COUNT) ++nrays;
                     if (h.slot == CRT_MISS) alive = false;
                 }
                 __syncwarp();
@@ -108,17 +113,20 @@ __global__ void __launch_bounds__(CRT_TRACE_BLOCK) k_srp(SceneView sv, SrpArgs A
                     absorbed = (1.0f - rs - rd) * E;
                     key = __ldg(sv.leaf_prim + h.slot);
                 }
-                if (A.facet) {
-                    // warp-aggregated facet power: lanes hitting the same facet add once
+                if (A.facet && __any_sync(0xffffffffu, hit)) {
+                    // warp-aggregated facet power: lanes hitting the same facet add once.  The group
+                    // sum (at most 32 terms) is FP32, the accumulation across groups FP64 atomics.
                     const uint32_t peers = __match_any_sync(0xffffffffu, key);
-                    double sum = 0.0;
-#pragma unroll 4
-                    for (int j = 0; j < 32; ++j) {
-                        const float v = __shfl_sync(0xffffffffu, absorbed, j);
-                        if ((peers >> j) & 1u) sum += (double)v;
+                    float sum = absorbed;
+                    if (__any_sync(0xffffffffu, hit && peers != (1u << lane))) {
+                        sum = 0.f;
+#pragma unroll 8
+                        for (int j = 0; j < 32; ++j) {
+                            const float v = __shfl_sync(0xffffffffu, absorbed, j);
+                            if ((peers >> j) & 1u) sum += v;
+                        }
                     }
-                    if (key != 0xFFFFFFFFu && lane == __ffs(peers) - 1)
-                        atomicAdd(&A.facet[(size_t)a * A.n_tris + key], sum);
+                    if (hit && lane == __ffs(peers) - 1) atomicAdd(&A.facet[(size_t)a * A.n_tris + key], (double)sum);
                 }
                 if (hit) {
                     if (rs > 0.f && seg < A.nb) {
@@ -144,6 +152,19 @@ __global__ void __launch_bounds__(CRT_TRACE_BLOCK) k_srp(SceneView sv, SrpArgs A
             for (int o = 16; o; o >>= 1) acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], o);
         if (lane == 0)
             for (int k = 0; k < 6; ++k) A.partial[6ull * g + k] = acc[k];
+    }
+    if (COUNT) {
+        unsigned long long a = nrays, b = st.nodes, c = st.tris;
+        for (int o = 16; o; o >>= 1) {
+            a += __shfl_xor_sync(0xffffffffu, a, o);
+            b += __shfl_xor_sync(0xffffffffu, b, o);
+            c += __shfl_xor_sync(0xffffffffu, c, o);
+        }
+        if (lane == 0) {
+            atomicAdd(counters + 0, a);
+            atomicAdd(counters + 1, b);
+            atomicAdd(counters + 2, c);
+        }
     }
 }
 
@@ -249,7 +270,8 @@ void srp_run(crt_context* ctx, crt_scene* s, const crt_srp_desc* desc, const dou
         if (d_facet) CRT_CUDA(cudaMemsetAsync(d_facet, 0, n_att * s->n_tris * 8, st));
         uint32_t* queue = (uint32_t*)ctx_scratch(ctx, SCR_QUEUE, 256);
         const size_t smem = (size_t)CRT_STACK_SMEM * CRT_TRACE_BLOCK * sizeof(uint2);
-        const int grid = occupancy_grid(ctx, (const void*)k_srp, CRT_TRACE_BLOCK, smem);
+        const int grid = occupancy_grid(ctx, ctx->counting ? (const void*)k_srp<true> : (const void*)k_srp<false>,
+                                        CRT_TRACE_BLOCK, smem);
         const SceneView sv = scene_view(s);
         for (size_t a0 = 0; a0 < n_att; a0 += att_per_launch) {
             const size_t na = std::min(att_per_launch, n_att - a0);
@@ -266,7 +288,10 @@ void srp_run(crt_context* ctx, crt_scene* s, const crt_srp_desc* desc, const dou
             A.facet = d_facet ? d_facet + a0 * s->n_tris : nullptr;
             A.n_tris = (uint32_t)s->n_tris;
             CRT_CUDA(cudaMemsetAsync(queue, 0, sizeof(uint32_t), st));
-            k_srp<<<grid, CRT_TRACE_BLOCK, smem, st>>>(sv, A, queue, ctx->d_error);
+            if (ctx->counting)
+                k_srp<true><<<grid, CRT_TRACE_BLOCK, smem, st>>>(sv, A, queue, ctx->d_error, ctx->d_counters);
+            else
+                k_srp<false><<<grid, CRT_TRACE_BLOCK, smem, st>>>(sv, A, queue, ctx->d_error, ctx->d_counters);
             check_launch(ctx, "k_srp");
             k_srp_reduce<<<(uint32_t)na, 256, 0, st>>>(d_partial, gpa, d_force + 3 * a0, d_torque + 3 * a0);
             check_launch(ctx, "k_srp_reduce");
@@ -402,7 +427,8 @@ extern "C" int crt_srp_static(crt_scene* s, const crt_srp_desc* desc, const doub
         double* t_out = host_out ? d_out + 3 * CRT_SRP_STATIC_MAX_ATT : torque;
         const size_t att_per_launch = std::max<size_t>(1, std::min<size_t>(n_att, SS_PART_BYTES / (48ull * gpa)));
         const size_t smem = (size_t)CRT_STACK_SMEM * CRT_TRACE_BLOCK * sizeof(uint2);
-        const int grid = occupancy_grid(ctx, (const void*)k_srp, CRT_TRACE_BLOCK, smem);
+        const int grid = occupancy_grid(ctx, ctx->counting ? (const void*)k_srp<true> : (const void*)k_srp<false>,
+                                        CRT_TRACE_BLOCK, smem);
         const SceneView sv = scene_view(s);
         for (size_t a0 = 0; a0 < n_att; a0 += att_per_launch) {
             const size_t na = std::min(att_per_launch, n_att - a0);
@@ -419,7 +445,10 @@ extern "C" int crt_srp_static(crt_scene* s, const crt_srp_desc* desc, const doub
             A.facet = nullptr;
             A.n_tris = (uint32_t)s->n_tris;
             CRT_CUDA(cudaMemsetAsync(queue, 0, sizeof(uint32_t), st));   // the counter must start at zero
-            k_srp<<<grid, CRT_TRACE_BLOCK, smem, st>>>(sv, A, queue, ctx->d_error);
+            if (ctx->counting)
+                k_srp<true><<<grid, CRT_TRACE_BLOCK, smem, st>>>(sv, A, queue, ctx->d_error, ctx->d_counters);
+            else
+                k_srp<false><<<grid, CRT_TRACE_BLOCK, smem, st>>>(sv, A, queue, ctx->d_error, ctx->d_counters);
             check_launch(ctx, "k_srp");
             k_srp_reduce<<<(uint32_t)na, 256, 0, st>>>(d_partial, gpa, f_out + 3 * a0, t_out + 3 * a0);
             check_launch(ctx, "k_srp_reduce");

@@ -264,16 +264,19 @@ int crt_srp_static(crt_scene* scene, const crt_srp_desc* desc, const double* qua
 
 /* ---------------------------------------------------------------- serving
  * A request loop over resident scenes (no counterpart in the reference, which renders one camera per
- * call): requests are submitted from any thread, queued, admitted FIFO into batches while their
- * estimated device-memory footprint fits a lane's budget, and run as crt_batch on one of `lanes`
- * concurrent lanes (each with its own stream and scratch), so batches formed while others run
- * overlap on the device.  Results equal the same requests run alone (crt_batch guarantee). */
+ * call), with continuous batching: requests are submitted from any thread and queued; each of
+ * `lanes` lanes (own stream, own wave engine) admits them in arrival order while their device state
+ * fits its budget, and runs one wavefront wave at a time over all of its resident requests,
+ * shortest remaining work first.  A request that arrives while others are on the GPU joins the next
+ * wave and leaves when its own last wave is done.  Results equal the same requests run alone. */
 typedef struct crt_server crt_server;
 enum { CRT_REQUEST_SRP = 2 };
 typedef struct {
-    uint32_t lanes;                       /* concurrent batches, >= 1 */
-    size_t lane_budget_bytes;             /* admission budget per batch (device scratch) */
-    uint32_t max_batch;                   /* requests per batch */
+    uint32_t lanes;                       /* concurrent lanes, 1..8 */
+    size_t lane_budget_bytes;             /* device memory per lane: one wave's path buffers + request state */
+    uint32_t max_batch;                   /* resident requests per lane */
+    uint32_t count_rays;                  /* 1: lanes run the counting build (crt_server_stats.rays) */
+    uint32_t wave_paths;                  /* camera paths per wave (0: 4194304; >= 65536) */
 } crt_server_config;
 typedef struct {
     crt_request base;                     /* kind RENDER or LIDAR: as for crt_batch; kind SRP: below */
@@ -284,13 +287,13 @@ typedef struct {
     double* torque;                       /* n_att * 3 */
 } crt_server_request;
 typedef struct {
-    int status;                           /* CRT_OK or the failure of the batch that ran it */
-    double submit_s, start_s, end_s;      /* steady-clock seconds */
-    uint32_t batch_size;                  /* requests in the batch that ran it */
+    int status;                           /* CRT_OK or the failure of the wave that ran it */
+    double submit_s, start_s, end_s;      /* steady-clock seconds: submitted, admitted, completed */
+    uint32_t batch_size;                  /* requests resident in the lane during its last wave */
 } crt_server_result;
 typedef struct {
-    uint64_t submitted, completed, batches, failed;
-    uint64_t rays;                        /* rays traced by completed batches */
+    uint64_t submitted, completed, batches, failed;   /* batches: waves and SRP launches run */
+    uint64_t rays;                        /* rays traced by completed batches (count_rays only) */
     double busy_s;                        /* summed lane time */
 } crt_server_stats;
 

@@ -1,6 +1,8 @@
 """Serving loop (crt_server_*): continuous batching over resident scenes.
 
-* every result equals the same request run alone (bit for bit), whatever batch it landed in;
+* every result equals the same request run alone (bit for bit), whatever waves it shared;
+* requests join running lanes: with small waves and a long render resident, later requests share
+  its waves and finish before it;
 * admission by memory budget: with a budget smaller than any request each request runs alone;
 * malformed requests are refused at submission and the server keeps serving;
 * waits are bounded (CRT_ERR_TIMEOUT), no GPU-side waiting is involved.
@@ -51,7 +53,7 @@ def alone(q):
 
 @pytest.fixture(scope="module")
 def server():
-    srv = lib.Server(0, lanes=2, lane_budget_bytes=64 << 20, max_batch=8)
+    srv = lib.Server(0, lanes=2, lane_budget_bytes=1 << 30, max_batch=8, count_rays=True, wave_paths=1 << 16)
     d = load_golden("cornell")
     cornell = srv.scene(entities_from(d))
     ast = srv.scene([scenes.EntitySpec("a", scenes.asteroid(20_000, seed=6), (0.2, 0.2, 0.2), rho_s=0.2,
@@ -87,6 +89,42 @@ def test_results_same_alone_and_in_the_mix(server):
                 np.testing.assert_array_equal(a, b)
     st = srv.stats()
     assert st["completed"] >= len(reqs) and st["failed"] == 0 and st["rays"] > 0
+
+
+def test_adaptive_and_long_renders_share_waves():
+    srv = lib.Server(0, lanes=1, lane_budget_bytes=1 << 30, max_batch=64, count_rays=True, wave_paths=1 << 16)
+    try:
+        d = load_golden("cornell")
+        cornell = srv.scene(entities_from(d))
+        cam = camera_from(d, "rcam")
+        area = lights_from(d["lights"])
+        # 256 x 240 x 32 spp: one sample (61,440 paths) per wave of 65,536 paths, so 32 waves
+        long_q = dict(kind="render", scene=cornell, camera=dict(cam, resolution=[256, 240]), lights=area,
+                      min_samples=32, max_samples=32, noise_threshold=0.0, num_bounces=2, seed=5, request=1,
+                      radiance=True)
+        short = [dict(kind="render", scene=cornell, camera=dict(cam, resolution=[20, 16]), lights=area, min_samples=4,
+                      max_samples=4, noise_threshold=0.0, num_bounces=2, seed=6, request=20 + r, radiance=True)
+                 for r in range(2)]
+        short.append(dict(kind="lidar", scene=cornell, position=[0.5, 0.5, 2.4], rotation=np.eye(3), nx=9, ny=7,
+                          half_x=0.1, half_y=0.1))
+        adaptive = [dict(kind="render", scene=cornell, camera=dict(cam, resolution=[20, 16]), lights=area,
+                         min_samples=2, max_samples=24, noise_threshold=1.5, num_bounces=2, seed=7, request=10 + r,
+                         radiance=True) for r in range(3)]
+        reqs = [long_q] + short + adaptive
+        expected = [alone(q) for q in reqs]
+        tickets = [srv.submit(q) for q in reqs]
+        results = [srv.wait(t, timeout=120.0) for t in tickets]
+        for (res, out), e in zip(results, expected):
+            assert res["status"] == 0
+            for a, b in zip(out, e):
+                if b is not None:
+                    np.testing.assert_array_equal(a, b)
+        # the short requests joined the long render's waves and left before it
+        end_long = results[0][0]["end_s"]
+        assert all(res["end_s"] < end_long for res, _ in results[1:1 + len(short)])
+        assert all(res["batch_size"] > 1 for res, _ in results[1:1 + len(short)])
+    finally:
+        srv.close()
 
 
 def test_admission_budget_runs_large_requests_alone():
