@@ -58,7 +58,10 @@ def parse():
     ap.add_argument("--no-srp", action="store_true")
     ap.add_argument("--srp-attitudes", type=int, default=256)
     ap.add_argument("--probe", type=int, default=0,
-                    help="profiling aid: only launch the primary-ray closest-hit kernel this many times")
+                    help="profiling aid: only run the --probe-kind workload this many times")
+    ap.add_argument("--probe-kind", default="closest", choices=["closest", "batched", "srp"],
+                    help="closest: crt_trace_closest on the 2048^2 primary rays; batched: one crt_batch of the "
+                         "64-request mix; srp: 8 attitudes x 4096^2 rays x 2 bounces with per-facet flux")
     return ap.parse_args()
 
 
@@ -71,7 +74,31 @@ def probe(args):
     ents = workloads.asteroid_entities(args.faces)
     cfg = workloads.asteroid_config(args.res, args.lidar)
     ctx = lib.Context(0)
+    if args.probe_kind == "srp":
+        s = workloads.srp_config(n_att=8)
+        scs = ctx.scene(s["entities"])
+        for _ in range(args.probe):
+            f, t, fp = scs.srp(s["sun"], s["quaternions"], s["grid"], num_bounces=s["num_bounces"], facet_power=True)
+        print(json.dumps({"probe_launches": args.probe, "kind": "srp", "force0": f[0].tolist()}))
+        scs.close()
+        ctx.close()
+        return
     sc = ctx.scene(ents)
+    if args.probe_kind == "batched":
+        reqs = []
+        for q in workloads.batched_config(seed=1):
+            if q["kind"] == "render":
+                reqs.append(dict(kind="render", scene=sc, camera=q["camera"], lights=q["lights"],
+                                 min_samples=q["spp"], max_samples=q["spp"], noise_threshold=0.0,
+                                 num_bounces=q["bounces"], seed=1, request=q["request"]))
+            else:
+                reqs.append(dict(kind="lidar", scene=sc, position=q["position"], rotation=q["rotation"], nx=q["nx"],
+                                 ny=q["ny"], half_x=q["half_x"], half_y=q["half_y"]))
+        for _ in range(args.probe):
+            _, st = ctx.batch(reqs)
+        print(json.dumps({"probe_launches": args.probe, "kind": "batched", "waves": st["waves"]}))
+        ctx.close()
+        return
     rays = torch.from_numpy(scenes_camera_rays(cfg["camera"])).cuda()
     hits = torch.empty((rays.shape[0], 4), dtype=torch.float32, device="cuda")
     for _ in range(args.probe):

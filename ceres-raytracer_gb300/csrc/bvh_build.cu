@@ -12,8 +12,9 @@
 //                    BVHs, octrees, and k-d trees", HPG 2012); ties broken by index
 //   k_refit          bottom-up boxes, second arrival at each node does the union
 //   k_collapse       top-down, level-synchronous collapse into 8-wide nodes: greedily open the
-//                    largest-area child until 8 slots are used, children with <= 3 triangles
-//                    become leaves, slots ordered by octant, child boxes quantised to 8 bits
+//                    largest-area child of more than 3 triangles until 8 slots are used (then
+//                    split small leaves into free slots), children with <= 3 triangles become
+//                    leaves, slots ordered by octant, child boxes quantised to 8 bits
 //                    (Ylitie, Karras, Laine, "Efficient incoherent ray traversal on GPUs through
 //                    compressed wide BVHs", HPG 2017); leaf triangles written contiguously.
 #include "common.cuh"
@@ -422,16 +423,24 @@ __global__ void k_collapse(CollapseArgs A, const int2* __restrict__ frontier, ui
         refs[0] = c.x;
         refs[1] = c.y;
         nc = 2;
+        // open the largest-area child that would otherwise become an internal node (> 3 triangles);
+        // only when none is left, split small leaves to fill the remaining slots
         while (nc < 8) {
             int best = -1;
+            bool best_big = false;
             float best_area = -1.f;
             for (int k = 0; k < nc; ++k) {
                 if (refs[k] < 0) continue;     // leaf of the binary tree: cannot open
+                const bool big = ref_count(A, refs[k]) > 3;
                 const size_t bi = box_index(n, refs[k]);
                 const float4 lo = A.nbox[2 * bi], hi = A.nbox[2 * bi + 1];
                 const float dx = hi.x - lo.x, dy = hi.y - lo.y, dz = hi.z - lo.z;
                 const float area = dx * dy + dy * dz + dz * dx;
-                if (area > best_area) { best_area = area; best = k; }
+                if ((big && !best_big) || (big == best_big && area > best_area)) {
+                    best_area = area;
+                    best = k;
+                    best_big = big;
+                }
             }
             if (best < 0) break;
             const int2 c2 = A.child[refs[best]];

@@ -1046,8 +1046,28 @@ struct WaveEngine {
     };
     std::vector<char> up_data;
     std::vector<Up> ups;
-    char* pinned = nullptr;
-    size_t pinned_bytes = 0;
+    char* pinned[2] = {nullptr, nullptr};   // upload buffers, alternating between consecutive waves
+    size_t pinned_bytes[2] = {0, 0};
+    int parity = 0;
+    // completion of the wave in flight: host outputs land in pinned staging (hout) by async copies
+    // and reach the caller's memory when the wave's event has completed
+    struct OutCopy {
+        void* dst;
+        size_t off, n;
+    };
+    struct Flight {
+        bool active = false;
+        cudaEvent_t ev = nullptr;
+        int err_slot = 0;
+        std::vector<uint64_t> tags;
+        std::vector<OutCopy> copies;
+    };
+    Flight flights[2];
+    int cur_flight = 0;
+    char* hout = nullptr;                    // pinned host staging of outputs
+    Ranges hout_r;
+    uint32_t* err_pin = nullptr;             // pinned copies of the device error word, one per flight
+    std::vector<uint64_t> failed;            // tags of a wave whose device check failed
     // fixed device tables
     RReq* d_rr = nullptr;
     LightDev* d_lights = nullptr;
@@ -1096,22 +1116,90 @@ void engine_upload(WaveEngine* e, void* dst, const void* src, size_t n) {
     e->ups.push_back({dst, off, n});
 }
 
+// Copies the queued uploads through this wave's pinned buffer.  The buffer was last used two waves
+// ago, and that wave has been drained (its event completed) before this one is planned.
 void engine_flush_uploads(WaveEngine* e) {
     if (e->ups.empty()) return;
     const size_t need = e->up_data.size();
-    if (e->pinned_bytes < need) {   // no copy from the pinned buffer is in flight between steps
-        if (e->pinned) CRT_CUDA(cudaFreeHost(e->pinned));
-        e->pinned = nullptr;
-        e->pinned_bytes = 0;
+    const int b = e->parity;
+    if (e->pinned_bytes[b] < need) {
+        CRT_CUDA(cudaStreamSynchronize(e->ctx->stream));
+        if (e->pinned[b]) CRT_CUDA(cudaFreeHost(e->pinned[b]));
+        e->pinned[b] = nullptr;
+        e->pinned_bytes[b] = 0;
         const size_t cap = (need + need / 2 + 4095) & ~size_t(4095);
-        CRT_CUDA(cudaMallocHost(&e->pinned, cap));
-        e->pinned_bytes = cap;
+        CRT_CUDA(cudaMallocHost(&e->pinned[b], cap));
+        e->pinned_bytes[b] = cap;
     }
-    std::memcpy(e->pinned, e->up_data.data(), need);
+    std::memcpy(e->pinned[b], e->up_data.data(), need);
     for (const WaveEngine::Up& u : e->ups)
-        CRT_CUDA(cudaMemcpyAsync(u.dst, e->pinned + u.off, u.n, cudaMemcpyHostToDevice, e->ctx->stream));
+        CRT_CUDA(cudaMemcpyAsync(u.dst, e->pinned[b] + u.off, u.n, cudaMemcpyHostToDevice, e->ctx->stream));
     e->ups.clear();
     e->up_data.clear();
+}
+
+// Completes a wave in flight: waits for its event, checks its copy of the device error word, copies
+// the staged host outputs to the callers' buffers and reports the finished requests.
+// Host copies of a flight's staged outputs (its copies into the staging must have completed).
+void engine_flush_copies(WaveEngine* e, WaveEngine::Flight& f) {
+    for (const WaveEngine::OutCopy& c : f.copies) {
+        std::memcpy(c.dst, e->hout + c.off, c.n);
+        e->hout_r.release(c.off, up256(c.n));
+    }
+    f.copies.clear();
+}
+
+void engine_drain_flight(WaveEngine* e, WaveEngine::Flight& f, std::vector<uint64_t>& completed) {
+    if (!f.active) return;
+    f.active = false;
+    CRT_CUDA(cudaEventSynchronize(f.ev));
+    const uint32_t h = e->err_pin[f.err_slot];
+    e->err_pin[f.err_slot] = 0;
+    engine_flush_copies(e, f);
+    std::vector<uint64_t> tags;
+    tags.swap(f.tags);
+    if (h) {
+        e->failed.insert(e->failed.end(), tags.begin(), tags.end());
+        std::string m = "serving wave: device check failed (";
+        if (h & DEVERR_STACK_OVERFLOW) m += " traversal-stack-overflow";
+        if (h & DEVERR_BAD_INDEX) m += " bad-index";
+        m += " )";
+        throw CrtError{CRT_ERR_DEVICE, m};
+    }
+    completed.insert(completed.end(), tags.begin(), tags.end());
+}
+
+void engine_drain_all(WaveEngine* e, std::vector<uint64_t>& completed) {
+    // the older flight first
+    WaveEngine::Flight& older = e->flights[e->cur_flight ^ 1];
+    WaveEngine::Flight& newer = e->flights[e->cur_flight];
+    engine_drain_flight(e, older, completed);
+    engine_drain_flight(e, newer, completed);
+}
+
+// Stages a device output for the caller's host buffer: async copy into pinned staging now, host copy
+// when the wave completes.  When the staging is full, the stream is synchronised and this flight's
+// copies are done early; a single output larger than the staging grows it.
+void engine_stage_out(WaveEngine* e, WaveEngine::Flight& f, void* dst, const void* src, size_t n) {
+    if (!dst || !n) return;
+    size_t off = 0;
+    if (!e->hout_r.alloc(up256(n), off)) {
+        // every copy issued so far has completed after the synchronise: move both flights' staged
+        // outputs to their callers now (the flights still report their requests when drained)
+        CRT_CUDA(cudaStreamSynchronize(e->ctx->stream));
+        for (WaveEngine::Flight& g : e->flights) engine_flush_copies(e, g);
+        if (!e->hout_r.alloc(up256(n), off)) {
+            // nothing is staged in the buffer any more
+            CRT_CUDA(cudaFreeHost(e->hout));
+            e->hout = nullptr;
+            const size_t cap = up256(n + n / 2);
+            CRT_CUDA(cudaMallocHost(&e->hout, cap));
+            e->hout_r.reset(cap);
+            e->hout_r.alloc(up256(n), off);
+        }
+    }
+    CRT_CUDA(cudaMemcpyAsync(e->hout + off, src, n, cudaMemcpyDeviceToHost, e->ctx->stream));
+    f.copies.push_back({dst, off, n});
 }
 
 void engine_release(WaveEngine* e, EReq& r) {
@@ -1146,6 +1234,12 @@ WaveEngine* engine_create(crt_context* ctx, size_t budget_bytes) {
         take(256);
         e->d_acount = (uint32_t*)take(4 * ENGINE_SLOTS);
         for (uint32_t s = ENGINE_SLOTS; s > 0; --s) e->free_slots.push_back(s - 1);
+        CRT_CUDA(cudaMallocHost(&e->err_pin, 2 * sizeof(uint32_t)));
+        e->err_pin[0] = e->err_pin[1] = 0;
+        for (WaveEngine::Flight& f : e->flights) CRT_CUDA(cudaEventCreateWithFlags(&f.ev, cudaEventDisableTiming));
+        const size_t hcap = std::min<size_t>(std::max<size_t>(budget_bytes / 8, 16u << 20), 512u << 20);
+        CRT_CUDA(cudaMallocHost(&e->hout, hcap));
+        e->hout_r.reset(hcap);
         // budget: path buffers for one wave, then pixel state and staging (2 : 3)
         e->want_P = std::max<uint32_t>(ctx->wave_paths, 1u << 16);
         // (a request larger than what is left runs alone, its arena growing to fit it)
@@ -1168,11 +1262,18 @@ void engine_destroy(WaveEngine* e) {
     cudaFree(e->units_mem);
     cudaFree(e->bytes_mem);
     cudaFree(e->fixed);
-    if (e->pinned) cudaFreeHost(e->pinned);
+    for (char* p : e->pinned)
+        if (p) cudaFreeHost(p);
+    if (e->hout) cudaFreeHost(e->hout);
+    if (e->err_pin) cudaFreeHost(e->err_pin);
+    for (WaveEngine::Flight& f : e->flights)
+        if (f.ev) cudaEventDestroy(f.ev);
     delete e;
 }
 
-size_t engine_resident(const WaveEngine* e) { return e->res.size(); }
+size_t engine_resident(const WaveEngine* e) {
+    return e->res.size() + e->flights[0].tags.size() + e->flights[1].tags.size();
+}
 
 // Admits a request when its state fits the free arenas now (false: retry after requests finish).
 // A request larger than an arena is admitted alone, the arena growing to fit it.
@@ -1205,6 +1306,8 @@ bool engine_admit(WaveEngine* e, const crt_request& q, uint64_t tag) {
         r.units = r.npix;
         r.bytes = b_rgba + b_rad + b_act;
         const bool alone = e->res.empty();
+        if (alone && (r.units > e->units.cap() || r.bytes > e->bytes.cap()))
+            CRT_CUDA(cudaStreamSynchronize(st));   // a completed wave's copies may still be in flight
         if (r.units > e->units.cap() && alone) engine_alloc_units(e, r.units + r.units / 4);
         if (r.bytes > e->bytes.cap() && alone) engine_alloc_bytes(e, r.bytes + r.bytes / 4);
         if (!e->units.alloc(r.units, r.unit_off)) return false;
@@ -1262,7 +1365,10 @@ bool engine_admit(WaveEngine* e, const crt_request& q, uint64_t tag) {
         const size_t b_range = host_range ? up256(n * 8) : 0;
         const size_t b_prim = host_prim ? up256(n * 4) : 0;
         r.bytes = b_tan + b_range + b_prim;
-        if (r.bytes > e->bytes.cap() && e->res.empty()) engine_alloc_bytes(e, r.bytes + r.bytes / 4);
+        if (r.bytes > e->bytes.cap() && e->res.empty()) {
+            CRT_CUDA(cudaStreamSynchronize(st));
+            engine_alloc_bytes(e, r.bytes + r.bytes / 4);
+        }
         if (!e->bytes.alloc(r.bytes, r.byte_off)) return false;
         char* b = e->bytes_mem + r.byte_off;
         r.tan = (double*)b;
@@ -1279,27 +1385,49 @@ bool engine_admit(WaveEngine* e, const crt_request& q, uint64_t tag) {
     return true;
 }
 
-// Drops every resident request (after a failed step); returns their tags.
+// Drops every resident request and the waves in flight (after a failed step); returns their tags.
 void engine_abort(WaveEngine* e, std::vector<uint64_t>& dropped) {
     cudaStreamSynchronize(e->ctx->stream);
+    cudaGetLastError();
     for (EReq& r : e->res) {
         engine_release(e, r);
         dropped.push_back(r.tag);
     }
     e->res.clear();
+    for (WaveEngine::Flight& f : e->flights) {
+        for (const WaveEngine::OutCopy& c : f.copies) e->hout_r.release(c.off, up256(c.n));
+        f.copies.clear();
+        dropped.insert(dropped.end(), f.tags.begin(), f.tags.end());
+        f.tags.clear();
+        f.active = false;
+    }
+    dropped.insert(dropped.end(), e->failed.begin(), e->failed.end());
+    e->failed.clear();
+    e->err_pin[0] = e->err_pin[1] = 0;
+    cudaMemsetAsync(e->ctx->d_error, 0, sizeof(uint32_t), e->ctx->stream);
     e->ups.clear();
     e->up_data.clear();
 }
 
-// Runs one wave over the resident requests and appends the tags of the requests it completed.
+// Runs one wave over the resident requests.  The wave is launched, then the previous wave (which ran
+// while this one was planned) is completed, so the GPU does not wait for the host between waves;
+// the tags of the requests completed by that earlier wave (and by this one, when nothing is left to
+// run) are appended to `completed`.
 void engine_step(WaveEngine* e, std::vector<uint64_t>& completed) {
     crt_context* ctx = e->ctx;
     cudaStream_t st = ctx->stream;
     CRT_CUDA(cudaSetDevice(ctx->device));
-    if (e->res.empty()) return;
-    // path buffers (wave-local state only, so they can be resized between waves)
+    if (e->res.empty()) {
+        engine_drain_all(e, completed);
+        return;
+    }
+    const int slot = e->cur_flight ^ 1;   // flight slot and upload buffer of the wave two steps back
+    WaveEngine::Flight& f = e->flights[slot];
+    engine_drain_flight(e, f, completed);   // normally drained already at the end of the last step
+    e->parity = slot;
+    // path buffers (wave-local state only; resizing waits for the wave in flight)
     if (e->want_P > e->P || e->want_NL > e->NL) {
-        CRT_CUDA(cudaStreamSynchronize(st));
+        engine_drain_all(e, completed);
         if (e->paths) CRT_CUDA(cudaFree(e->paths));
         e->paths = nullptr;
         e->P = e->NL = 0;
@@ -1347,12 +1475,14 @@ void engine_step(WaveEngine* e, std::vector<uint64_t>& completed) {
     for (EReq& r : e->res)
         if (!r.lidar && r.next_sample >= r.total && (!r.adaptive || r.next_sample >= r.upto)) r.finished = true;
 
-    // adaptive requests past their fixed prefix: compact the still-active pixels
+    // adaptive requests past their fixed prefix: compact the still-active pixels (reads counts back,
+    // so the wave in flight is completed first)
     std::vector<EReq*> compacting;
     for (EReq& r : e->res)
         if (!r.lidar && r.adaptive && r.next_sample >= r.upto && r.next_sample < r.total && r.n_active > 0)
             compacting.push_back(&r);
     if (!compacting.empty()) {
+        engine_drain_all(e, completed);
         CRT_CUDA(cudaMemsetAsync(e->d_acount, 0, 4 * compacting.size(), st));
         for (size_t k = 0; k < compacting.size(); ++k) {
             EReq& r = *compacting[k];
@@ -1454,7 +1584,7 @@ void engine_step(WaveEngine* e, std::vector<uint64_t>& completed) {
     w.n_primary = w.n_lidar_items + w.n_paths;
 
     // run it
-    // one flush per step: the pinned buffer is reused only after the step's closing synchronise
+    // launch
     const bool any_work = w.n_primary > 0;
     if (any_work) {
         if (lreqs.size()) engine_upload(e, e->d_lr, lreqs.data(), sizeof(LReq) * lreqs.size());
@@ -1465,34 +1595,45 @@ void engine_step(WaveEngine* e, std::vector<uint64_t>& completed) {
         CRT_CUDA(cudaMemsetAsync(e->d_wave_idx, 0, 4, st));
         launch_wave_kernels(ctx, B, P, NL, lidar_items, max_bounces, qa, qb, e->d_tqueue);
     }
-    // completions: finalize renders, copy host outputs
-    std::vector<EReq*> done_now;
+    // completions of this wave: finalize, stage host outputs, release device state (later work on
+    // the stream reuses it only after these copies)
     for (EReq* r : wave_lidar) {
         const crt_lidar_grid_desc& g = *r->q.lidar;
         const size_t n = (size_t)g.nx * g.ny;
-        out_finish(ctx, r->q.range, r->range, n * 8);
-        if (r->q.prim) out_finish(ctx, r->q.prim, r->prim, n * 4);
+        if ((void*)r->range != (void*)r->q.range) engine_stage_out(e, f, r->q.range, r->range, n * 8);
+        if (r->q.prim && (void*)r->prim != (void*)r->q.prim) engine_stage_out(e, f, r->q.prim, r->prim, n * 4);
         r->finished = true;
     }
     for (EReq& r : e->res) {
         if (r.lidar || !r.finished) continue;
         k_finalize_one<<<grid_for(ctx, r.npix), 256, 0, st>>>(B, r.slot);
         check_launch(ctx, "k_finalize_one");
-        if (r.q.rgba8) out_finish(ctx, r.q.rgba8, r.rgba, (size_t)r.npix * 4);
-        if (r.q.radiance) out_finish(ctx, r.q.radiance, r.rad, (size_t)r.npix * 16);
+        if (r.q.rgba8 && (void*)r.rgba != (void*)r.q.rgba8)
+            engine_stage_out(e, f, r.q.rgba8, r.rgba, (size_t)r.npix * 4);
+        if (r.q.radiance && (void*)r.rad != (void*)r.q.radiance)
+            engine_stage_out(e, f, r.q.radiance, r.rad, (size_t)r.npix * 16);
     }
-    check_device_error(ctx, "serving wave");   // synchronises the stream
+    CRT_CUDA(cudaMemcpyAsync(e->err_pin + slot, ctx->d_error, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    CRT_CUDA(cudaMemsetAsync(ctx->d_error, 0, sizeof(uint32_t), st));
+    CRT_CUDA(cudaEventRecord(f.ev, st));
+    f.active = true;
+    f.err_slot = slot;
     std::vector<EReq> keep;
     keep.reserve(e->res.size());
     for (EReq& r : e->res) {
         if (r.finished) {
             engine_release(e, r);
-            completed.push_back(r.tag);
+            f.tags.push_back(r.tag);
         } else {
             keep.push_back(r);
         }
     }
     e->res.swap(keep);
+    e->cur_flight = slot;
+    // the previous wave ran while this one was planned: complete it now
+    engine_drain_flight(e, e->flights[slot ^ 1], completed);
+    // nothing left to run: complete this wave too
+    if (e->res.empty()) engine_drain_flight(e, f, completed);
 }
 
 namespace {

@@ -139,20 +139,20 @@ void lane_loop(crt_server* S, size_t lane) {
         const double t0 = now_s();
         const size_t sharing = resident.size();
         finished.clear();
-        int rc = crt_guard(ctx, [&] { engine_step(E, finished); });
-        if (rc != CRT_OK) {
-            finished.clear();
-            engine_abort(E, finished);
-        }
+        std::vector<uint64_t> dropped;
+        const int rc = crt_guard(ctx, [&] { engine_step(E, finished); });
+        if (rc != CRT_OK) engine_abort(E, dropped);
         const double t1 = now_s();
         if (S->cfg.count_rays) crt_context_get_counters(ctx, &c1);
         {
             std::lock_guard<std::mutex> lk(S->mu);
-            for (uint64_t tag : finished) {
-                auto it = resident.find(tag);
-                if (it == resident.end()) continue;
-                publish(S, it->second.first, rc, it->second.second, t1, (uint32_t)sharing);
-                resident.erase(it);
+            for (int pass = 0; pass < 2; ++pass) {
+                for (uint64_t tag : pass ? dropped : finished) {
+                    auto it = resident.find(tag);
+                    if (it == resident.end()) continue;
+                    publish(S, it->second.first, pass ? rc : CRT_OK, it->second.second, t1, (uint32_t)sharing);
+                    resident.erase(it);
+                }
             }
             S->stats.batches++;
             S->stats.busy_s += t1 - t0;

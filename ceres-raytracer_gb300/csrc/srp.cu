@@ -12,7 +12,8 @@
 // start on a grid x grid square of side 2 R_b (R_b = half diagonal of the scene box) centred on the
 // box centre, 2 R_b + 1 upstream, one ray per cell centre, power flux * cell area.
 //
-// Reduction: each persistent warp takes CHUNK tiles (8 x 4 rays each) of one attitude at a time;
+// Reduction: each persistent warp takes `chunk` tiles (8 x 4 rays each) of one attitude at a time
+// (16, fewer for small grids so that the grabs outnumber the resident warps four to one);
 // lanes accumulate force and torque in FP64, the warp reduces them with shuffles, and lane 0 writes
 // the chunk's partial sums to a slot indexed by the chunk, so the per-attitude totals (summed by
 // k_srp_reduce in a fixed order) are bitwise reproducible.  Facet powers are summed per facet within
@@ -26,7 +27,7 @@
 
 namespace {
 
-constexpr uint32_t CHUNK = 16;   // tiles per work grab
+constexpr uint32_t CHUNK = 16;   // tiles per work grab (at most)
 
 struct SrpAtt {
     float org[3];   // centre of cell (0, 0)
@@ -42,6 +43,7 @@ struct SrpArgs {
     uint32_t G;
     uint32_t tiles;          // tiles per attitude
     uint32_t grabs_per_att;
+    uint32_t chunk;          // tiles per grab
     uint32_t n_att;
     float inv_c;
     float cm[3];
@@ -67,8 +69,8 @@ __global__ void __launch_bounds__(CRT_TRACE_BLOCK) k_srp(SceneView sv, SrpArgs A
         g = __shfl_sync(0xffffffffu, g, 0);
         if (g >= total) break;
         const uint32_t a = g / A.grabs_per_att;
-        const uint32_t t0 = (g % A.grabs_per_att) * CHUNK;
-        const uint32_t t1 = min(t0 + CHUNK, A.tiles);
+        const uint32_t t0 = (g % A.grabs_per_att) * A.chunk;
+        const uint32_t t1 = min(t0 + A.chunk, A.tiles);
         const SrpAtt P = A.att[a];
         double acc[6] = {0, 0, 0, 0, 0, 0};
         for (uint32_t tile = t0; tile < t1; ++tile) {
@@ -258,7 +260,14 @@ void srp_run(crt_context* ctx, crt_scene* s, const crt_srp_desc* desc, const dou
             att[a].pad = 0.f;
         }
         const uint32_t tiles = ((G + 7) / 8) * ((G + 3) / 4);
-        const uint32_t gpa = (tiles + CHUNK - 1) / CHUNK;
+        const size_t smem = (size_t)CRT_STACK_SMEM * CRT_TRACE_BLOCK * sizeof(uint2);
+        const int grid = occupancy_grid(ctx, ctx->counting ? (const void*)k_srp<true> : (const void*)k_srp<false>,
+                                        CRT_TRACE_BLOCK, smem);
+        // tiles per grab: up to CHUNK, fewer when the grabs would not outnumber the resident warps 4:1
+        const size_t warps = (size_t)grid * (CRT_TRACE_BLOCK / 32);
+        const uint32_t chunk =
+            (uint32_t)std::max<size_t>(1, std::min<size_t>(CHUNK, (size_t)tiles * n_att / (4 * warps)));
+        const uint32_t gpa = (tiles + chunk - 1) / chunk;
         // keep each launch's grab count well inside 32 bits
         const size_t att_per_launch = std::max<size_t>(1, std::min<size_t>(n_att, (1u << 30) / gpa));
         SrpAtt* d_att = (SrpAtt*)ctx_scratch(ctx, SCR_IN1, sizeof(SrpAtt) * n_att);
@@ -269,9 +278,6 @@ void srp_run(crt_context* ctx, crt_scene* s, const crt_srp_desc* desc, const dou
         double* d_facet = facet_power ? (double*)out_device(ctx, facet_power, n_att * s->n_tris * 8, SCR_OUT2) : nullptr;
         if (d_facet) CRT_CUDA(cudaMemsetAsync(d_facet, 0, n_att * s->n_tris * 8, st));
         uint32_t* queue = (uint32_t*)ctx_scratch(ctx, SCR_QUEUE, 256);
-        const size_t smem = (size_t)CRT_STACK_SMEM * CRT_TRACE_BLOCK * sizeof(uint2);
-        const int grid = occupancy_grid(ctx, ctx->counting ? (const void*)k_srp<true> : (const void*)k_srp<false>,
-                                        CRT_TRACE_BLOCK, smem);
         const SceneView sv = scene_view(s);
         for (size_t a0 = 0; a0 < n_att; a0 += att_per_launch) {
             const size_t na = std::min(att_per_launch, n_att - a0);
@@ -280,6 +286,7 @@ void srp_run(crt_context* ctx, crt_scene* s, const crt_srp_desc* desc, const dou
             A.G = G;
             A.tiles = tiles;
             A.grabs_per_att = gpa;
+            A.chunk = chunk;
             A.n_att = (uint32_t)na;
             A.inv_c = (float)(1.0 / desc->c);
             for (int k = 0; k < 3; ++k) A.cm[k] = (float)desc->center_of_mass[k];
@@ -437,6 +444,7 @@ extern "C" int crt_srp_static(crt_scene* s, const crt_srp_desc* desc, const doub
             A.G = G;
             A.tiles = tiles;
             A.grabs_per_att = gpa;
+            A.chunk = CHUNK;
             A.n_att = (uint32_t)na;
             A.inv_c = (float)(1.0 / desc->c);
             for (int k = 0; k < 3; ++k) A.cm[k] = (float)desc->center_of_mass[k];
