@@ -29,10 +29,13 @@ struct TravStats {
     uint32_t nodes, tris;
 };
 
-// byte k of w as an exact float in [0, 255]
-__device__ __forceinline__ float byte_f(uint32_t w, int k) {
-    const uint32_t sel = (uint32_t)k | 0x7540u;           // bytes {w_k, 0x00, 0x00, 0x4B}
-    return __uint_as_float(__byte_perm(w, 0x4B000000u, sel)) - 8388608.0f;
+// 32768 + (byte k of w) as an exact float: the byte lands in bits 8..15 of the mantissa of 2^15
+// (result bytes {0x00, w_k, 0x00, 0x47}).  Plane distances are then fma(32768 + b, s, a - 32768 s):
+// one PRMT and one FFMA per plane, with the node-constant offset folded into a - 32768 s.  Its
+// rounding adds at most 2^-24 (|a| + 2^15 |s|), i.e. the size of the existing rounding of a plus
+// 0.002 quantum, well inside the build's one-quantum slack on every child box.
+__device__ __forceinline__ float byte_f15(uint32_t w, int k) {
+    return __uint_as_float(__byte_perm(w, 0x47000000u, 0x7404u | ((uint32_t)k << 4)));
 }
 
 template <bool ANY, bool COUNT>
@@ -99,9 +102,9 @@ __device__ __forceinline__ THit traverse(const SceneView& sv, TRay ray, uint2* _
         const float sx = __uint_as_float((uint32_t)(((int)(int8_t)(ew & 0xFF) + 127) << 23)) * idir.x;
         const float sy = __uint_as_float((uint32_t)(((int)(int8_t)((ew >> 8) & 0xFF) + 127) << 23)) * idir.y;
         const float sz = __uint_as_float((uint32_t)(((int)(int8_t)((ew >> 16) & 0xFF) + 127) << 23)) * idir.z;
-        const float ax = (w0.x - ray.o.x) * idir.x;
-        const float ay = (w0.y - ray.o.y) * idir.y;
-        const float az = (w0.z - ray.o.z) * idir.z;
+        const float ax = fmaf(-32768.0f, sx, (w0.x - ray.o.x) * idir.x);
+        const float ay = fmaf(-32768.0f, sy, (w0.y - ray.o.y) * idir.y);
+        const float az = fmaf(-32768.0f, sz, (w0.z - ray.o.z) * idir.z);
         const uint32_t imask = ew >> 24;
         // entry / exit planes per axis depend on the ray octant
         uint32_t xlo0 = __float_as_uint(w2.x), xlo1 = __float_as_uint(w2.y);
@@ -121,9 +124,9 @@ __device__ __forceinline__ THit traverse(const SceneView& sv, TRay ray, uint2* _
             const uint32_t xl = c < 4 ? xlo0 : xlo1, xh = c < 4 ? xhi0 : xhi1;
             const uint32_t yl = c < 4 ? ylo0 : ylo1, yh = c < 4 ? yhi0 : yhi1;
             const uint32_t zl = c < 4 ? zlo0 : zlo1, zh = c < 4 ? zhi0 : zhi1;
-            const float tx0 = fmaf(byte_f(xl, k), sx, ax), tx1 = fmaf(byte_f(xh, k), sx, ax);
-            const float ty0 = fmaf(byte_f(yl, k), sy, ay), ty1 = fmaf(byte_f(yh, k), sy, ay);
-            const float tz0 = fmaf(byte_f(zl, k), sz, az), tz1 = fmaf(byte_f(zh, k), sz, az);
+            const float tx0 = fmaf(byte_f15(xl, k), sx, ax), tx1 = fmaf(byte_f15(xh, k), sx, ax);
+            const float ty0 = fmaf(byte_f15(yl, k), sy, ay), ty1 = fmaf(byte_f15(yh, k), sy, ay);
+            const float tz0 = fmaf(byte_f15(zl, k), sz, az), tz1 = fmaf(byte_f15(zh, k), sz, az);
             const float tmin = fmaxf(fmaxf(tx0, ty0), fmaxf(tz0, ray.tmin));
             const float tmax = fminf(fminf(tx1, ty1), fminf(tz1, ray.tmax));
             if (tmin <= tmax) {
