@@ -53,7 +53,8 @@ def parse():
     ap.add_argument("--served-seconds", type=float, default=10.0,
                     help="length of the Poisson request stream (the configuration states 60 s)")
     ap.add_argument("--served-rate", type=float, default=200.0)
-    ap.add_argument("--served-lanes", type=int, default=2)
+    ap.add_argument("--served-lanes", type=int, default=4)
+    ap.add_argument("--served-wave-paths", type=int, default=1 << 22)
     ap.add_argument("--served-budget-mib", type=int, default=4096)
     ap.add_argument("--no-srp", action="store_true")
     ap.add_argument("--srp-attitudes", type=int, default=256)
@@ -531,7 +532,8 @@ def served_measure(args, device):
     import threading
     from crt_gb300 import lib, workloads
     stream = workloads.served_stream(args.served_rate, args.served_seconds)
-    srv = lib.Server(device, lanes=args.served_lanes, lane_budget_bytes=args.served_budget_mib << 20, max_batch=256)
+    srv = lib.Server(device, lanes=args.served_lanes, lane_budget_bytes=args.served_budget_mib << 20, max_batch=256,
+                     wave_paths=args.served_wave_paths)
     t0 = time.perf_counter()
     ents = workloads.served_bodies()
     t_gen = time.perf_counter() - t0
@@ -627,6 +629,7 @@ def served_measure(args, device):
                        % (args.served_rate, args.served_seconds, len(items)),
            "rays": rays, "offered_mrays_s": round(rays / args.served_seconds / 1e6, 1),
            "lanes": args.served_lanes, "lane_budget_mib": args.served_budget_mib,
+           "wave_paths": args.served_wave_paths,
            "open_loop": {"served": dict(summary(lat_s, span_s), waves=nb_s, clocks=clk_s),
                          "per_call": dict(summary(lat_p, span_p), clocks=clk_p)},
            "closed_loop": {"served": dict(summary(clat_s, cspan_s), waves=cnb_s, clocks=cclk_s),

@@ -256,7 +256,7 @@ int crt_server_submit(crt_server* S, const crt_server_request* r, uint64_t* tick
         if (q.kind == CRT_REQUEST_SRP) {
             CRT_CHECK(r->srp && r->quaternions && r->force && r->torque, CRT_ERR_INVALID, "incomplete SRP request");
             CRT_CHECK(r->n_att > 0 && r->n_att <= (1u << 20), CRT_ERR_INVALID, "bad attitude count");
-            CRT_CHECK(r->srp->grid > 0 && r->srp->grid <= 65536, CRT_ERR_INVALID, "grid must be in [1, 65536]");
+            CRT_CHECK(r->srp->grid > 0 && r->srp->grid <= 32768, CRT_ERR_INVALID, "grid must be in [1, 32768]");
             p->srp = true;
             p->srp_desc = *r->srp;
             p->quats.assign(r->quaternions, r->quaternions + 4 * r->n_att);

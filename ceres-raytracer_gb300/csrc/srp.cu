@@ -193,6 +193,211 @@ __global__ void k_srp_reduce(const double* __restrict__ partial, uint32_t grabs_
     }
 }
 
+// ---------------------------------------------------------------- wavefront SRP (crt_srp)
+// Items are (attitude, tile, lane) with each attitude's items padded to SRP_BLOCK_ITEMS; a wave is a
+// range of items aligned to SRP_BLOCK_ITEMS.  Each segment is one trace launch (the persistent
+// ray-queue kernel) writing per-item hits, then one shade launch in which block b sums the force and
+// torque of items [b * SRP_BLOCK_ITEMS, (b + 1) * SRP_BLOCK_ITEMS) in a fixed order into partial slot
+// b of the attitude.  Specular continuations stay at their item index, so every sum is independent
+// of scheduling and the results are bitwise reproducible.
+constexpr uint32_t SRP_BLOCK_ITEMS = 1024;
+constexpr uint32_t SRP_SHADE_THREADS = 256;
+
+struct SrpWave {
+    const SrpAtt* att;
+    uint32_t G, tiles_x, tiles;
+    uint32_t items_per_att;   // multiple of SRP_BLOCK_ITEMS
+    uint64_t i0;              // first item of the wave
+    uint32_t a0, r0;          // i0 = a0 * items_per_att + r0
+    uint32_t multi;           // the wave holds whole attitudes (r0 == 0) rather than part of one
+    float4* hit;              // per wave item: t, u, v, slot
+    float4* st_o;             // continuing ray: origin, power
+    float4* st_d;             // continuing ray: direction, triangle it leaves
+    uint8_t* alive;           // continuing ray present
+};
+
+// attitude of wave item i (32-bit arithmetic: a wave is whole attitudes or a part of one)
+__device__ __forceinline__ uint32_t srp_att(const SrpWave& W, uint32_t i, uint32_t& local) {
+    if (W.multi) {
+        const uint32_t q = i / W.items_per_att;
+        local = i - q * W.items_per_att;
+        return W.a0 + q;
+    }
+    local = W.r0 + i;
+    return W.a0;
+}
+
+__device__ __forceinline__ bool srp_item(const SrpWave& W, uint32_t i, uint32_t& a, uint32_t& px, uint32_t& py) {
+    uint32_t local;
+    a = srp_att(W, i, local);
+    const uint32_t tile = local >> 5, lane = local & 31u;
+    if (tile >= W.tiles) return false;
+    px = (tile % W.tiles_x) * 8u + (lane & 7u);
+    py = (tile / W.tiles_x) * 4u + (lane >> 3);
+    return px < W.G && py < W.G;
+}
+
+struct SrpPrimaryJob : JobBase {
+    SrpWave W;
+    __device__ bool ray(uint32_t i, TRay& r, Item&) const {
+        uint32_t a, px, py;
+        if (!srp_item(W, i, a, px, py)) return false;
+        const SrpAtt& P = W.att[a];
+        r.o = f3(P.org[0] + px * P.du[0] + py * P.dv[0], P.org[1] + px * P.du[1] + py * P.dv[1],
+                 P.org[2] + px * P.du[2] + py * P.dv[2]);
+        r.d = f3(P.dir[0], P.dir[1], P.dir[2]);
+        r.tmin = 0.f;
+        r.tmax = 3.402823466e38f;
+        return true;
+    }
+    __device__ void write(const SceneView&, uint32_t i, const TRay&, const THit& h, const Item&) const {
+        W.hit[i] = make_float4(h.t, h.u, h.v, __uint_as_float(h.slot));
+    }
+};
+
+// continuing rays: a compacted queue of item indices (hits still land at the item's own slot)
+struct SrpBounceJob {
+    SrpWave W;
+    const uint32_t* q;
+    struct Item {
+        uint32_t i;
+    };
+    __device__ __forceinline__ const SceneView& view(const SceneView& sv, const Item&) const { return sv; }
+    __device__ bool ray(uint32_t k, TRay& r, Item& it) const {
+        const uint32_t i = q[k];
+        const float4 o = W.st_o[i], d = W.st_d[i];
+        r.o = f3(o.x, o.y, o.z);
+        r.d = f3(d.x, d.y, d.z);
+        r.tmin = 0.f;
+        r.tmax = 3.402823466e38f;
+        r.skip = __float_as_uint(d.w);
+        it.i = i;
+        return true;
+    }
+    __device__ void write(const SceneView&, uint32_t, const TRay&, const THit& h, const Item& it) const {
+        W.hit[it.i] = make_float4(h.t, h.u, h.v, __uint_as_float(h.slot));
+    }
+};
+
+// warp-aggregated append of one entry per participating lane
+__device__ __forceinline__ uint32_t srp_append(uint32_t* counter) {
+    const uint32_t mask = __activemask();
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(mask) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(counter, (uint32_t)__popc(mask));
+    base = __shfl_sync(mask, base, leader);
+    return base + __popc(mask & ((1u << lane) - 1u));
+}
+
+struct SrpShadeArgs {
+    uint32_t n_items;         // items in the wave
+    uint32_t seg, nb;
+    float inv_c;
+    float cm[3];
+    double* partial;          // 6 per block of SRP_BLOCK_ITEMS items (global block index)
+    double* facet;            // n_att * n_tris or null
+    uint32_t n_tris;
+    uint32_t* q_out;          // continuing items of the next segment
+    uint32_t* q_count;
+};
+
+template <bool FIRST>
+__global__ void __launch_bounds__(SRP_SHADE_THREADS) k_srp_shade(SceneView sv, SrpWave W, SrpShadeArgs A) {
+    __shared__ double red[SRP_SHADE_THREADS / 32][6];
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    double acc[6] = {0, 0, 0, 0, 0, 0};
+#pragma unroll 1
+    for (uint32_t j = 0; j < SRP_BLOCK_ITEMS / SRP_SHADE_THREADS; ++j) {
+        const uint32_t i = blockIdx.x * SRP_BLOCK_ITEMS + j * SRP_SHADE_THREADS + threadIdx.x;
+        uint32_t a = 0, px = 0, py = 0, local = 0;
+        bool alive = false;
+        if (i < A.n_items) alive = FIRST ? srp_item(W, i, a, px, py) : W.alive[i] != 0;
+        if (!FIRST) a = srp_att(W, i, local);
+        THit h;
+        h.slot = CRT_MISS;
+        float3 d = f3(0.f, 0.f, 0.f);
+        float E = 0.f;
+        if (alive) {
+            const float4 hv = W.hit[i];
+            h.t = hv.x;
+            h.u = hv.y;
+            h.v = hv.z;
+            h.slot = __float_as_uint(hv.w);
+            if (FIRST) {
+                const SrpAtt& P = W.att[a];
+                d = f3(P.dir[0], P.dir[1], P.dir[2]);
+                E = P.E0;
+            } else {
+                const float4 o = W.st_o[i], dd = W.st_d[i];
+                d = f3(dd.x, dd.y, dd.z);
+                E = o.w;
+            }
+        }
+        const bool hit = h.slot != CRT_MISS;
+        float absorbed = 0.f;
+        uint32_t key = 0xFFFFFFFFu;
+        bool cont = false;
+        if (hit) {
+            const SurfacePoint sp = surface_point(sv, h);
+            const EntityDev& Ent = sv.entities[sp.entity];
+            const float rs = Ent.rho_s, rd = Ent.rho_d;
+            float3 n = sp.flat_n * -1.0f;                 // outward for counter-clockwise meshes
+            if (dot3(d, n) > 0.f) n = n * -1.0f;          // two-sided: face the incoming ray
+            const float cs = -dot3(d, n);
+            const float k1 = E * A.inv_c * (1.0f - rs);
+            const float k2 = E * A.inv_c * (2.0f * rs * cs + (2.0f / 3.0f) * rd);
+            const float3 dF = d * k1 - n * k2;
+            const float3 x = sp.x;
+            const float3 dT = cross3(x - f3(A.cm[0], A.cm[1], A.cm[2]), dF);
+            acc[0] += dF.x; acc[1] += dF.y; acc[2] += dF.z;
+            acc[3] += dT.x; acc[4] += dT.y; acc[5] += dT.z;
+            absorbed = (1.0f - rs - rd) * E;
+            key = __ldg(sv.leaf_prim + h.slot);
+            if (rs > 0.f && A.seg < A.nb) {
+                const float3 dn = d - n * (2.0f * dot3(d, n));
+                const float m = fmaxf(fabsf(x.x), fmaxf(fabsf(x.y), fabsf(x.z)));
+                int e;
+                frexpf(m, &e);
+                const float off = fmaxf(1e-5f, ldexpf(1.0f, e - 24 + 3));
+                const float3 o = x + n * off;
+                W.st_o[i] = make_float4(o.x, o.y, o.z, E * rs);
+                W.st_d[i] = make_float4(dn.x, dn.y, dn.z, __uint_as_float(h.slot));
+                cont = true;
+                A.q_out[srp_append(A.q_count)] = i;
+            }
+        }
+        if (A.nb > A.seg && i < A.n_items) W.alive[i] = cont ? 1 : 0;
+        if (A.facet && __any_sync(0xffffffffu, hit)) {
+            // warp-aggregated facet power (FP32 group sums of at most 32 terms, FP64 atomics)
+            const uint32_t peers = __match_any_sync(0xffffffffu, key);
+            float sum = absorbed;
+            if (__any_sync(0xffffffffu, hit && peers != (1u << lane))) {
+                sum = 0.f;
+#pragma unroll 8
+                for (int q = 0; q < 32; ++q) {
+                    const float v = __shfl_sync(0xffffffffu, absorbed, q);
+                    if ((peers >> q) & 1u) sum += v;
+                }
+            }
+            if (hit && lane == (uint32_t)(__ffs(peers) - 1))
+                atomicAdd(&A.facet[(size_t)a * A.n_tris + key], (double)sum);
+        }
+    }
+    // fixed-order block reduction: warp tree, then the warps in order
+    for (int k = 0; k < 6; ++k)
+        for (int o = 16; o; o >>= 1) acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], o);
+    if (lane == 0)
+        for (int k = 0; k < 6; ++k) red[warp][k] = acc[k];
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        double t = 0.0;
+        for (uint32_t w = 0; w < SRP_SHADE_THREADS / 32; ++w) t += red[w][threadIdx.x];
+        const size_t slot = (size_t)(W.i0 / SRP_BLOCK_ITEMS + blockIdx.x) * 6 + threadIdx.x;
+        A.partial[slot] = FIRST ? t : A.partial[slot] + t;
+    }
+}
+
 }  // namespace
 
 // Runs on `ctx` (stream, scratch, error word), which may differ from the scene's own context on the
@@ -201,7 +406,7 @@ void srp_run(crt_context* ctx, crt_scene* s, const crt_srp_desc* desc, const dou
              double* force, double* torque, double* facet_power) {
     [&] {
         CRT_CHECK(n_att == 0 || (quats && force && torque), CRT_ERR_INVALID, "null buffer");
-        CRT_CHECK(desc->grid > 0 && desc->grid <= 65536, CRT_ERR_INVALID, "grid must be in [1, 65536]");
+        CRT_CHECK(desc->grid > 0 && desc->grid <= 32768, CRT_ERR_INVALID, "grid must be in [1, 32768]");
         CRT_CHECK(desc->c > 0 && std::isfinite(desc->flux), CRT_ERR_INVALID, "bad flux or speed of light");
         CRT_CHECK(desc->num_bounces <= 16, CRT_ERR_INVALID, "at most 16 specular bounces");
         if (!n_att) return;
@@ -259,50 +464,85 @@ void srp_run(crt_context* ctx, crt_scene* s, const crt_srp_desc* desc, const dou
             att[a].E0 = (float)(desc->flux * h * h);
             att[a].pad = 0.f;
         }
-        const uint32_t tiles = ((G + 7) / 8) * ((G + 3) / 4);
-        const size_t smem = (size_t)CRT_STACK_SMEM * CRT_TRACE_BLOCK * sizeof(uint2);
-        const int grid = occupancy_grid(ctx, ctx->counting ? (const void*)k_srp<true> : (const void*)k_srp<false>,
-                                        CRT_TRACE_BLOCK, smem);
-        // tiles per grab: up to CHUNK, fewer when the grabs would not outnumber the resident warps 4:1
-        const size_t warps = (size_t)grid * (CRT_TRACE_BLOCK / 32);
-        const uint32_t chunk =
-            (uint32_t)std::max<size_t>(1, std::min<size_t>(CHUNK, (size_t)tiles * n_att / (4 * warps)));
-        const uint32_t gpa = (tiles + chunk - 1) / chunk;
-        // keep each launch's grab count well inside 32 bits
-        const size_t att_per_launch = std::max<size_t>(1, std::min<size_t>(n_att, (1u << 30) / gpa));
+        const uint32_t tiles_x = (G + 7) / 8, tiles = tiles_x * ((G + 3) / 4);
+        const uint64_t ipa = ((uint64_t)tiles * 32 + SRP_BLOCK_ITEMS - 1) / SRP_BLOCK_ITEMS * SRP_BLOCK_ITEMS;
+        const uint64_t total = ipa * n_att;
+        const uint64_t blocks_per_att = ipa / SRP_BLOCK_ITEMS;
+        CRT_CHECK(blocks_per_att * n_att < (1ull << 31), CRT_ERR_INVALID, "too many rays in one call");
+        // a wave: whole attitudes, or a part of one attitude, of up to 2^24 items (about 50 bytes of
+        // state each); always a multiple of the reduction block
+        const uint32_t wave_cap = 1u << 24;
+        const uint64_t att_per_wave = ipa <= wave_cap ? wave_cap / ipa : 0;
+        // specular continuations only when some entity reflects specularly
+        bool specular = false;
+        for (const EntityDev& E : s->host_entities) specular |= E.rho_s > 0.f;
+        const uint32_t nb = specular ? desc->num_bounces : 0u;
+        const uint64_t wave_items = att_per_wave ? std::min<uint64_t>(att_per_wave * ipa, total) : wave_cap;
         SrpAtt* d_att = (SrpAtt*)ctx_scratch(ctx, SCR_IN1, sizeof(SrpAtt) * n_att);
         CRT_CUDA(cudaMemcpyAsync(d_att, att.data(), sizeof(SrpAtt) * n_att, cudaMemcpyHostToDevice, st));
-        double* d_partial = (double*)ctx_scratch(ctx, SCR_WAVE3, sizeof(double) * 6 * gpa * att_per_launch);
+        double* d_partial = (double*)ctx_scratch(ctx, SCR_WAVE3, sizeof(double) * 6 * blocks_per_att * n_att);
+        char* state = (char*)ctx_scratch(ctx, SCR_WAVE4, wave_items * (nb ? 16 + 16 + 16 + 1 : 16) + 1024);
+        uint32_t* bq = nb ? (uint32_t*)ctx_scratch(ctx, SCR_WAVE5, wave_items * 4 + 256) : nullptr;
+        uint32_t* bcount = (uint32_t*)ctx_scratch(ctx, SCR_WAVE6, 256);
         double* d_force = (double*)out_device(ctx, force, n_att * 24, SCR_OUT0);
         double* d_torque = (double*)out_device(ctx, torque, n_att * 24, SCR_OUT1);
         double* d_facet = facet_power ? (double*)out_device(ctx, facet_power, n_att * s->n_tris * 8, SCR_OUT2) : nullptr;
         if (d_facet) CRT_CUDA(cudaMemsetAsync(d_facet, 0, n_att * s->n_tris * 8, st));
-        uint32_t* queue = (uint32_t*)ctx_scratch(ctx, SCR_QUEUE, 256);
         const SceneView sv = scene_view(s);
-        for (size_t a0 = 0; a0 < n_att; a0 += att_per_launch) {
-            const size_t na = std::min(att_per_launch, n_att - a0);
-            SrpArgs A;
-            A.att = d_att + a0;
-            A.G = G;
-            A.tiles = tiles;
-            A.grabs_per_att = gpa;
-            A.chunk = chunk;
-            A.n_att = (uint32_t)na;
-            A.inv_c = (float)(1.0 / desc->c);
-            for (int k = 0; k < 3; ++k) A.cm[k] = (float)desc->center_of_mass[k];
-            A.nb = desc->num_bounces;
-            A.partial = d_partial;
-            A.facet = d_facet ? d_facet + a0 * s->n_tris : nullptr;
-            A.n_tris = (uint32_t)s->n_tris;
-            CRT_CUDA(cudaMemsetAsync(queue, 0, sizeof(uint32_t), st));
-            if (ctx->counting)
-                k_srp<true><<<grid, CRT_TRACE_BLOCK, smem, st>>>(sv, A, queue, ctx->d_error, ctx->d_counters);
-            else
-                k_srp<false><<<grid, CRT_TRACE_BLOCK, smem, st>>>(sv, A, queue, ctx->d_error, ctx->d_counters);
-            check_launch(ctx, "k_srp");
-            k_srp_reduce<<<(uint32_t)na, 256, 0, st>>>(d_partial, gpa, d_force + 3 * a0, d_torque + 3 * a0);
-            check_launch(ctx, "k_srp_reduce");
+        SrpWave W;
+        W.att = d_att;
+        W.G = G;
+        W.tiles_x = tiles_x;
+        W.tiles = tiles;
+        W.items_per_att = (uint32_t)ipa;
+        W.hit = (float4*)state;
+        W.st_o = nb ? (float4*)(state + wave_items * 16) : nullptr;
+        W.st_d = nb ? (float4*)(state + wave_items * 32) : nullptr;
+        W.alive = nb ? (uint8_t*)(state + wave_items * 48) : nullptr;
+        SrpShadeArgs A;
+        A.nb = nb;
+        A.inv_c = (float)(1.0 / desc->c);
+        for (int k = 0; k < 3; ++k) A.cm[k] = (float)desc->center_of_mass[k];
+        A.partial = d_partial;
+        A.facet = d_facet;
+        A.n_tris = (uint32_t)s->n_tris;
+        A.q_out = bq;
+        for (uint64_t i0 = 0; i0 < total;) {
+            // whole attitudes, or the rest of the current attitude
+            const uint64_t r0 = i0 % ipa;
+            const uint32_t n = (uint32_t)(att_per_wave ? std::min<uint64_t>(wave_items, total - i0)
+                                                       : std::min<uint64_t>(wave_cap, ipa - r0));
+            W.i0 = i0;
+            W.a0 = (uint32_t)(i0 / ipa);
+            W.r0 = (uint32_t)r0;
+            W.multi = att_per_wave ? 1u : 0u;
+            i0 += n;
+            A.n_items = n;
+            const uint32_t nblk = (n + SRP_BLOCK_ITEMS - 1) / SRP_BLOCK_ITEMS;
+            for (uint32_t seg = 0; seg <= nb; ++seg) {
+                A.seg = seg;
+                A.q_count = bcount + (seg & 1);          // filled by this segment's shade
+                if (seg < nb) CRT_CUDA(cudaMemsetAsync(A.q_count, 0, sizeof(uint32_t), st));
+                if (seg == 0) {
+                    SrpPrimaryJob J;
+                    J.W = W;
+                    // single 32-ray grabs keep the warps on a narrow band of the grid, so BVH nodes
+                    // are reused from L1/L2 (measured: larger grabs were slower on the 2M asteroid)
+                    launch_trace<false>(ctx, sv, J, n);
+                    k_srp_shade<true><<<nblk, SRP_SHADE_THREADS, 0, st>>>(sv, W, A);
+                } else {
+                    // the queue filled by the previous segment's shade; its count stays on the device
+                    SrpBounceJob J;
+                    J.W = W;
+                    J.q = bq;
+                    launch_trace<false>(ctx, sv, J, n, bcount + ((seg - 1) & 1));
+                    k_srp_shade<false><<<nblk, SRP_SHADE_THREADS, 0, st>>>(sv, W, A);
+                }
+                check_launch(ctx, "k_srp_shade");
+            }
         }
+        k_srp_reduce<<<(uint32_t)n_att, 256, 0, st>>>(d_partial, (uint32_t)blocks_per_att, d_force, d_torque);
+        check_launch(ctx, "k_srp_reduce");
         out_finish(ctx, force, d_force, n_att * 24);
         out_finish(ctx, torque, d_torque, n_att * 24);
         if (facet_power) out_finish(ctx, facet_power, d_facet, n_att * s->n_tris * 8);
@@ -360,7 +600,7 @@ extern "C" int crt_srp_static(crt_scene* s, const crt_srp_desc* desc, const doub
         CRT_CHECK(n_att == 0 || (quats && force && torque), CRT_ERR_INVALID, "null buffer");
         CRT_CHECK(n_att <= CRT_SRP_STATIC_MAX_ATT, CRT_ERR_INVALID,
                   "crt_srp_static: at most 4096 attitudes per call (static scratch limit)");
-        CRT_CHECK(desc->grid > 0 && desc->grid <= 65536, CRT_ERR_INVALID, "grid must be in [1, 65536]");
+        CRT_CHECK(desc->grid > 0 && desc->grid <= 32768, CRT_ERR_INVALID, "grid must be in [1, 32768]");
         CRT_CHECK(desc->c > 0 && std::isfinite(desc->flux), CRT_ERR_INVALID, "bad flux or speed of light");
         CRT_CHECK(desc->num_bounces <= 16, CRT_ERR_INVALID, "at most 16 specular bounces");
         CRT_CHECK(!is_device_ptr(quats), CRT_ERR_INVALID, "crt_srp_static reads the quaternions from host memory");

@@ -71,7 +71,10 @@ struct JobBase {
     __device__ __forceinline__ const SceneView& view(const SceneView& sv, const Item&) const { return sv; }
 };
 
-// Persistent ray-queue kernel: each warp takes `chunk` x 32 consecutive items per atomic grab.
+// Persistent ray-queue kernel.  Each warp takes groups of 32 consecutive items per atomic grab: with
+// chunk == 1 one group, otherwise a guided size of up to `chunk` groups, shrinking with the work
+// left so that the last grabs stay small (few atomics on the queue counter while much work is left,
+// balance at the end).
 template <bool ANY, bool COUNT, class Job>
 __global__ void __launch_bounds__(CRT_TRACE_BLOCK, 8) k_trace(SceneView sv, Job job, uint32_t n_items,
                                                             const uint32_t* __restrict__ n_dev,
@@ -82,12 +85,21 @@ __global__ void __launch_bounds__(CRT_TRACE_BLOCK, 8) k_trace(SceneView sv, Job 
     const int lane = threadIdx.x & 31;
     TravStats st{0u, 0u};
     uint32_t nrays = 0;
+    const uint32_t warps_total = gridDim.x * (blockDim.x >> 5);
     while (true) {
-        uint32_t base = 0;
-        if (lane == 0) base = atomicAdd(queue, 32u * chunk);
+        uint32_t base = 0, take = 1;
+        if (lane == 0) {
+            if (chunk > 1) {
+                const uint32_t cur = *reinterpret_cast<volatile uint32_t*>(queue);
+                const uint32_t left = cur < n_items ? (n_items - cur) >> 5 : 0u;
+                take = min(chunk, max(1u, left / (4u * warps_total)));
+            }
+            base = atomicAdd(queue, 32u * take);
+        }
         base = __shfl_sync(0xffffffffu, base, 0);
+        take = __shfl_sync(0xffffffffu, take, 0);
         if (base >= n_items) break;
-        for (uint32_t c = 0; c < chunk; ++c) {
+        for (uint32_t c = 0; c < take; ++c) {
             const uint32_t i = base + 32u * c + lane;
             TRay r;
             typename Job::Item it;
@@ -117,7 +129,7 @@ __global__ void __launch_bounds__(CRT_TRACE_BLOCK, 8) k_trace(SceneView sv, Job 
 // given: n_items is then the upper bound used to size the grid).
 template <bool ANY, class Job>
 void launch_trace(crt_context* ctx, const SceneView& sv, const Job& job, uint32_t n_items,
-                  const uint32_t* n_dev = nullptr, uint32_t* queue = nullptr) {
+                  const uint32_t* n_dev = nullptr, uint32_t* queue = nullptr, uint32_t chunk_override = 0) {
     if (!queue) queue = (uint32_t*)ctx_scratch(ctx, SCR_QUEUE, 256);
     CRT_CUDA(cudaMemsetAsync(queue, 0, sizeof(uint32_t), ctx->stream));
     const size_t smem = (size_t)CRT_STACK_SMEM * CRT_TRACE_BLOCK * sizeof(uint2);
@@ -125,7 +137,7 @@ void launch_trace(crt_context* ctx, const SceneView& sv, const Job& job, uint32_
     int grid = occupancy_grid(ctx, kfn, CRT_TRACE_BLOCK, smem);
     const uint32_t need = (n_items + CRT_TRACE_BLOCK - 1) / CRT_TRACE_BLOCK;
     if ((uint32_t)grid > need) grid = (int)std::max<uint32_t>(need, 1u);
-    const uint32_t chunk = ctx->queue_chunk ? ctx->queue_chunk : 1u;
+    const uint32_t chunk = chunk_override ? chunk_override : (ctx->queue_chunk ? ctx->queue_chunk : 1u);
     if (ctx->counting)
         k_trace<ANY, true, Job><<<grid, CRT_TRACE_BLOCK, smem, ctx->stream>>>(sv, job, n_items, n_dev, queue,
                                                                              ctx->d_error, ctx->d_counters, chunk);

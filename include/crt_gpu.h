@@ -126,7 +126,7 @@ typedef struct {
     double flux;                  /* W / m^2 at the body */
     double c;                     /* m / s */
     double center_of_mass[3];     /* body frame */
-    uint32_t grid;                /* grid x grid rays per attitude */
+    uint32_t grid;                /* grid x grid rays per attitude, 1..32768 */
     uint32_t num_bounces;         /* specular continuation segments after the primary hit */
 } crt_srp_desc;
 
@@ -156,7 +156,7 @@ typedef struct {
 
 /* Tuning knobs of the persistent kernels and the batched wavefront (chosen by the autotuner). */
 typedef struct {
-    uint32_t queue_chunk;                 /* 32-ray groups a warp takes per atomic grab (1..8) */
+    uint32_t queue_chunk;                 /* max 32-ray groups per atomic grab (1..8), guided by the work left */
     uint32_t wave_paths;                  /* camera paths per wave (>= 65536) */
     int use_graphs;                       /* replay batched waves as CUDA graphs */
 } crt_tuning;
