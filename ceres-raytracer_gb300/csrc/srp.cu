@@ -302,18 +302,29 @@ struct SrpShadeArgs {
     uint32_t* q_count;
 };
 
+// Sums: each thread adds its (at most 4) rays in FP32, the warp tree is FP32 (at most 128 terms, so
+// the rounding is below 1e-5 of the summed magnitudes), the 8 warps of a block and all blocks are
+// summed in FP64, every step in a fixed order.  Blocks without a hit skip the reduction (GB300 runs
+// FP64 at a small fraction of its FP32 rate, and most blocks of a sun grid miss the body).
 template <bool FIRST>
 __global__ void __launch_bounds__(SRP_SHADE_THREADS) k_srp_shade(SceneView sv, SrpWave W, SrpShadeArgs A) {
     __shared__ double red[SRP_SHADE_THREADS / 32][6];
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-    double acc[6] = {0, 0, 0, 0, 0, 0};
+    float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    bool any_hit = false;
 #pragma unroll 1
     for (uint32_t j = 0; j < SRP_BLOCK_ITEMS / SRP_SHADE_THREADS; ++j) {
         const uint32_t i = blockIdx.x * SRP_BLOCK_ITEMS + j * SRP_SHADE_THREADS + threadIdx.x;
         uint32_t a = 0, px = 0, py = 0, local = 0;
         bool alive = false;
-        if (i < A.n_items) alive = FIRST ? srp_item(W, i, a, px, py) : W.alive[i] != 0;
-        if (!FIRST) a = srp_att(W, i, local);
+        if (i < A.n_items) {
+            if (FIRST) {
+                alive = srp_item(W, i, a, px, py);
+            } else {
+                alive = W.alive[i] != 0;
+                if (alive) a = srp_att(W, i, local);
+            }
+        }
         THit h;
         h.slot = CRT_MISS;
         float3 d = f3(0.f, 0.f, 0.f);
@@ -335,6 +346,7 @@ __global__ void __launch_bounds__(SRP_SHADE_THREADS) k_srp_shade(SceneView sv, S
             }
         }
         const bool hit = h.slot != CRT_MISS;
+        any_hit |= hit;
         float absorbed = 0.f;
         uint32_t key = 0xFFFFFFFFu;
         bool cont = false;
@@ -367,7 +379,7 @@ __global__ void __launch_bounds__(SRP_SHADE_THREADS) k_srp_shade(SceneView sv, S
                 A.q_out[srp_append(A.q_count)] = i;
             }
         }
-        if (A.nb > A.seg && i < A.n_items) W.alive[i] = cont ? 1 : 0;
+        if (A.nb > A.seg && i < A.n_items && (FIRST || alive)) W.alive[i] = cont ? 1 : 0;
         if (A.facet && __any_sync(0xffffffffu, hit)) {
             // warp-aggregated facet power (FP32 group sums of at most 32 terms, FP64 atomics)
             const uint32_t peers = __match_any_sync(0xffffffffu, key);
@@ -384,17 +396,20 @@ __global__ void __launch_bounds__(SRP_SHADE_THREADS) k_srp_shade(SceneView sv, S
                 atomicAdd(&A.facet[(size_t)a * A.n_tris + key], (double)sum);
         }
     }
-    // fixed-order block reduction: warp tree, then the warps in order
+    const size_t slot = (size_t)(W.i0 / SRP_BLOCK_ITEMS + blockIdx.x) * 6;
+    if (!__syncthreads_or(any_hit)) {
+        if (FIRST && threadIdx.x < 6) A.partial[slot + threadIdx.x] = 0.0;
+        return;
+    }
     for (int k = 0; k < 6; ++k)
         for (int o = 16; o; o >>= 1) acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], o);
     if (lane == 0)
-        for (int k = 0; k < 6; ++k) red[warp][k] = acc[k];
+        for (int k = 0; k < 6; ++k) red[warp][k] = (double)acc[k];
     __syncthreads();
     if (threadIdx.x < 6) {
         double t = 0.0;
         for (uint32_t w = 0; w < SRP_SHADE_THREADS / 32; ++w) t += red[w][threadIdx.x];
-        const size_t slot = (size_t)(W.i0 / SRP_BLOCK_ITEMS + blockIdx.x) * 6 + threadIdx.x;
-        A.partial[slot] = FIRST ? t : A.partial[slot] + t;
+        A.partial[slot + threadIdx.x] = FIRST ? t : A.partial[slot + threadIdx.x] + t;
     }
 }
 
