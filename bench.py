@@ -114,6 +114,17 @@ def dist_info():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
 
+def replica_throughput(ms, rays_per_step, world, device):
+    """Whole-job throughput of `world` replicas (one per GPU, no data-path collective): the step
+    time is the maximum over ranks, the rays are every rank's.  Returns (max ms, Mrays/s)."""
+    if world > 1:
+        import torch
+        t = torch.tensor([ms], dtype=torch.float64, device=device)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    return ms, rays_per_step * world / (ms / 1e3) / 1e6
+
+
 def percentile(xs, q):
     xs = sorted(xs)
     if not xs:
@@ -353,12 +364,7 @@ def gpu_arm(args):
     lat_render = [a.elapsed_time(b) for a, b, c in ev]
     lat_lidar = [b.elapsed_time(c) for a, b, c in ev]
     step_ms = [a.elapsed_time(c) for a, b, c in ev]
-    ms = float(np.mean(step_ms))
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = rays_step * world / (ms / 1e3) / 1e6
+    ms, value = replica_throughput(float(np.mean(step_ms)), rays_step, world, dev)
 
     # ---- roofline of the dominant kernel: closest-hit traversal of the primary camera rays
     rays64 = scenes_camera_rays(cam)
