@@ -141,6 +141,8 @@ SIGNATURES = {
     "crt_batch": ([vp, vp, sz, ctypes.POINTER(BatchStats)], i32),
     "crt_context_set_tuning": ([vp, ctypes.POINTER(Tuning)], i32),
     "crt_context_get_tuning": ([vp, ctypes.POINTER(Tuning)], i32),
+    "crt_host_alloc": ([sz, ctypes.POINTER(vp)], i32),
+    "crt_host_free": ([vp], i32),
     "crt_server_create": ([i32, ctypes.POINTER(ServerConfig), ctypes.POINTER(vp)], i32),
     "crt_server_destroy": ([vp], i32),
     "crt_server_last_error": ([], ctypes.c_char_p),

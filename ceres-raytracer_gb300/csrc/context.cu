@@ -255,6 +255,25 @@ int crt_context_get_tuning(const crt_context* ctx, crt_tuning* out) {
     return CRT_OK;
 }
 
+int crt_host_alloc(size_t bytes, void** out) {
+    if (!out) return CRT_ERR_INVALID;
+    *out = nullptr;
+    if (cudaMallocHost(out, bytes ? bytes : 1) != cudaSuccess) {
+        cudaGetLastError();
+        *out = nullptr;
+        return CRT_ERR_OOM;
+    }
+    return CRT_OK;
+}
+
+int crt_host_free(void* ptr) {
+    if (ptr && cudaFreeHost(ptr) != cudaSuccess) {
+        cudaGetLastError();
+        return CRT_ERR_CUDA;
+    }
+    return CRT_OK;
+}
+
 const char* crt_context_last_error(const crt_context* ctx) { return ctx ? ctx->last_error.c_str() : "null context"; }
 
 }  // extern "C"

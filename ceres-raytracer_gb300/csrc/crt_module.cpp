@@ -18,6 +18,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <map>
 #include <memory>
 #include <mutex>
 #include <stdexcept>
@@ -55,6 +56,67 @@ crt_context* ctx() {
         }
     }
     return g_ctx;
+}
+
+// Page-locked result arrays: renders, passes and scans return numpy arrays whose memory comes from
+// crt_host_alloc, so the device-to-host copies run at the full host link rate.  Buffers of released
+// arrays are kept for reuse, up to 1 GiB.  The pool is never destroyed (arrays may outlive the
+// module's static objects at interpreter exit).
+struct PinnedPool {
+    std::mutex mu;
+    std::multimap<size_t, void*> free_;
+    size_t cached = 0;
+    void* get(size_t n, size_t& cap) {
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            auto it = free_.lower_bound(n);
+            if (it != free_.end() && it->first <= 2 * n + 4096) {
+                cap = it->first;
+                void* p = it->second;
+                cached -= cap;
+                free_.erase(it);
+                return p;
+            }
+        }
+        void* p = nullptr;
+        if (crt_host_alloc(n, &p) != CRT_OK || !p) throw std::bad_alloc();
+        cap = n;
+        return p;
+    }
+    void put(void* p, size_t cap) {
+        std::lock_guard<std::mutex> lk(mu);
+        if (cached + cap > ((size_t)1 << 30)) {
+            crt_host_free(p);
+            return;
+        }
+        free_.emplace(cap, p);
+        cached += cap;
+    }
+};
+
+PinnedPool& pinned_pool() {
+    static PinnedPool* pool = new PinnedPool();
+    return *pool;
+}
+
+struct PinnedBlock {
+    void* p;
+    size_t cap;
+};
+
+template <class T>
+py::array_t<T> pinned_array(std::vector<py::ssize_t> shape) {
+    size_t n = sizeof(T);
+    for (py::ssize_t d : shape) n *= (size_t)d;
+    size_t cap = 0;
+    void* p = pinned_pool().get(std::max<size_t>(n, 1), cap);
+    auto* blk = new PinnedBlock{p, cap};
+    py::capsule owner(blk, [](void* q) {
+        PinnedBlock* b = static_cast<PinnedBlock*>(q);
+        pinned_pool().put(b->p, b->cap);
+        delete b;
+    });
+    return py::array_t<T>(shape, static_cast<T*>(p), owner);
 }
 
 bool verbose() {
@@ -300,9 +362,9 @@ py::object do_render(crt_scene* s, const SimpleCamera& cam, const py::list& ligh
     const crt_camera_desc cd = cam.desc();
     const auto ls = light_descs(lights);
     crt_render_params p{min_s, max_s, thr, bounces, seed, request};
-    py::array_t<uint8_t> img({cam.height(), cam.width(), 4});
+    py::array_t<uint8_t> img = pinned_array<uint8_t>({cam.height(), cam.width(), 4});
     py::array_t<float> rad;
-    if (return_radiance) rad = py::array_t<float>({cam.height(), cam.width(), 4});
+    if (return_radiance) rad = pinned_array<float>({cam.height(), cam.width(), 4});
     {
         uint8_t* ip = img.mutable_data();
         float* rp = return_radiance ? rad.mutable_data() : nullptr;
@@ -317,7 +379,7 @@ py::object do_render(crt_scene* s, const SimpleCamera& cam, const py::list& ligh
 
 py::array_t<double> do_points(crt_scene* s, const SimpleCamera& cam, bool normals) {
     const crt_camera_desc cd = cam.desc();
-    py::array_t<double> out({cam.height(), cam.width(), 3});
+    py::array_t<double> out = pinned_array<double>({cam.height(), cam.width(), 3});
     double* o = out.mutable_data();
     py::gil_scoped_release nogil;
     std::lock_guard<std::mutex> lk(g_mu);
@@ -328,7 +390,7 @@ py::array_t<double> do_points(crt_scene* s, const SimpleCamera& cam, bool normal
 
 py::array_t<uint32_t> do_instances(crt_scene* s, const SimpleCamera& cam) {
     const crt_camera_desc cd = cam.desc();
-    py::array_t<uint32_t> out({cam.height(), cam.width()});
+    py::array_t<uint32_t> out = pinned_array<uint32_t>({cam.height(), cam.width()});
     uint32_t* o = out.mutable_data();
     py::gil_scoped_release nogil;
     std::lock_guard<std::mutex> lk(g_mu);
@@ -348,7 +410,7 @@ double do_single_lidar(crt_scene* s, const SimpleLidar& l) {
 
 py::array_t<double> do_batch_lidar(crt_scene* s, const SimpleLidar& l) {
     const size_t n = l.batch_positions.size() / 3;
-    py::array_t<double> out({(py::ssize_t)1, (py::ssize_t)n});
+    py::array_t<double> out = pinned_array<double>({(py::ssize_t)1, (py::ssize_t)n});
     double* o = out.mutable_data();
     if (n) {
         py::gil_scoped_release nogil;
@@ -370,8 +432,8 @@ py::tuple do_lidar_scan(crt_scene* s, const SimpleLidar& l) {
     g.ny = l.ny;
     g.half_angle_x = l.half_x;
     g.half_angle_y = l.half_y;
-    py::array_t<double> rng({(py::ssize_t)l.ny, (py::ssize_t)l.nx});
-    py::array_t<uint32_t> prim({(py::ssize_t)l.ny, (py::ssize_t)l.nx});
+    py::array_t<double> rng = pinned_array<double>({(py::ssize_t)l.ny, (py::ssize_t)l.nx});
+    py::array_t<uint32_t> prim = pinned_array<uint32_t>({(py::ssize_t)l.ny, (py::ssize_t)l.nx});
     double* rp = rng.mutable_data();
     uint32_t* pp = prim.mutable_data();
     {

@@ -262,6 +262,12 @@ int crt_srp(crt_scene* scene, const crt_srp_desc* desc, const double* quaternion
 int crt_srp_static(crt_scene* scene, const crt_srp_desc* desc, const double* quaternions, size_t n_att,
                    double* force, double* torque);
 
+/* Page-locked host memory for outputs (no counterpart in the reference): device-to-host copies
+ * into such buffers run at the full host link rate instead of through a pageable bounce buffer.
+ * The pybind11 module hands its result arrays out of a pool of these. */
+int crt_host_alloc(size_t bytes, void** out);
+int crt_host_free(void* ptr);
+
 /* ---------------------------------------------------------------- serving
  * A request loop over resident scenes (no counterpart in the reference, which renders one camera per
  * call), with continuous batching: requests are submitted from any thread and queued; each of
