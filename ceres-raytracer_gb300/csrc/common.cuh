@@ -166,7 +166,6 @@ void scene_build(crt_scene* s, const crt_entity_desc* ents, uint32_t n);   // bv
 // render.cu: batched wavefront on an explicit context (its stream, scratch and error word)
 void batch_run(crt_context* ctx, const crt_request* reqs, size_t n, crt_batch_stats* stats);
 void batch_check_request(const crt_request& q);
-size_t batch_footprint(const crt_request& q, uint32_t wave_paths);
 // serving engine (render.cu): resident requests, one wave per step
 struct WaveEngine;
 WaveEngine* engine_create(crt_context* ctx, size_t budget_bytes);
@@ -174,7 +173,6 @@ void engine_destroy(WaveEngine* e);
 bool engine_admit(WaveEngine* e, const crt_request& q, uint64_t tag);
 void engine_step(WaveEngine* e, std::vector<uint64_t>& completed);
 void engine_abort(WaveEngine* e, std::vector<uint64_t>& dropped);
-size_t engine_resident(const WaveEngine* e);
 // srp.cu: radiation pressure on an explicit context
 void srp_run(crt_context* ctx, crt_scene* s, const crt_srp_desc* desc, const double* quats, size_t n_att,
              double* force, double* torque, double* facet_power);

@@ -1271,10 +1271,6 @@ void engine_destroy(WaveEngine* e) {
     delete e;
 }
 
-size_t engine_resident(const WaveEngine* e) {
-    return e->res.size() + e->flights[0].tags.size() + e->flights[1].tags.size();
-}
-
 // Admits a request when its state fits the free arenas now (false: retry after requests finish).
 // A request larger than an arena is admitted alone, the arena growing to fit it.
 bool engine_admit(WaveEngine* e, const crt_request& q, uint64_t tag) {
@@ -1643,17 +1639,6 @@ void batch_run(crt_context* ctx, const crt_request* reqs, size_t n, crt_batch_st
     run_batch(ctx, reqs, n, stats);
 }
 void batch_check_request(const crt_request& q) { check_request(q); }
-
-size_t batch_footprint(const crt_request& q, uint32_t wave_paths) {
-    if (q.kind == CRT_REQUEST_RENDER) {
-        const size_t npix = (size_t)std::floor(q.camera->resolution[0]) * (size_t)std::floor(q.camera->resolution[1]);
-        const size_t paths = std::min<size_t>(npix * (size_t)std::max(1, q.params->max_samples),
-                                              std::max<size_t>(wave_paths, npix));
-        const size_t L = std::max<uint32_t>(q.n_lights, 1);
-        return paths * (188 + 57 * L) + npix * 45;
-    }
-    return (size_t)q.lidar->nx * q.lidar->ny * 24 + 16 * (q.lidar->nx + q.lidar->ny);
-}
 
 extern "C" int crt_batch(crt_context* ctx, const crt_request* reqs, size_t n, crt_batch_stats* stats) {
     if (!ctx || (n && !reqs)) return CRT_ERR_INVALID;

@@ -34,7 +34,6 @@ struct Pending {
     std::vector<double> quats;
     double* force = nullptr;
     double* torque = nullptr;
-    size_t footprint = 0;
     double submit_s = 0;
     void fix_pointers() {
         req.camera = &camera;
@@ -162,11 +161,6 @@ void lane_loop(crt_server* S, size_t lane) {
     }
 }
 
-size_t srp_footprint(const crt_srp_desc& d, size_t n_att) {
-    const size_t tiles = ((size_t)(d.grid + 7) / 8) * ((d.grid + 3) / 4);
-    return (tiles / 16 + 1) * 48 * std::max<size_t>(n_att, 1) + n_att * 112;
-}
-
 thread_local std::string t_submit_error;
 
 // crt_guard for the submitting thread: the message goes to a per-thread string, not to a lane's
@@ -246,7 +240,6 @@ int crt_server_submit(crt_server* S, const crt_server_request* r, uint64_t* tick
     if (!S || !r || !ticket) return CRT_ERR_INVALID;
     Pending* p = new (std::nothrow) Pending();
     if (!p) return CRT_ERR_OOM;
-    const uint32_t wave_paths = S->lanes[0]->wave_paths;
     int rc = submit_guard([&] {
         const crt_request& q = r->base;
         CRT_CHECK(q.scene && q.scene->ctx && q.scene->ctx->device == S->device, CRT_ERR_INVALID,
@@ -262,7 +255,6 @@ int crt_server_submit(crt_server* S, const crt_server_request* r, uint64_t* tick
             p->quats.assign(r->quaternions, r->quaternions + 4 * r->n_att);
             p->force = r->force;
             p->torque = r->torque;
-            p->footprint = srp_footprint(p->srp_desc, r->n_att);
         } else {
             batch_check_request(q);
             if (q.kind == CRT_REQUEST_RENDER) {
@@ -274,7 +266,6 @@ int crt_server_submit(crt_server* S, const crt_server_request* r, uint64_t* tick
                 p->lidar = *q.lidar;
             }
             p->fix_pointers();
-            p->footprint = batch_footprint(p->req, wave_paths);
         }
     });
     if (rc != CRT_OK) {

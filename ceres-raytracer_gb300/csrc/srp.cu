@@ -12,13 +12,14 @@
 // start on a grid x grid square of side 2 R_b (R_b = half diagonal of the scene box) centred on the
 // box centre, 2 R_b + 1 upstream, one ray per cell centre, power flux * cell area.
 //
-// Reduction: each persistent warp takes `chunk` tiles (8 x 4 rays each) of one attitude at a time
-// (16, fewer for small grids so that the grabs outnumber the resident warps four to one);
-// lanes accumulate force and torque in FP64, the warp reduces them with shuffles, and lane 0 writes
-// the chunk's partial sums to a slot indexed by the chunk, so the per-attitude totals (summed by
-// k_srp_reduce in a fixed order) are bitwise reproducible.  Facet powers are summed per facet within
-// a warp (FP32, at most 32 terms) and added with FP64 atomics (reproducible up to the order of
-// additions); warps whose rays all missed skip that step.
+// crt_srp runs as a wavefront on the shared persistent trace kernel (per-segment trace launches
+// into per-ray hits, then k_srp_shade; see the section below).  crt_srp_static, which may not
+// allocate, keeps the fused kernel k_srp: each persistent warp takes 16 tiles (8 x 4 rays) of one
+// attitude per grab, lanes accumulate force and torque in FP64, the warp reduces them with
+// shuffles and lane 0 writes the grab's partial sums to a slot indexed by the grab.
+// In both, per-attitude totals are summed by k_srp_reduce in a fixed order (bitwise reproducible);
+// facet powers are summed per facet within a warp (FP32, at most 32 terms) and added with FP64
+// atomics (reproducible up to the order of additions); warps whose rays all missed skip that step.
 #include "common.cuh"
 #include "trace.cuh"
 
