@@ -350,7 +350,7 @@ __global__ void k_refit(const uint32_t* __restrict__ sorted, const float4* __res
         hi = make_float4(fmaxf(ahi.x, bhi.x), fmaxf(ahi.y, bhi.y), fmaxf(ahi.z, bhi.z), 0.f);
         __stcg(&nbox[2ull * node], lo);
         __stcg(&nbox[2ull * node + 1], hi);
-        node = node == 0 ? -1 : parent[node];
+        node = parent[node];
     }
 }
 
@@ -595,6 +595,492 @@ __global__ void k_collapse(CollapseArgs A, const int2* __restrict__ frontier, ui
     A.nodes[wnode] = w;
 }
 
+// ---------------------------------------------------------------- binned-SAH topology
+// Top-down, level-synchronous binned SAH (16 bins on each axis over the centroid bounds) down to
+// segments of at most SAH_T triangles, which Karras' construction then builds (its prefix function
+// restricted to the segment).  Partitions are stable, so every segment keeps the Morton order of
+// the global sort.  Node numbering follows the binary radix tree: a segment [f, l] uses internal
+// indices f .. l - 1, and the split that puts [first, p) left and [p, last] right gets index p - 1,
+// the last position of its left part, which no segment uses; together that is exactly n - 1 nodes,
+// so the collapse consumes the tree unchanged (its root is passed explicitly).
+constexpr int SAH_BINS = 16;
+constexpr int SAH_T = 4;
+constexpr int SAH_W = 13;                               // count, box lo/hi, centroid lo/hi (fkeys)
+constexpr int SAH_TASK_WORDS = 3 * SAH_BINS * SAH_W;
+constexpr int SAH_BLOCK_ITEMS = 2048;
+
+struct SahTask {
+    int first, count;
+    float clo[3], chi[3];    // centroid bounds
+    int parent, side;        // parent split node (-1 for the root) and which child this is
+};
+
+struct SahSplit {
+    int nl;                  // triangles of the left child
+    int axis, bin;           // axis < 0: split by position (no usable centroid extent)
+    float lclo[3], lchi[3], rclo[3], rchi[3];
+};
+
+struct SahSeg {
+    int first, count, parent, side;
+};
+
+__device__ __forceinline__ int sah_bin(float c, float lo, float hi) {
+    const float ext = hi - lo;
+    if (!(ext > 0.f)) return 0;
+    const int b = (int)((c - lo) * ((float)SAH_BINS / ext));
+    return max(0, min(SAH_BINS - 1, b));
+}
+
+__global__ void k_sah_root(const uint32_t* __restrict__ keys, int n, SahTask* __restrict__ t) {
+    SahTask r;
+    r.first = 0;
+    r.count = n;
+    for (int k = 0; k < 3; ++k) {
+        r.clo[k] = fkey_inv(keys[6 + k]);
+        r.chi[k] = fkey_inv(keys[9 + k]);
+    }
+    r.parent = -1;
+    r.side = 0;
+    t[0] = r;
+}
+
+__global__ void k_sah_clear(uint32_t* __restrict__ bins, size_t words) {
+    for (size_t w = blockIdx.x * (size_t)blockDim.x + threadIdx.x; w < words; w += (size_t)gridDim.x * blockDim.x) {
+        const int k = (int)(w % SAH_W);
+        bins[w] = k == 0 ? 0u : (((k - 1) % 6) < 3 ? 0xFFFFFFFFu : 0u);
+    }
+}
+
+__device__ __forceinline__ void sah_add(uint32_t* b, const float4& lo, const float4& hi, const float4& c) {
+    atomicAdd(&b[0], 1u);
+    atomicMin(&b[1], fkey(lo.x)); atomicMin(&b[2], fkey(lo.y)); atomicMin(&b[3], fkey(lo.z));
+    atomicMax(&b[4], fkey(hi.x)); atomicMax(&b[5], fkey(hi.y)); atomicMax(&b[6], fkey(hi.z));
+    atomicMin(&b[7], fkey(c.x)); atomicMin(&b[8], fkey(c.y)); atomicMin(&b[9], fkey(c.z));
+    atomicMax(&b[10], fkey(c.x)); atomicMax(&b[11], fkey(c.y)); atomicMax(&b[12], fkey(c.z));
+}
+
+// One block per SAH_BLOCK_ITEMS positions; a block whose positions all belong to one task (tasks
+// are contiguous ranges) bins into shared memory first.
+__global__ void __launch_bounds__(256) k_sah_bin(const uint32_t* __restrict__ perm, const int* __restrict__ task_of,
+                                                 const SahTask* __restrict__ tasks, const float4* __restrict__ tbox,
+                                                 const float4* __restrict__ cen, int n, uint32_t* __restrict__ bins) {
+    __shared__ uint32_t sb[SAH_TASK_WORDS];
+    const int b0 = blockIdx.x * SAH_BLOCK_ITEMS, b1 = min(n, b0 + SAH_BLOCK_ITEMS);
+    if (b0 >= n) return;
+    const int t0 = task_of[b0], t1 = task_of[b1 - 1];
+    const bool priv = t0 >= 0 && t0 == t1;
+    if (priv) {
+        for (int w = threadIdx.x; w < SAH_TASK_WORDS; w += blockDim.x) {
+            const int k = w % SAH_W;
+            sb[w] = k == 0 ? 0u : (((k - 1) % 6) < 3 ? 0xFFFFFFFFu : 0u);
+        }
+        __syncthreads();
+    }
+    for (int i = b0 + threadIdx.x; i < b1; i += blockDim.x) {
+        const int t = task_of[i];
+        if (t < 0) continue;
+        const SahTask& T = tasks[t];
+        const uint32_t p = perm[i];
+        const float4 lo = tbox[2ull * p], hi = tbox[2ull * p + 1], c = cen[p];
+        const float cv[3] = {c.x, c.y, c.z};
+        uint32_t* base = priv ? sb : bins + (size_t)t * SAH_TASK_WORDS;
+        for (int a = 0; a < 3; ++a) sah_add(base + (a * SAH_BINS + sah_bin(cv[a], T.clo[a], T.chi[a])) * SAH_W, lo, hi, c);
+    }
+    if (priv) {
+        __syncthreads();
+        uint32_t* g = bins + (size_t)t0 * SAH_TASK_WORDS;
+        for (int w = threadIdx.x; w < SAH_TASK_WORDS; w += blockDim.x) {
+            const int k = w % SAH_W;
+            const uint32_t v = sb[w];
+            if (k == 0) {
+                if (v) atomicAdd(&g[w], v);
+            } else if (((k - 1) % 6) < 3) {
+                if (v != 0xFFFFFFFFu) atomicMin(&g[w], v);
+            } else if (v) {
+                atomicMax(&g[w], v);
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ float sah_area(const float lo[3], const float hi[3]) {
+    const float dx = hi[0] - lo[0], dy = hi[1] - lo[1], dz = hi[2] - lo[2];
+    return dx * dy + dy * dz + dz * dx;
+}
+
+// One thread per task: the cheapest of the 3 x 15 bin boundaries by surface area x count.
+__global__ void k_sah_split(const SahTask* __restrict__ tasks, int n_tasks, const uint32_t* __restrict__ bins,
+                            SahSplit* __restrict__ splits) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n_tasks) return;
+    const SahTask T = tasks[t];
+    const uint32_t* B = bins + (size_t)t * SAH_TASK_WORDS;
+    float best = 3.0e38f;
+    int ba = -1, bb = 0;
+    for (int a = 0; a < 3; ++a) {
+        if (!(T.chi[a] - T.clo[a] > 0.f)) continue;
+        // right sweep: area x count of bins [s, SAH_BINS)
+        float rcost[SAH_BINS];
+        float lo[3] = {3.0e38f, 3.0e38f, 3.0e38f}, hi[3] = {-3.0e38f, -3.0e38f, -3.0e38f};
+        uint32_t cnt = 0;
+        for (int s = SAH_BINS - 1; s >= 1; --s) {
+            const uint32_t* w = B + (a * SAH_BINS + s) * SAH_W;
+            if (w[0]) {
+                cnt += w[0];
+                for (int k = 0; k < 3; ++k) {
+                    lo[k] = fminf(lo[k], fkey_inv(w[1 + k]));
+                    hi[k] = fmaxf(hi[k], fkey_inv(w[4 + k]));
+                }
+            }
+            rcost[s] = cnt ? sah_area(lo, hi) * (float)cnt : -1.f;
+        }
+        for (int k = 0; k < 3; ++k) { lo[k] = 3.0e38f; hi[k] = -3.0e38f; }
+        cnt = 0;
+        for (int s = 1; s < SAH_BINS; ++s) {
+            const uint32_t* w = B + (a * SAH_BINS + s - 1) * SAH_W;
+            if (w[0]) {
+                cnt += w[0];
+                for (int k = 0; k < 3; ++k) {
+                    lo[k] = fminf(lo[k], fkey_inv(w[1 + k]));
+                    hi[k] = fmaxf(hi[k], fkey_inv(w[4 + k]));
+                }
+            }
+            if (cnt == 0 || rcost[s] < 0.f) continue;
+            const float c = sah_area(lo, hi) * (float)cnt + rcost[s];
+            if (c < best) {
+                best = c;
+                ba = a;
+                bb = s;
+            }
+        }
+    }
+    SahSplit S;
+    if (ba < 0) {
+        S.nl = T.count / 2;
+        S.axis = -1;
+        S.bin = 0;
+        for (int k = 0; k < 3; ++k) {
+            S.lclo[k] = S.rclo[k] = T.clo[k];
+            S.lchi[k] = S.rchi[k] = T.chi[k];
+        }
+    } else {
+        int nl = 0;
+        float llo[3] = {3.0e38f, 3.0e38f, 3.0e38f}, lhi[3] = {-3.0e38f, -3.0e38f, -3.0e38f};
+        float rlo[3] = {3.0e38f, 3.0e38f, 3.0e38f}, rhi[3] = {-3.0e38f, -3.0e38f, -3.0e38f};
+        for (int s = 0; s < SAH_BINS; ++s) {
+            const uint32_t* w = B + (ba * SAH_BINS + s) * SAH_W;
+            if (!w[0]) continue;
+            float* clo = s < bb ? llo : rlo;
+            float* chi = s < bb ? lhi : rhi;
+            if (s < bb) nl += (int)w[0];
+            for (int k = 0; k < 3; ++k) {
+                clo[k] = fminf(clo[k], fkey_inv(w[7 + k]));
+                chi[k] = fmaxf(chi[k], fkey_inv(w[10 + k]));
+            }
+        }
+        S.nl = nl;
+        S.axis = ba;
+        S.bin = bb;
+        for (int k = 0; k < 3; ++k) {
+            S.lclo[k] = llo[k];
+            S.lchi[k] = lhi[k];
+            S.rclo[k] = rlo[k];
+            S.rchi[k] = rhi[k];
+        }
+    }
+    splits[t] = S;
+}
+
+__device__ __forceinline__ bool sah_left(const SahTask& T, const SahSplit& S, int i, const float4& c) {
+    if (S.axis < 0) return i - T.first < S.nl;
+    const float cv[3] = {c.x, c.y, c.z};
+    return sah_bin(cv[S.axis], T.clo[S.axis], T.chi[S.axis]) < S.bin;
+}
+
+__global__ void k_sah_flags(const uint32_t* __restrict__ perm, const int* __restrict__ task_of,
+                            const SahTask* __restrict__ tasks, const SahSplit* __restrict__ splits,
+                            const float4* __restrict__ cen, int n, uint32_t* __restrict__ flags) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int t = task_of[i];
+    flags[i] = t >= 0 && sah_left(tasks[t], splits[t], i, cen[perm[i]]) ? 1u : 0u;
+}
+
+// child-task and segment flags: [2t] left, [2t + 1] right
+__global__ void k_sah_child_flags(const SahTask* __restrict__ tasks, const SahSplit* __restrict__ splits, int n_tasks,
+                                  uint32_t* __restrict__ tflag, uint32_t* __restrict__ sflag) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n_tasks) return;
+    const int cl = splits[t].nl, cr = tasks[t].count - cl;
+    tflag[2 * t] = cl > SAH_T;
+    tflag[2 * t + 1] = cr > SAH_T;
+    sflag[2 * t] = cl <= SAH_T;
+    sflag[2 * t + 1] = cr <= SAH_T;
+}
+
+// Split nodes and the next level's tasks / final segments.  tscan / sscan: exclusive scans of the
+// child flags; seg_base: segments found by earlier levels.
+__global__ void k_sah_emit(const SahTask* __restrict__ tasks, const SahSplit* __restrict__ splits, int n_tasks,
+                           const uint32_t* __restrict__ tflag, const uint32_t* __restrict__ tscan,
+                           const uint32_t* __restrict__ sflag, const uint32_t* __restrict__ sscan, uint32_t seg_base,
+                           SahTask* __restrict__ next, SahSeg* __restrict__ segs, int2* __restrict__ child,
+                           int2* __restrict__ range, int* __restrict__ parent) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n_tasks) return;
+    const SahTask T = tasks[t];
+    const SahSplit S = splits[t];
+    const int X = T.first + S.nl - 1;
+    range[X] = make_int2(T.first, T.first + T.count - 1);
+    parent[X] = T.parent;
+    if (T.parent >= 0) {
+        if (T.side == 0) child[T.parent].x = X;
+        else child[T.parent].y = X;
+    }
+    for (int side = 0; side < 2; ++side) {
+        const int f = side ? T.first + S.nl : T.first;
+        const int c = side ? T.count - S.nl : S.nl;
+        if (tflag[2 * t + side]) {
+            SahTask C;
+            C.first = f;
+            C.count = c;
+            for (int k = 0; k < 3; ++k) {
+                C.clo[k] = side ? S.rclo[k] : S.lclo[k];
+                C.chi[k] = side ? S.rchi[k] : S.lchi[k];
+            }
+            C.parent = X;
+            C.side = side;
+            next[tscan[2 * t + side]] = C;
+        } else if (sflag[2 * t + side]) {
+            segs[seg_base + sscan[2 * t + side]] = SahSeg{f, c, X, side};
+        }
+    }
+}
+
+__global__ void k_sah_scatter(const uint32_t* __restrict__ perm_in, uint32_t* __restrict__ perm_out,
+                              const int* __restrict__ task_in, int* __restrict__ task_out,
+                              const SahTask* __restrict__ tasks, const SahSplit* __restrict__ splits,
+                              const uint32_t* __restrict__ flags, const uint32_t* __restrict__ scan,
+                              const uint32_t* __restrict__ tflag, const uint32_t* __restrict__ tscan, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int t = task_in[i];
+    if (t < 0) {
+        perm_out[i] = perm_in[i];
+        task_out[i] = -1;
+        return;
+    }
+    const int f = tasks[t].first, nl = splits[t].nl;
+    const int lr = (int)(scan[i] - scan[f]);   // left items before i in this task
+    const bool left = flags[i] != 0;
+    const int pos = left ? f + lr : f + nl + (i - f - lr);
+    const int side = left ? 0 : 1;
+    perm_out[pos] = perm_in[i];
+    task_out[pos] = tflag[2 * t + side] ? (int)tscan[2 * t + side] : -1;
+}
+
+__global__ void k_sah_segments(const SahSeg* __restrict__ segs, int n_segs, int n, int* __restrict__ seg_lo,
+                               int* __restrict__ seg_hi, int2* __restrict__ child, int* __restrict__ parent) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n_segs) return;
+    const SahSeg S = segs[s];
+    for (int p = S.first; p < S.first + S.count; ++p) {
+        seg_lo[p] = S.first;
+        seg_hi[p] = S.first + S.count - 1;
+    }
+    const int root = S.count >= 2 ? S.first : ~S.first;
+    if (S.parent >= 0) {
+        if (S.side == 0) child[S.parent].x = root;
+        else child[S.parent].y = root;
+        parent[root >= 0 ? root : (n - 1) + ~root] = S.parent;
+    }
+}
+
+__global__ void k_gather_codes(const uint32_t* __restrict__ perm, const uint32_t* __restrict__ code_by_prim, int n,
+                               uint32_t* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = code_by_prim[perm[i]];
+}
+
+__device__ __forceinline__ int delta_seg(const uint32_t* __restrict__ code, int lo, int hi, int i, int j) {
+    if (j < lo || j > hi) return -1;
+    const uint32_t a = code[i], b = code[j];
+    if (a == b) return 32 + __clz((uint32_t)(i ^ j));
+    return __clz(a ^ b);
+}
+
+// Karras' construction inside each segment [seg_lo, seg_hi] (the last position of a segment is not
+// an internal node of it)
+__global__ void k_karras_seg(const uint32_t* __restrict__ code, int n, const int* __restrict__ seg_lo,
+                             const int* __restrict__ seg_hi, int2* __restrict__ child, int2* __restrict__ range,
+                             int* __restrict__ parent) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n - 1) return;
+    const int lo_s = seg_lo[i], hi_s = seg_hi[i];
+    if (i >= hi_s) return;
+    const int d = (delta_seg(code, lo_s, hi_s, i, i + 1) - delta_seg(code, lo_s, hi_s, i, i - 1)) >= 0 ? 1 : -1;
+    const int dmin = delta_seg(code, lo_s, hi_s, i, i - d);
+    int lmax = 2;
+    while (delta_seg(code, lo_s, hi_s, i, i + lmax * d) > dmin) lmax *= 2;
+    int l = 0;
+    for (int t = lmax / 2; t >= 1; t /= 2)
+        if (delta_seg(code, lo_s, hi_s, i, i + (l + t) * d) > dmin) l += t;
+    const int j = i + l * d;
+    const int dnode = delta_seg(code, lo_s, hi_s, i, j);
+    int s = 0, t = l;
+    do {
+        t = (t + 1) >> 1;
+        if (delta_seg(code, lo_s, hi_s, i, i + (s + t) * d) > dnode) s += t;
+    } while (t > 1);
+    const int gamma = i + s * d + min(d, 0);
+    const int lo = min(i, j), hi = max(i, j);
+    const int left = (lo == gamma) ? ~gamma : gamma;
+    const int right = (hi == gamma + 1) ? ~(gamma + 1) : gamma + 1;
+    child[i] = make_int2(left, right);
+    range[i] = make_int2(lo, hi);
+    parent[left >= 0 ? left : (n - 1) + ~left] = i;
+    parent[right >= 0 ? right : (n - 1) + ~right] = i;
+}
+
+// exclusive scan, multi-block: per-block totals, one-block scan of the totals, per-block scan
+constexpr int SCAN_ITEMS = 2048;
+__global__ void __launch_bounds__(256) k_scan_blocks(const uint32_t* __restrict__ in, uint32_t* __restrict__ out,
+                                                     uint32_t m, uint32_t* __restrict__ totals) {
+    __shared__ uint32_t part[256];
+    const uint32_t b0 = blockIdx.x * SCAN_ITEMS + threadIdx.x * 8;
+    uint32_t v[8], s = 0;
+    for (int k = 0; k < 8; ++k) {
+        v[k] = b0 + k < m ? in[b0 + k] : 0u;
+        s += v[k];
+    }
+    part[threadIdx.x] = s;
+    __syncthreads();
+    for (int off = 1; off < 256; off <<= 1) {
+        const uint32_t x = threadIdx.x >= (uint32_t)off ? part[threadIdx.x - off] : 0u;
+        __syncthreads();
+        part[threadIdx.x] += x;
+        __syncthreads();
+    }
+    uint32_t run = part[threadIdx.x] - s;
+    for (int k = 0; k < 8; ++k) {
+        if (b0 + k < m) out[b0 + k] = run;
+        run += v[k];
+    }
+    if (threadIdx.x == 255) totals[blockIdx.x] = part[255];
+}
+
+__global__ void k_scan_add(uint32_t* __restrict__ out, uint32_t m, const uint32_t* __restrict__ totals) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < m) out[i] += totals[i / SCAN_ITEMS];
+}
+
+void scan_exclusive(crt_context* ctx, const uint32_t* in, uint32_t* out, uint32_t m, uint32_t* totals) {
+    if (!m) return;
+    cudaStream_t st = ctx->stream;
+    const uint32_t nb = (m + SCAN_ITEMS - 1) / SCAN_ITEMS;
+    k_scan_blocks<<<nb, 256, 0, st>>>(in, out, m, totals);
+    check_launch(ctx, "k_scan_blocks");
+    k_scan<<<1, 1024, 0, st>>>(totals, nb);
+    check_launch(ctx, "k_scan");
+    k_scan_add<<<(m + 255) / 256, 256, 0, st>>>(out, m, totals);
+    check_launch(ctx, "k_scan_add");
+}
+
+// Binned-SAH binary tree over the Morton-sorted triangles (n > SAH_T): fills child / range / parent
+// like k_karras and writes the triangle order of the tree's leaves to `sorted` (in place of the
+// Morton order).  Returns the root's internal index.
+int sah_topology(crt_context* ctx, int n, const float4* tbox, const float4* cen, const uint32_t* keys,
+                 uint32_t* sorted, const uint32_t* code_by_prim, int2* child, int2* range, int* parent) {
+    cudaStream_t st = ctx->stream;
+    const size_t max_tasks = (size_t)n / (SAH_T + 1) + 2;
+    const size_t max_segs = (size_t)n;
+    char* mem = nullptr;
+    size_t off = 0;
+    auto take = [&](size_t bytes) { const size_t o = off; off += (bytes + 255) & ~size_t(255); return o; };
+    const size_t o_perm = take(4ull * n), o_task0 = take(4ull * n), o_task1 = take(4ull * n), o_flags = take(4ull * n),
+                 o_scan = take(4ull * n), o_tot = take(4ull * ((2 * max_tasks + n) / SCAN_ITEMS + 2)),
+                 o_tasks0 = take(sizeof(SahTask) * max_tasks), o_tasks1 = take(sizeof(SahTask) * max_tasks),
+                 o_split = take(sizeof(SahSplit) * max_tasks), o_bins = take(4ull * SAH_TASK_WORDS * max_tasks),
+                 o_tf = take(8ull * max_tasks), o_ts = take(8ull * max_tasks), o_sf = take(8ull * max_tasks),
+                 o_ss = take(8ull * max_tasks), o_segs = take(sizeof(SahSeg) * max_segs), o_lo = take(4ull * n),
+                 o_hi = take(4ull * n), o_code = take(4ull * n);
+    CRT_CUDA(cudaMalloc(&mem, off));
+    struct Free {
+        char* p;
+        ~Free() { cudaFree(p); }
+    } guard{mem};
+    uint32_t* perm[2] = {sorted, (uint32_t*)(mem + o_perm)};
+    int* task_of[2] = {(int*)(mem + o_task0), (int*)(mem + o_task1)};
+    uint32_t* flags = (uint32_t*)(mem + o_flags);
+    uint32_t* scan = (uint32_t*)(mem + o_scan);
+    uint32_t* totals = (uint32_t*)(mem + o_tot);
+    SahTask* tasks[2] = {(SahTask*)(mem + o_tasks0), (SahTask*)(mem + o_tasks1)};
+    SahSplit* splits = (SahSplit*)(mem + o_split);
+    uint32_t* bins = (uint32_t*)(mem + o_bins);
+    uint32_t *tflag = (uint32_t*)(mem + o_tf), *tscan = (uint32_t*)(mem + o_ts);
+    uint32_t *sflag = (uint32_t*)(mem + o_sf), *sscan = (uint32_t*)(mem + o_ss);
+    SahSeg* segs = (SahSeg*)(mem + o_segs);
+    int *seg_lo = (int*)(mem + o_lo), *seg_hi = (int*)(mem + o_hi);
+    uint32_t* code = (uint32_t*)(mem + o_code);
+
+    CRT_CUDA(cudaMemsetAsync(task_of[0], 0, 4ull * n, st));   // every position in task 0 (the root)
+    k_sah_root<<<1, 1, 0, st>>>(keys, n, tasks[0]);
+    check_launch(ctx, "k_sah_root");
+    int cur = 0, n_tasks = 1, root = -1;
+    uint32_t n_segs = 0;
+    for (int level = 0; n_tasks > 0; ++level) {
+        CRT_CHECK(level < 256 && (size_t)n_tasks <= max_tasks, CRT_ERR_DEVICE, "SAH build did not converge");
+        const size_t words = (size_t)n_tasks * SAH_TASK_WORDS;
+        k_sah_clear<<<(uint32_t)std::min<size_t>((words + 255) / 256, 4096), 256, 0, st>>>(bins, words);
+        check_launch(ctx, "k_sah_clear");
+        k_sah_bin<<<(n + SAH_BLOCK_ITEMS - 1) / SAH_BLOCK_ITEMS, 256, 0, st>>>(perm[cur], task_of[cur], tasks[cur],
+                                                                              tbox, cen, n, bins);
+        check_launch(ctx, "k_sah_bin");
+        k_sah_split<<<(n_tasks + 127) / 128, 128, 0, st>>>(tasks[cur], n_tasks, bins, splits);
+        check_launch(ctx, "k_sah_split");
+        k_sah_flags<<<(n + 255) / 256, 256, 0, st>>>(perm[cur], task_of[cur], tasks[cur], splits, cen, n, flags);
+        check_launch(ctx, "k_sah_flags");
+        scan_exclusive(ctx, flags, scan, (uint32_t)n, totals);
+        k_sah_child_flags<<<(n_tasks + 255) / 256, 256, 0, st>>>(tasks[cur], splits, n_tasks, tflag, sflag);
+        check_launch(ctx, "k_sah_child_flags");
+        scan_exclusive(ctx, tflag, tscan, 2u * n_tasks, totals);
+        scan_exclusive(ctx, sflag, sscan, 2u * n_tasks, totals);
+        k_sah_emit<<<(n_tasks + 255) / 256, 256, 0, st>>>(tasks[cur], splits, n_tasks, tflag, tscan, sflag, sscan, n_segs,
+                                                          tasks[cur ^ 1], segs, child, range, parent);
+        check_launch(ctx, "k_sah_emit");
+        k_sah_scatter<<<(n + 255) / 256, 256, 0, st>>>(perm[cur], perm[cur ^ 1], task_of[cur], task_of[cur ^ 1],
+                                                       tasks[cur], splits, flags, scan, tflag, tscan, n);
+        check_launch(ctx, "k_sah_scatter");
+        if (level == 0) {
+            int nl = 0;
+            CRT_CUDA(cudaMemcpyAsync(&nl, &splits[0].nl, sizeof(int), cudaMemcpyDeviceToHost, st));
+            CRT_CUDA(cudaStreamSynchronize(st));
+            root = nl - 1;
+        }
+        // next level's task count and the segment count: last exclusive-scan value + last flag
+        uint32_t h[4];
+        CRT_CUDA(cudaMemcpyAsync(&h[0], tscan + 2 * n_tasks - 1, 4, cudaMemcpyDeviceToHost, st));
+        CRT_CUDA(cudaMemcpyAsync(&h[1], tflag + 2 * n_tasks - 1, 4, cudaMemcpyDeviceToHost, st));
+        CRT_CUDA(cudaMemcpyAsync(&h[2], sscan + 2 * n_tasks - 1, 4, cudaMemcpyDeviceToHost, st));
+        CRT_CUDA(cudaMemcpyAsync(&h[3], sflag + 2 * n_tasks - 1, 4, cudaMemcpyDeviceToHost, st));
+        CRT_CUDA(cudaStreamSynchronize(st));
+        n_tasks = (int)(h[0] + h[1]);
+        n_segs += h[2] + h[3];
+        CRT_CHECK(n_segs <= max_segs, CRT_ERR_DEVICE, "SAH build: too many segments");
+        cur ^= 1;
+    }
+    if (perm[cur] != sorted)
+        CRT_CUDA(cudaMemcpyAsync(sorted, perm[cur], 4ull * n, cudaMemcpyDeviceToDevice, st));
+    k_sah_segments<<<(n_segs + 255) / 256, 256, 0, st>>>(segs, (int)n_segs, n, seg_lo, seg_hi, child, parent);
+    check_launch(ctx, "k_sah_segments");
+    k_gather_codes<<<(n + 255) / 256, 256, 0, st>>>(sorted, code_by_prim, n, code);
+    check_launch(ctx, "k_gather_codes");
+    k_karras_seg<<<(n + 254) / 256, 256, 0, st>>>(code, n, seg_lo, seg_hi, child, range, parent);
+    check_launch(ctx, "k_karras_seg");
+    CRT_CUDA(cudaStreamSynchronize(st));   // the temporaries are released on return
+    return root;
+}
+
 inline uint32_t cdiv(size_t a, uint32_t b) { return (uint32_t)((a + b - 1) / b); }
 
 }  // namespace
@@ -646,6 +1132,10 @@ void scene_build(crt_scene* s, const crt_entity_desc* ents, uint32_t n_ents) {
     CRT_CUDA(cudaMemcpyAsync(d_xf, xf.data(), sizeof(EntXform) * xf.size(), cudaMemcpyHostToDevice, st));
 
     const size_t nn = std::max<uint32_t>(n, 1);
+    // binned-SAH topology for scenes larger than one segment (the context's build setting), else
+    // Karras' radix tree over the Morton order
+    const bool sah = ctx->build_sah && n > (uint32_t)SAH_T;
+    int root_index = 0;
     // scratch layout
     float* d_xyz = (float*)ctx_scratch(ctx, SCR_BUILD0, nn * 9 * sizeof(float));
     float* d_vnin = any_vn ? (float*)ctx_scratch(ctx, SCR_BUILD1, nn * 9 * sizeof(float)) : nullptr;
@@ -660,6 +1150,7 @@ void scene_build(crt_scene* s, const crt_entity_desc* ents, uint32_t n_ents) {
     // one scratch region carved into 256-byte aligned arrays (measured first, then assigned)
     float4 *geo = nullptr, *vn = nullptr, *tbox = nullptr, *cen = nullptr, *nbox = nullptr;
     uint32_t *prim_ent = nullptr, *code_a = nullptr, *idx_a = nullptr, *code_b = nullptr, *idx_b = nullptr;
+    uint32_t* code_prim = nullptr;
     uint32_t *hist = nullptr, *flags = nullptr, *keys = nullptr;
     int2 *child = nullptr, *range = nullptr, *front = nullptr, *front_b = nullptr;
     int* parent = nullptr;
@@ -679,6 +1170,7 @@ void scene_build(crt_scene* s, const crt_entity_desc* ents, uint32_t n_ents) {
         cen = (float4*)take(nn * 16);
         code_a = (uint32_t*)take(nn * 4);
         idx_a = (uint32_t*)take(nn * 4);
+        code_prim = (uint32_t*)take(nn * 4);
         code_b = (uint32_t*)take(nn * 4);
         idx_b = (uint32_t*)take(nn * 4);
         hist = (uint32_t*)take(nb_sort * 256 * 4);
@@ -709,6 +1201,7 @@ void scene_build(crt_scene* s, const crt_entity_desc* ents, uint32_t n_ents) {
         check_launch(ctx, "k_bounds");
         k_morton<<<cdiv(n, BLOCK), BLOCK, 0, st>>>(cen, n, keys, code_a, idx_a);
         check_launch(ctx, "k_morton");
+        if (sah) CRT_CUDA(cudaMemcpyAsync(code_prim, code_a, 4ull * n, cudaMemcpyDeviceToDevice, st));
         const uint32_t nb = cdiv(n, SORT_TILE);
         uint32_t *ka = code_a, *va = idx_a, *kb = code_b, *vb = idx_b;
         for (int shift = 0; shift < 32; shift += 8) {
@@ -722,7 +1215,9 @@ void scene_build(crt_scene* s, const crt_entity_desc* ents, uint32_t n_ents) {
             std::swap(va, vb);
         }
         // after 4 passes the sorted data is back in (code_a, idx_a)
-        if (n > 1) {
+        if (sah) {
+            root_index = sah_topology(ctx, (int)n, tbox, cen, keys, va, code_prim, child, range, parent);
+        } else if (n > 1) {
             k_karras<<<cdiv(n - 1, BLOCK), BLOCK, 0, st>>>(ka, (int)n, child, range, parent);
             check_launch(ctx, "k_karras");
         }
@@ -741,7 +1236,7 @@ void scene_build(crt_scene* s, const crt_entity_desc* ents, uint32_t n_ents) {
     uint32_t* counters = keys + 16;
     const uint32_t c0[3] = {1, 0, 0};
     CRT_CUDA(cudaMemcpyAsync(counters, c0, sizeof(c0), cudaMemcpyHostToDevice, st));
-    int2 root = make_int2(n > 3 ? 0 : 0x7FFFFFFF, 0);
+    int2 root = make_int2(n > 3 ? root_index : 0x7FFFFFFF, 0);
     CRT_CUDA(cudaMemcpyAsync(front, &root, sizeof(root), cudaMemcpyHostToDevice, st));
 
     CollapseArgs A;

@@ -85,6 +85,7 @@ struct crt_context {
     uint32_t queue_chunk = 1;        // 32-item groups per atomic grab of the ray queue
     uint32_t wave_paths = 1u << 23;  // render paths per wavefront wave
     int use_graphs = 1;              // replay batched waves as CUDA graphs
+    int build_sah = 1;               // scene builds: binned-SAH topology (1) or Karras radix tree (0)
     // graph cache of the batched wavefront (one executable per wave shape)
     void* graph_exec = nullptr;
     uint64_t graph_key = 0;

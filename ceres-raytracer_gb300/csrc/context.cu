@@ -244,6 +244,7 @@ int crt_context_set_tuning(crt_context* ctx, const crt_tuning* t) {
     ctx->queue_chunk = t->queue_chunk;
     ctx->wave_paths = t->wave_paths;
     ctx->use_graphs = t->use_graphs ? 1 : 0;
+    ctx->build_sah = t->build_sah ? 1 : 0;
     return CRT_OK;
 }
 
@@ -252,6 +253,7 @@ int crt_context_get_tuning(const crt_context* ctx, crt_tuning* out) {
     out->queue_chunk = ctx->queue_chunk;
     out->wave_paths = ctx->wave_paths;
     out->use_graphs = ctx->use_graphs;
+    out->build_sah = ctx->build_sah;
     return CRT_OK;
 }
 

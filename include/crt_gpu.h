@@ -159,6 +159,8 @@ typedef struct {
     uint32_t queue_chunk;                 /* max 32-ray groups per atomic grab (1..8), guided by the work left */
     uint32_t wave_paths;                  /* camera paths per wave (>= 65536) */
     int use_graphs;                       /* replay batched waves as CUDA graphs */
+    int build_sah;                        /* scenes built afterwards: binned-SAH tree (1, default) or
+                                             Karras radix tree over the Morton order (0, faster build) */
 } crt_tuning;
 
 typedef struct {
