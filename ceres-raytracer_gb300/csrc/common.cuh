@@ -270,13 +270,27 @@ struct CamBasis {
 // Distance along an FP64 ray (o, d) to the plane of the FP32 triangle stored at leaf `slot`
 // (p0 and n of the record): the traversal picks the triangle in FP32, the reported hit point and
 // range are then evaluated along the FP64 ray of the FP64 pose, as the reference evaluates them.
+// FP64 reciprocal and inverse square root from an FP32 seed and one Newton-Raphson step
+// (y <- y (2 - x y), y <- y (3 - x y^2) / 2): the seed's relative error e becomes about e^2, i.e.
+// ~1e-14, far below the 1e-5 the FP64 epilogues need, for a few FP64 fused multiply-adds instead of
+// a full-precision FP64 division or square root (GB300 runs FP64 at a small fraction of its FP32
+// rate).  Inputs outside the FP32 normal range give a non-finite result; callers test isfinite.
+__device__ __forceinline__ double rcp64(double x) {
+    const double y = (double)__frcp_rn((float)x);
+    return y * fma(-x, y, 2.0);
+}
+__device__ __forceinline__ double rsqrt64(double x) {
+    const double y = (double)rsqrtf((float)x);
+    return y * fma(-0.5 * x, y * y, 1.5);
+}
+
 __device__ __forceinline__ double plane_t64(const float4* __restrict__ tris, uint32_t slot, const double o[3],
                                             const double d[3]) {
     const float4 a = __ldg(tris + 3ull * slot), c = __ldg(tris + 3ull * slot + 2);
     const double n0 = c.y, n1 = c.z, n2 = c.w;
     const double den = n0 * d[0] + n1 * d[1] + n2 * d[2];
     const double num = n0 * ((double)a.x - o[0]) + n1 * ((double)a.y - o[1]) + n2 * ((double)a.z - o[2]);
-    return num / den;
+    return num * rcp64(den);
 }
 
 // Barycentric u, v of the FP64 ray (o, d) on the FP32 triangle at leaf `slot`, with the reference's
@@ -289,7 +303,7 @@ __device__ __forceinline__ bool bary64(const float4* __restrict__ tris, uint32_t
     const double r[3] = {d[1] * c[2] - d[2] * c[1], d[2] * c[0] - d[0] * c[2], d[0] * c[1] - d[1] * c[0]};
     const double det = n[0] * d[0] + n[1] * d[1] + n[2] * d[2];
     if (det == 0.0) return false;
-    const double inv = 1.0 / det;
+    const double inv = rcp64(det);
     u = (r[0] * e2[0] + r[1] * e2[1] + r[2] * e2[2]) * inv;
     v = (r[0] * e1[0] + r[1] * e1[1] + r[2] * e1[2]) * inv;
     return isfinite(u) && isfinite(v);

@@ -178,7 +178,7 @@ struct PrimaryJob {
     __device__ SceneView view(const SceneView&, const Item& it) const { return it.lidar ? B.lr[it.req].sv : B.rr[it.req].sv; }
     __device__ void beam64(const LReq& L, uint32_t px, uint32_t py, double d[3]) const {
         const double s0 = B.tan[L.tan_base + px], s1 = B.tan[L.tan_base + L.nx + py], s2 = L.zsign;
-        const double inv = 1.0 / sqrt(s0 * s0 + s1 * s1 + s2 * s2);
+        const double inv = rsqrt64(s0 * s0 + s1 * s1 + s2 * s2);
         for (int k = 0; k < 3; ++k) d[k] = (L.rt[3 * k] * s0 + L.rt[3 * k + 1] * s1 + L.rt[3 * k + 2] * s2) * inv;
     }
     __device__ bool ray(uint32_t i, TRay& r, Item& it) const {

@@ -93,7 +93,7 @@ struct PassJob : JobBase {
                     o[k] = cam.o64[k];
                     d[k] = cam.a64[k] + (double)px * cam.b64[k] + (double)py * cam.c64[k];
                 }
-                const double inv = 1.0 / sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+                const double inv = rsqrt64(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
                 for (int k = 0; k < 3; ++k) d[k] *= inv;
                 if (xyz) {
                     double t = plane_t64(sv.tris, h.slot, o, d);
@@ -110,7 +110,7 @@ struct PassJob : JobBase {
                         n64[0] = u * v1.x + v * v2.x + w * v0.x;
                         n64[1] = u * v1.y + v * v2.y + w * v0.y;
                         n64[2] = u * v1.z + v * v2.z + w * v0.z;
-                        const double l = 1.0 / sqrt(n64[0] * n64[0] + n64[1] * n64[1] + n64[2] * n64[2]);
+                        const double l = rsqrt64(n64[0] * n64[0] + n64[1] * n64[1] + n64[2] * n64[2]);
                         for (int k = 0; k < 3; ++k) n64[k] *= l;
                     } else {
                         n64[0] = nrm.x; n64[1] = nrm.y; n64[2] = nrm.z;
@@ -153,7 +153,9 @@ struct LidarBatchJob : JobBase {
             const double o[3] = {pos[3ull * i], pos[3ull * i + 1], pos[3ull * i + 2]};
             const double d[3] = {zsign * rot[9ull * i + 6], zsign * rot[9ull * i + 7], zsign * rot[9ull * i + 8]};
             const double t = plane_t64(sv.tris, h.slot, o, d);
-            rng = isfinite(t) ? t * sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]) : (double)h.t;
+            const double q = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+            const double len = q * rsqrt64(q);
+            rng = isfinite(t) && isfinite(len) ? t * len : (double)h.t;
         }
         range[i] = rng;
         if (prim) prim[i] = h.slot != CRT_MISS ? sv.leaf_prim[h.slot] : CRT_MISS;
@@ -171,7 +173,7 @@ struct LidarGridJob : JobBase {
     uint32_t* prim;
     __device__ void beam64(uint32_t px, uint32_t py, double d[3]) const {
         const double s0 = tx[px], s1 = ty[py], s2 = zsign;
-        const double inv = 1.0 / sqrt(s0 * s0 + s1 * s1 + s2 * s2);
+        const double inv = rsqrt64(s0 * s0 + s1 * s1 + s2 * s2);
         for (int k = 0; k < 3; ++k) d[k] = (rt[3 * k] * s0 + rt[3 * k + 1] * s1 + rt[3 * k + 2] * s2) * inv;
     }
     __device__ bool ray(uint32_t i, TRay& r, Item&) const {
