@@ -57,6 +57,7 @@ def parse():
     ap.add_argument("--served-wave-paths", type=int, default=1 << 22)
     ap.add_argument("--served-budget-mib", type=int, default=4096)
     ap.add_argument("--no-srp", action="store_true")
+    ap.add_argument("--no-cornell", action="store_true")
     ap.add_argument("--srp-attitudes", type=int, default=256)
     ap.add_argument("--probe", type=int, default=0,
                     help="profiling aid: only run the --probe-kind workload this many times")
@@ -407,6 +408,10 @@ def gpu_arm(args):
     if not args.no_srp and rank == 0:
         srp = srp_measure(args, ctx, stream)
 
+    cornell = None
+    if not args.no_cornell and rank == 0:
+        cornell = cornell_measure(ctx, stream, cpu=not args.no_cpu)
+
     served = None
     if not args.no_served and rank == 0:
         served = served_measure(args, local)
@@ -432,7 +437,7 @@ def gpu_arm(args):
                                "lidar_p50": round(percentile(lat_lidar, 50), 3),
                                "lidar_p99": round(percentile(lat_lidar, 99), 3)},
                 "roofline": roof, "gpu_launches": int(launches), "clocks": clk, "e2e": e2e, "batched": batched,
-                "served": served, "srp": srp}
+                "served": served, "srp": srp, "cornell": cornell}
         if world == 1 and not args.no_cpu:
             mr, det = cpu_measure(ents, cfg, args.cpu_seconds)
             line["cpu_baseline"] = {"value": round(mr, 3), "unit": UNIT, "cores": det["cores"], "kind": "port",
@@ -643,6 +648,59 @@ def served_measure(args, device):
                            "speedup": round(cspan_p / cspan_s, 3)},
            "body_generation_s": round(t_gen, 1)}
     srv.close()
+    return out
+
+
+def cornell_measure(ctx, stream, cpu=True):
+    """Cornell box (36 triangles): 256^2 render, 16 spp, 3 bounces, area light, seed 0, and the
+    depth / normal / instance passes -- on the GPU (CUDA events, device outputs) and, for the render,
+    the CPU oracle on all host cores (same Philox streams, so the same paths and ray count)."""
+    import torch
+    from crt_gb300 import scenes
+    ents, cam, lights = scenes.cornell()
+    sc = ctx.scene(ents)
+    W, H = int(cam["resolution"][0]), int(cam["resolution"][1])
+    dev = torch.device("cuda", torch.cuda.current_device())
+    rgba = torch.empty((H, W, 4), dtype=torch.uint8, device=dev)
+    xyz = torch.empty((H, W, 3), dtype=torch.float64, device=dev)
+    ids = torch.empty((H, W), dtype=torch.int32, device=dev)
+    nrm = torch.empty((H, W, 3), dtype=torch.float64, device=dev)
+
+    def render():
+        sc.render(cam, lights, 16, 16, 0.0, 3, seed=0, want_radiance=False, out_rgba=rgba)
+
+    def passes():
+        sc.passes(cam, xyz=xyz, ids=ids, normals=nrm)
+
+    with torch.cuda.stream(stream):
+        ctx.reset_counters()
+        ctx.set_counting(True)
+        render()
+        rays = int(ctx.counters()["rays"])
+        ctx.set_counting(False)
+        times = {}
+        for name, fn, reps in (("render", render, 10), ("passes", passes, 20)):
+            fn()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            for _ in range(reps):
+                fn()
+            b.record(stream)
+            torch.cuda.synchronize()
+            times[name] = a.elapsed_time(b) / reps
+    out = {"workload": "Cornell box 36 triangles: render %dx%d, 16 spp, 3 bounces, area light, seed 0; "
+                       "depth + normal + instance passes" % (W, H),
+           "rays": rays, "gpu_render_ms": round(times["render"], 3), "gpu_passes_ms": round(times["passes"], 3),
+           "gpu_mrays_s": round(rays / times["render"] / 1e3, 1)}
+    if cpu:
+        import oracle
+        o = oracle.Scene(ents, nthreads=os.cpu_count() or 1)
+        t = time.perf_counter()
+        o.render(cam, lights, 16, 16, 0.0, 3, seed=0)
+        cs = time.perf_counter() - t
+        out.update(cpu_render_s=round(cs, 3), cpu_mrays_s=round(rays / cs / 1e6, 2), cpu_cores=os.cpu_count() or 1,
+                   gpu_speedup=round(cs * 1e3 / times["render"], 1))
+    sc.close()
     return out
 
 

@@ -389,9 +389,11 @@ class Scene:
     def passes(self, cam, xyz=True, ids=True, normals=True):
         c = fill_camera(cam)
         W, H = int(np.floor(cam["resolution"][0])), int(np.floor(cam["resolution"][1]))
-        ox = np.empty((H, W, 3)) if xyz is True else (xyz or None)
-        oi = np.empty((H, W), np.uint32) if ids is True else (ids or None)
-        on = np.empty((H, W, 3)) if normals is True else (normals or None)
+        def out(a, shape, dtype=np.float64):   # True: allocate; False / None: skip; else caller buffer
+            return np.empty(shape, dtype) if a is True else (None if a is None or a is False else a)
+        ox = out(xyz, (H, W, 3))
+        oi = out(ids, (H, W), np.uint32)
+        on = out(normals, (H, W, 3))
         self.ctx._check(self.ctx.L.crt_passes(self.h, ctypes.byref(c), ptr(ox), ptr(oi), ptr(on)))
         return ox, oi, on
 
