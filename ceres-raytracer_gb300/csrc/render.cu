@@ -7,7 +7,8 @@
 //   primary   LiDAR beams of the batch + camera ray per (pixel, sample)       (persistent trace)
 //   shade     surface point, one shadow ray per light, bounce ray             (k_shade)
 //   shadow    any hit for the shadow queue                                     (persistent trace)
-//   accum     sum lights, clamp after the first bounce, times path weight      (k_accum)
+//   accum     sum lights, clamp after the first bounce, times path weight      (k_accum; folded into
+//             k_update when the wave's only bounce is bounce 0)
 //   bounce    closest hit for the continuing-path queue                        (persistent trace)
 //   update    per-pixel running mean and adaptive stop, samples in order       (k_update)
 //   finalize  RGBA float and clamp(v * 256, 0, 255) bytes per request          (k_finalize)
@@ -397,6 +398,26 @@ __global__ void k_shade(Batch B, int bounce, const uint32_t* __restrict__ q_in, 
 }
 
 // ---------------------------------------------------------------- accumulate
+// Light reaching path p's current vertex (unidirectional.hpp:62-80): the unoccluded contributions
+// in light order, clamped to [0, 1] after the first bounce, times the path weight.  Shared by
+// k_accum and the fused accumulate of k_update, with explicit roundings, so both give the same bits.
+__device__ __forceinline__ float4 add_light(const Batch& B, uint32_t p, uint32_t n_lights, int bounce, float4 r) {
+    float3 lr = f3(0.f, 0.f, 0.f);
+    for (uint32_t l = 0; l < n_lights; ++l) {
+        if (!B.occ[(size_t)p * B.L + l]) {
+            const float4 cb = B.contrib[(size_t)p * B.L + l];
+            lr = f3(__fadd_rn(lr.x, cb.x), __fadd_rn(lr.y, cb.y), __fadd_rn(lr.z, cb.z));
+        }
+    }
+    if (bounce >= 1) {   // unidirectional.hpp:74-78
+        lr.x = fminf(fmaxf(lr.x, 0.f), 1.f);
+        lr.y = fminf(fmaxf(lr.y, 0.f), 1.f);
+        lr.z = fminf(fmaxf(lr.z, 0.f), 1.f);
+    }
+    const float4 wa = B.wacc[p];
+    return make_float4(__fmaf_rn(lr.x, wa.x, r.x), __fmaf_rn(lr.y, wa.y, r.y), __fmaf_rn(lr.z, wa.z, r.z), 0.f);
+}
+
 __global__ void k_accum(Batch B, int bounce, const uint32_t* __restrict__ q_in) {
     const uint32_t n = bounce == 0 ? B.cur->n_paths : B.counts[0];
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -404,25 +425,13 @@ __global__ void k_accum(Batch B, int bounce, const uint32_t* __restrict__ q_in) 
         if (__float_as_uint(B.hit[p].w) == CRT_MISS) continue;
         const RReq& R = B.rr[B.preq[p]];
         if (bounce >= R.c.num_bounces) continue;
-        float3 lr = f3(0.f, 0.f, 0.f);
-        for (uint32_t l = 0; l < R.n_lights; ++l) {
-            if (!B.occ[(size_t)p * B.L + l]) {
-                const float4 cb = B.contrib[(size_t)p * B.L + l];
-                lr = lr + f3(cb.x, cb.y, cb.z);
-            }
-        }
-        if (bounce >= 1) {   // unidirectional.hpp:74-78
-            lr.x = fminf(fmaxf(lr.x, 0.f), 1.f);
-            lr.y = fminf(fmaxf(lr.y, 0.f), 1.f);
-            lr.z = fminf(fmaxf(lr.z, 0.f), 1.f);
-        }
-        const float4 wa = B.wacc[p];
-        const float4 r = B.rad[p];
-        B.rad[p] = make_float4(r.x + lr.x * wa.x, r.y + lr.y * wa.y, r.z + lr.z * wa.z, 0.f);
+        B.rad[p] = add_light(B, p, R.n_lights, bounce, B.rad[p]);
     }
 }
 
 // ---------------------------------------------------------------- pixel update (do_render.hpp:84-114)
+// ACC0: the wave's only bounce is bounce 0 and its light is added here instead of by k_accum
+template <bool ACC0>
 __global__ void k_update(Batch B) {
     const WaveDesc& w = *B.cur;
     for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < w.n_update; u += gridDim.x * blockDim.x) {
@@ -442,7 +451,10 @@ __global__ void k_update(Batch B) {
         uint32_t t = B.taken[g];
         for (uint32_t k = 0; k < S.ns; ++k) {
             const uint32_t sample = S.s0 + k + 1;   // 1-based as in the reference loop
-            const float4 L = B.rad[(size_t)S.path_base + (size_t)k * S.npix + a];
+            const size_t p = (size_t)S.path_base + (size_t)k * S.npix + a;
+            float4 L = B.rad[p];
+            if (ACC0 && R.c.num_bounces > 0 && __float_as_uint(B.hit[p].w) != CRT_MISS)
+                L = add_light(B, (uint32_t)p, R.n_lights, 0, L);
             const float inv = 1.0f / (float)sample;
             const float dx = (L.x - m.x) * inv, dy = (L.y - m.y) * inv, dz = (L.z - m.z) * inv;
             m.x += dx; m.y += dy; m.z += dz;
@@ -530,13 +542,16 @@ void launch_wave_kernels(crt_context* ctx, const Batch& B, size_t P, size_t NL, 
                         &B.cur->n_primary, tqueue);
     const uint32_t* q_in = nullptr;
     uint32_t* q_out = qa;
+    const bool fuse = max_bounces == 1;   // k_update adds the light of the only bounce
     for (int b = 0; b < max_bounces; ++b) {
         k_shade<<<gsz, 256, 0, st>>>(B, b, q_in, q_out);
         check_launch(ctx, "k_shade");
         launch_trace<true>(ctx, SceneView{}, ShadowJob{B}, (uint32_t)std::min<size_t>(P * NL, 0xFFFFFF00u),
                            &B.counts[2], tqueue);
-        k_accum<<<gsz, 256, 0, st>>>(B, b, q_in);
-        check_launch(ctx, "k_accum");
+        if (!fuse) {
+            k_accum<<<gsz, 256, 0, st>>>(B, b, q_in);
+            check_launch(ctx, "k_accum");
+        }
         if (b < max_bounces - 1) {
             launch_trace<false>(ctx, SceneView{}, BounceJob{B, q_out}, (uint32_t)P, &B.counts[1], tqueue);
             k_queue_rotate<<<1, 1, 0, st>>>(B.counts);
@@ -545,7 +560,8 @@ void launch_wave_kernels(crt_context* ctx, const Batch& B, size_t P, size_t NL, 
             q_out = (q_out == qa) ? qb : qa;
         }
     }
-    k_update<<<gsz, 256, 0, st>>>(B);
+    if (fuse) k_update<true><<<gsz, 256, 0, st>>>(B);
+    else k_update<false><<<gsz, 256, 0, st>>>(B);
     check_launch(ctx, "k_update");
     k_wave_end<<<1, 1, 0, st>>>(B);
     check_launch(ctx, "k_wave_end");
