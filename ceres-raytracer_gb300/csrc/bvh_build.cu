@@ -10,11 +10,12 @@
 //   radix_sort       stable LSD radix sort, 8-bit digits, 4 passes (histogram / scan / scatter)
 //   k_karras         binary radix tree (Karras, "Maximizing parallelism in the construction of
 //                    BVHs, octrees, and k-d trees", HPG 2012); ties broken by index
-//   k_refit          bottom-up boxes, second arrival at each node does the union
-//   k_collapse       top-down, level-synchronous collapse into 8-wide nodes: greedily open the
-//                    largest-area child of more than 3 triangles until 8 slots are used (then
-//                    split small leaves into free slots), children with <= 3 triangles become
-//                    leaves, slots ordered by octant, child boxes quantised to 8 bits
+//   k_refit          bottom-up boxes and collapse costs, second arrival at each node does the
+//                    union
+//   k_collapse       top-down, level-synchronous collapse into 8-wide nodes by a surface-area
+//                    cost dynamic program over the binary tree (costs computed in the refit:
+//                    each wide node spreads its 8 slots over subtrees where that is cheaper than
+//                    keeping them whole); children with <= 3 triangles become leaves, slots ordered by octant, child boxes quantised to 8 bits
 //                    (Ylitie, Karras, Laine, "Efficient incoherent ray traversal on GPUs through
 //                    compressed wide BVHs", HPG 2017); leaf triangles written contiguously.
 #include "common.cuh"
@@ -326,11 +327,37 @@ __global__ void k_karras(const uint32_t* __restrict__ code, int n, int2* __restr
     parent[right >= 0 ? right : (n - 1) + ~right] = i;
 }
 
-// ---------------------------------------------------------------- refit
+// ---------------------------------------------------------------- refit + collapse costs
+// Surface-area costs for the 8-wide collapse (a dynamic program over the binary tree): for an
+// internal node b, dp[8 b] = cost of b as one root of a wide node's slot (a leaf when it holds at
+// most 3 triangles, else an 8-wide node: COST_NODE area + the best spread of 8 slots over its
+// children), dp[8 b + j - 1] = cost of spreading j = 2..8 slots over its two children.  The ratio
+// COST_TRI : COST_NODE is the measured instruction cost of a triangle test against an 8-wide node
+// test in the trace kernel (~40 : ~280).
+constexpr float COST_NODE = 1.0f, COST_TRI = 0.15f;
+
+__device__ __forceinline__ float box_area(const float4& lo, const float4& hi) {
+    const float dx = hi.x - lo.x, dy = hi.y - lo.y, dz = hi.z - lo.z;
+    return dx * dy + dy * dz + dz * dx;
+}
+
+// cost of child `ref` given i slots (1..8): out[i]
+__device__ __forceinline__ void dp_child(const float* __restrict__ dp, int ref, float leaf_area, float out[9]) {
+    if (ref < 0) {
+        const float v = COST_TRI * leaf_area;
+        for (int i = 1; i <= 8; ++i) out[i] = v;
+        return;
+    }
+    const float* d = dp + 8ull * ref;
+    const float single = __ldcg(d);
+    out[1] = single;
+    for (int i = 2; i <= 8; ++i) out[i] = fminf(single, __ldcg(d + i - 1));
+}
+
 // node boxes: 2 float4 per node; internal nodes [0, n-1), leaves [n-1, 2n-1)
 __global__ void k_refit(const uint32_t* __restrict__ sorted, const float4* __restrict__ tbox, int n,
                         const int2* __restrict__ child, const int* __restrict__ parent, float4* nbox,
-                        uint32_t* __restrict__ flags) {
+                        uint32_t* __restrict__ flags, const int2* __restrict__ range, float* __restrict__ dp) {
     int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n) return;
     const uint32_t p = sorted[j];
@@ -350,6 +377,24 @@ __global__ void k_refit(const uint32_t* __restrict__ sorted, const float4* __res
         hi = make_float4(fmaxf(ahi.x, bhi.x), fmaxf(ahi.y, bhi.y), fmaxf(ahi.z, bhi.z), 0.f);
         __stcg(&nbox[2ull * node], lo);
         __stcg(&nbox[2ull * node + 1], hi);
+        if (dp) {
+            float cl[9], cr[9];
+            dp_child(dp, c.x, box_area(alo, ahi), cl);
+            dp_child(dp, c.y, box_area(blo, bhi), cr);
+            float* out = dp + 8ull * node;
+            float dist8 = 3.0e38f;
+            for (int j = 2; j <= 8; ++j) {
+                float best = 3.0e38f;
+                for (int k = 1; k < j; ++k) best = fminf(best, cl[k] + cr[j - k]);
+                __stcg(out + j - 1, best);
+                dist8 = best;
+            }
+            const int2 r = range[node];
+            const float a = box_area(lo, hi);
+            const float c_int = COST_NODE * a + dist8;
+            const float c_leaf = r.y - r.x + 1 <= 3 ? COST_TRI * (float)(r.y - r.x + 1) * a : 3.0e38f;
+            __stcg(out, fminf(c_int, c_leaf));
+        }
         node = parent[node];
     }
 }
@@ -372,6 +417,7 @@ struct CollapseArgs {
     uint32_t* counters;           // [0] wide nodes used, [1] triangles placed, [2] next frontier size
     uint32_t node_cap;
     uint32_t* err;
+    const float* dp;              // collapse costs from k_refit
 };
 
 __device__ __forceinline__ size_t box_index(int n, int ref) { return ref >= 0 ? (size_t)ref : (size_t)(n - 1 + ~ref); }
@@ -419,33 +465,35 @@ __global__ void k_collapse(CollapseArgs A, const int2* __restrict__ frontier, ui
         nc = n > 0 ? 1 : 0;
         refs[0] = 0x7FFFFFFF;
     } else {
-        int2 c = A.child[bnode];
-        refs[0] = c.x;
-        refs[1] = c.y;
-        nc = 2;
-        // open the largest-area child that would otherwise become an internal node (> 3 triangles);
-        // only when none is left, split small leaves to fill the remaining slots
-        while (nc < 8) {
-            int best = -1;
-            bool best_big = false;
-            float best_area = -1.f;
-            for (int k = 0; k < nc; ++k) {
-                if (refs[k] < 0) continue;     // leaf of the binary tree: cannot open
-                const bool big = ref_count(A, refs[k]) > 3;
-                const size_t bi = box_index(n, refs[k]);
-                const float4 lo = A.nbox[2 * bi], hi = A.nbox[2 * bi + 1];
-                const float dx = hi.x - lo.x, dy = hi.y - lo.y, dz = hi.z - lo.z;
-                const float area = dx * dy + dy * dz + dz * dx;
-                if ((big && !best_big) || (big == best_big && area > best_area)) {
-                    best_area = area;
-                    best = k;
-                    best_big = big;
+        // expand by the cost decisions: a child given k slots stays one root (a leaf or an 8-wide
+        // node) unless spreading its k slots over its own children is cheaper
+        int sr[8], sk[8], sp = 0;
+        sr[sp] = bnode;
+        sk[sp++] = 8;
+        while (sp) {
+            --sp;
+            const int r = sr[sp], k = sk[sp];
+            if (r != bnode && (r < 0 || k == 1 || !(__ldg(A.dp + 8ull * r + k - 1) < __ldg(A.dp + 8ull * r)))) {
+                refs[nc++] = r;
+                continue;
+            }
+            const int2 c = A.child[r];
+            float cl[9], cr[9];
+            dp_child(A.dp, c.x, c.x < 0 ? box_area(A.nbox[2 * box_index(n, c.x)], A.nbox[2 * box_index(n, c.x) + 1]) : 0.f, cl);
+            dp_child(A.dp, c.y, c.y < 0 ? box_area(A.nbox[2 * box_index(n, c.y)], A.nbox[2 * box_index(n, c.y) + 1]) : 0.f, cr);
+            int bk = 1;
+            float best = 3.0e38f;
+            for (int kk = 1; kk < k; ++kk) {
+                const float v = cl[kk] + cr[k - kk];
+                if (v < best) {
+                    best = v;
+                    bk = kk;
                 }
             }
-            if (best < 0) break;
-            const int2 c2 = A.child[refs[best]];
-            refs[best] = c2.x;
-            refs[nc++] = c2.y;
+            sr[sp] = c.y;
+            sk[sp++] = k - bk;
+            sr[sp] = c.x;
+            sk[sp++] = bk;
         }
     }
 
@@ -1151,6 +1199,7 @@ void scene_build(crt_scene* s, const crt_entity_desc* ents, uint32_t n_ents) {
     float4 *geo = nullptr, *vn = nullptr, *tbox = nullptr, *cen = nullptr, *nbox = nullptr;
     uint32_t *prim_ent = nullptr, *code_a = nullptr, *idx_a = nullptr, *code_b = nullptr, *idx_b = nullptr;
     uint32_t* code_prim = nullptr;
+    float* dpc = nullptr;
     uint32_t *hist = nullptr, *flags = nullptr, *keys = nullptr;
     int2 *child = nullptr, *range = nullptr, *front = nullptr, *front_b = nullptr;
     int* parent = nullptr;
@@ -1179,6 +1228,7 @@ void scene_build(crt_scene* s, const crt_entity_desc* ents, uint32_t n_ents) {
         parent = (int*)take(nn * 8);          // 2n - 1 entries: internal nodes then leaves
         flags = (uint32_t*)take(nn * 4);
         nbox = (float4*)take(nn * 64);        // 2n - 1 nodes x (lo, hi)
+        dpc = (float*)take(nn * 32);          // collapse costs: 8 per internal node
         keys = (uint32_t*)take(64 * 4);
         front = (int2*)take(nn * 8 + 8);
         front_b = (int2*)take(nn * 8 + 8);
@@ -1221,7 +1271,7 @@ void scene_build(crt_scene* s, const crt_entity_desc* ents, uint32_t n_ents) {
             k_karras<<<cdiv(n - 1, BLOCK), BLOCK, 0, st>>>(ka, (int)n, child, range, parent);
             check_launch(ctx, "k_karras");
         }
-        k_refit<<<cdiv(n, BLOCK), BLOCK, 0, st>>>(va, tbox, (int)n, child, parent, nbox, flags);
+        k_refit<<<cdiv(n, BLOCK), BLOCK, 0, st>>>(va, tbox, (int)n, child, parent, nbox, flags, range, dpc);
         check_launch(ctx, "k_refit");
         idx_a = va;
     }
@@ -1256,6 +1306,7 @@ void scene_build(crt_scene* s, const crt_entity_desc* ents, uint32_t n_ents) {
     A.counters = counters;
     A.node_cap = cap;
     A.err = ctx->d_error;
+    A.dp = dpc;
 
     uint32_t fcount = 1, depth = 0;
     int2 *cur = front, *nxt = front_b;
