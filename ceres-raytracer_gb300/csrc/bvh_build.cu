@@ -332,9 +332,10 @@ __global__ void k_karras(const uint32_t* __restrict__ code, int n, int2* __restr
 // internal node b, dp[8 b] = cost of b as one root of a wide node's slot (a leaf when it holds at
 // most 3 triangles, else an 8-wide node: COST_NODE area + the best spread of 8 slots over its
 // children), dp[8 b + j - 1] = cost of spreading j = 2..8 slots over its two children.  The ratio
-// COST_TRI : COST_NODE is the measured instruction cost of a triangle test against an 8-wide node
-// test in the trace kernel (~40 : ~280).
-constexpr float COST_NODE = 1.0f, COST_TRI = 0.15f;
+// triangle-test cost `cost_tri` is relative to an 8-wide node test (COST_NODE = 1): the default
+// 0.15 is the trace kernel's instruction ratio (~40 : ~280), best for coherent rays; incoherent
+// multi-bounce workloads prefer smaller leaves (a larger cost, crt_tuning.collapse_tri_cost).
+constexpr float COST_NODE = 1.0f;
 
 __device__ __forceinline__ float box_area(const float4& lo, const float4& hi) {
     const float dx = hi.x - lo.x, dy = hi.y - lo.y, dz = hi.z - lo.z;
@@ -342,9 +343,10 @@ __device__ __forceinline__ float box_area(const float4& lo, const float4& hi) {
 }
 
 // cost of child `ref` given i slots (1..8): out[i]
-__device__ __forceinline__ void dp_child(const float* __restrict__ dp, int ref, float leaf_area, float out[9]) {
+__device__ __forceinline__ void dp_child(const float* __restrict__ dp, int ref, float leaf_area, float cost_tri,
+                                         float out[9]) {
     if (ref < 0) {
-        const float v = COST_TRI * leaf_area;
+        const float v = cost_tri * leaf_area;
         for (int i = 1; i <= 8; ++i) out[i] = v;
         return;
     }
@@ -357,7 +359,8 @@ __device__ __forceinline__ void dp_child(const float* __restrict__ dp, int ref, 
 // node boxes: 2 float4 per node; internal nodes [0, n-1), leaves [n-1, 2n-1)
 __global__ void k_refit(const uint32_t* __restrict__ sorted, const float4* __restrict__ tbox, int n,
                         const int2* __restrict__ child, const int* __restrict__ parent, float4* nbox,
-                        uint32_t* __restrict__ flags, const int2* __restrict__ range, float* __restrict__ dp) {
+                        uint32_t* __restrict__ flags, const int2* __restrict__ range, float* __restrict__ dp,
+                        float cost_tri) {
     int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n) return;
     const uint32_t p = sorted[j];
@@ -379,8 +382,8 @@ __global__ void k_refit(const uint32_t* __restrict__ sorted, const float4* __res
         __stcg(&nbox[2ull * node + 1], hi);
         if (dp) {
             float cl[9], cr[9];
-            dp_child(dp, c.x, box_area(alo, ahi), cl);
-            dp_child(dp, c.y, box_area(blo, bhi), cr);
+            dp_child(dp, c.x, box_area(alo, ahi), cost_tri, cl);
+            dp_child(dp, c.y, box_area(blo, bhi), cost_tri, cr);
             float* out = dp + 8ull * node;
             float dist8 = 3.0e38f;
             for (int j = 2; j <= 8; ++j) {
@@ -392,7 +395,7 @@ __global__ void k_refit(const uint32_t* __restrict__ sorted, const float4* __res
             const int2 r = range[node];
             const float a = box_area(lo, hi);
             const float c_int = COST_NODE * a + dist8;
-            const float c_leaf = r.y - r.x + 1 <= 3 ? COST_TRI * (float)(r.y - r.x + 1) * a : 3.0e38f;
+            const float c_leaf = r.y - r.x + 1 <= 3 ? cost_tri * (float)(r.y - r.x + 1) * a : 3.0e38f;
             __stcg(out, fminf(c_int, c_leaf));
         }
         node = parent[node];
@@ -418,6 +421,7 @@ struct CollapseArgs {
     uint32_t node_cap;
     uint32_t* err;
     const float* dp;              // collapse costs from k_refit
+    float cost_tri;               // triangle-test cost relative to a node test
 };
 
 __device__ __forceinline__ size_t box_index(int n, int ref) { return ref >= 0 ? (size_t)ref : (size_t)(n - 1 + ~ref); }
@@ -479,8 +483,10 @@ __global__ void k_collapse(CollapseArgs A, const int2* __restrict__ frontier, ui
             }
             const int2 c = A.child[r];
             float cl[9], cr[9];
-            dp_child(A.dp, c.x, c.x < 0 ? box_area(A.nbox[2 * box_index(n, c.x)], A.nbox[2 * box_index(n, c.x) + 1]) : 0.f, cl);
-            dp_child(A.dp, c.y, c.y < 0 ? box_area(A.nbox[2 * box_index(n, c.y)], A.nbox[2 * box_index(n, c.y) + 1]) : 0.f, cr);
+            dp_child(A.dp, c.x, c.x < 0 ? box_area(A.nbox[2 * box_index(n, c.x)], A.nbox[2 * box_index(n, c.x) + 1]) : 0.f,
+                     A.cost_tri, cl);
+            dp_child(A.dp, c.y, c.y < 0 ? box_area(A.nbox[2 * box_index(n, c.y)], A.nbox[2 * box_index(n, c.y) + 1]) : 0.f,
+                     A.cost_tri, cr);
             int bk = 1;
             float best = 3.0e38f;
             for (int kk = 1; kk < k; ++kk) {
@@ -1271,7 +1277,8 @@ void scene_build(crt_scene* s, const crt_entity_desc* ents, uint32_t n_ents) {
             k_karras<<<cdiv(n - 1, BLOCK), BLOCK, 0, st>>>(ka, (int)n, child, range, parent);
             check_launch(ctx, "k_karras");
         }
-        k_refit<<<cdiv(n, BLOCK), BLOCK, 0, st>>>(va, tbox, (int)n, child, parent, nbox, flags, range, dpc);
+        k_refit<<<cdiv(n, BLOCK), BLOCK, 0, st>>>(va, tbox, (int)n, child, parent, nbox, flags, range, dpc,
+                                                  ctx->collapse_tri_cost);
         check_launch(ctx, "k_refit");
         idx_a = va;
     }
@@ -1307,6 +1314,7 @@ void scene_build(crt_scene* s, const crt_entity_desc* ents, uint32_t n_ents) {
     A.node_cap = cap;
     A.err = ctx->d_error;
     A.dp = dpc;
+    A.cost_tri = ctx->collapse_tri_cost;
 
     uint32_t fcount = 1, depth = 0;
     int2 *cur = front, *nxt = front_b;
@@ -1336,7 +1344,16 @@ void scene_build(crt_scene* s, const crt_entity_desc* ents, uint32_t n_ents) {
     s->build_ms = ms;
     s->n_nodes = used[0];
     s->depth = depth;
+    // the node array was sized for the worst case (n / 3 + 2 nodes); keep only the nodes used
+    if (used[0] < cap) {
+        WideNode* exact = nullptr;
+        CRT_CUDA(cudaMalloc(&exact, sizeof(WideNode) * std::max<uint32_t>(used[0], 1)));
+        CRT_CUDA(cudaMemcpyAsync(exact, s->nodes, sizeof(WideNode) * used[0], cudaMemcpyDeviceToDevice, st));
+        CRT_CUDA(cudaStreamSynchronize(st));
+        CRT_CUDA(cudaFree(s->nodes));
+        s->nodes = exact;
+    }
     for (int k = 0; k < 6; ++k) s->bounds[k] = n ? fkey_inv(kb_h[k]) : 0.f;
-    s->device_bytes = sizeof(WideNode) * cap + nn * (48 + 4 + 4) + (any_vn ? nn * 48 : 0) +
+    s->device_bytes = sizeof(WideNode) * std::max<uint32_t>(used[0], 1) + nn * (48 + 4 + 4) + (any_vn ? nn * 48 : 0) +
                       sizeof(EntityDev) * s->host_entities.size();
 }

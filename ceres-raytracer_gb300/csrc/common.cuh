@@ -86,6 +86,7 @@ struct crt_context {
     uint32_t wave_paths = 1u << 23;  // render paths per wavefront wave
     int use_graphs = 1;              // replay batched waves as CUDA graphs
     int build_sah = 1;               // scene builds: binned-SAH topology (1) or Karras radix tree (0)
+    float collapse_tri_cost = 0.15f; // scene builds: triangle-test cost of the 8-wide collapse (node = 1)
     // graph cache of the batched wavefront (one executable per wave shape)
     void* graph_exec = nullptr;
     uint64_t graph_key = 0;

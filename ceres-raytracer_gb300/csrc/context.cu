@@ -237,14 +237,16 @@ int crt_context_reset_counters(crt_context* ctx) {
 
 int crt_context_set_tuning(crt_context* ctx, const crt_tuning* t) {
     if (!ctx || !t) return CRT_ERR_INVALID;
-    if (t->queue_chunk < 1 || t->queue_chunk > 8 || t->wave_paths < (1u << 16)) {
-        ctx->last_error = "tuning out of range (queue_chunk 1..8, wave_paths >= 65536)";
+    if (t->queue_chunk < 1 || t->queue_chunk > 8 || t->wave_paths < (1u << 16) ||
+        !(t->collapse_tri_cost >= 0.01f && t->collapse_tri_cost <= 10.0f)) {
+        ctx->last_error = "tuning out of range (queue_chunk 1..8, wave_paths >= 65536, collapse_tri_cost 0.01..10)";
         return CRT_ERR_INVALID;
     }
     ctx->queue_chunk = t->queue_chunk;
     ctx->wave_paths = t->wave_paths;
     ctx->use_graphs = t->use_graphs ? 1 : 0;
     ctx->build_sah = t->build_sah ? 1 : 0;
+    ctx->collapse_tri_cost = t->collapse_tri_cost;
     return CRT_OK;
 }
 
@@ -254,6 +256,7 @@ int crt_context_get_tuning(const crt_context* ctx, crt_tuning* out) {
     out->wave_paths = ctx->wave_paths;
     out->use_graphs = ctx->use_graphs;
     out->build_sah = ctx->build_sah;
+    out->collapse_tri_cost = ctx->collapse_tri_cost;
     return CRT_OK;
 }
 

@@ -161,6 +161,10 @@ typedef struct {
     int use_graphs;                       /* replay batched waves as CUDA graphs */
     int build_sah;                        /* scenes built afterwards: binned-SAH tree (1, default) or
                                              Karras radix tree over the Morton order (0, faster build) */
+    float collapse_tri_cost;              /* scenes built afterwards: cost of a triangle test relative to
+                                             an 8-wide node test in the 8-wide collapse (default 0.15,
+                                             best for coherent rays; ~0.5 suits multi-bounce path
+                                             tracing); 0.01 .. 10 */
 } crt_tuning;
 
 typedef struct {

@@ -41,9 +41,17 @@ def build_both(ctx, ents):
     return a, b
 
 
-def test_sah_and_radix_trees_agree_on_asteroid(ctx):
+@pytest.mark.parametrize("other", ["radix", "leaf_cost_0.5"])
+def test_sah_and_radix_trees_agree_on_asteroid(ctx, other):
     ents = [scenes.EntitySpec("a", scenes.asteroid(100_000, seed=11), (0.1, 0.1, 0.1))]
-    sah, radix = build_both(ctx, ents)
+    if other == "radix":
+        sah, radix = build_both(ctx, ents)
+    else:   # the same topology collapsed with a larger triangle cost (smaller leaves)
+        sah = ctx.scene(ents)
+        ctx.set_tuning(collapse_tri_cost=0.5)
+        radix = ctx.scene(ents)
+        ctx.set_tuning()
+        assert radix.stats()["n_nodes"] > sah.stats()["n_nodes"]
     assert sah.stats()["n_tris"] == radix.stats()["n_tris"] == 100_000
     rng = np.random.Generator(np.random.PCG64(5))
     rays = as32(random_rays(rng, 200_000, spread=1500.0))
