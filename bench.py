@@ -626,12 +626,19 @@ def served_measure(args, device):
         return lat, time.perf_counter() - t_first
 
     small = [q.get("size", 0) <= 1024 for _, q in items]
+    kinds = [q["kind"] for _, q in items]
 
     def summary(lat, span):
         ls = [x for x, f in zip(lat, small) if f]
+        by_kind = {}
+        for k in ("render", "lidar", "srp"):
+            lk = [x for x, f, kk in zip(lat, small, kinds) if f and kk == k]
+            if lk:
+                by_kind[k] = round(percentile(lk, 99), 2)
         return {"mrays_s": round(rays / span / 1e6, 1), "span_s": round(span, 3),
                 "p50_ms": round(percentile(lat, 50), 2), "p99_ms": round(percentile(lat, 99), 2),
-                "p50_ms_le1024": round(percentile(ls, 50), 2), "p99_ms_le1024": round(percentile(ls, 99), 2)}
+                "p50_ms_le1024": round(percentile(ls, 50), 2), "p99_ms_le1024": round(percentile(ls, 99), 2),
+                "p99_ms_le1024_by_kind": by_kind}
 
     def clocked(fn, *a):
         cs = ClockSampler(device)

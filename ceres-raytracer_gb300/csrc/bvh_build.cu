@@ -1042,7 +1042,8 @@ void scan_exclusive(crt_context* ctx, const uint32_t* in, uint32_t* out, uint32_
 
 // Binned-SAH binary tree over the Morton-sorted triangles (n > SAH_T): fills child / range / parent
 // like k_karras and writes the triangle order of the tree's leaves to `sorted` (in place of the
-// Morton order).  Returns the root's internal index.
+// Morton order).  Returns the root's internal index, or -1 (with nothing modified) when its
+// temporaries (about 0.6 GB per million triangles) cannot be allocated.
 int sah_topology(crt_context* ctx, int n, const float4* tbox, const float4* cen, const uint32_t* keys,
                  uint32_t* sorted, const uint32_t* code_by_prim, int2* child, int2* range, int* parent) {
     cudaStream_t st = ctx->stream;
@@ -1058,7 +1059,10 @@ int sah_topology(crt_context* ctx, int n, const float4* tbox, const float4* cen,
                  o_tf = take(8ull * max_tasks), o_ts = take(8ull * max_tasks), o_sf = take(8ull * max_tasks),
                  o_ss = take(8ull * max_tasks), o_segs = take(sizeof(SahSeg) * max_segs), o_lo = take(4ull * n),
                  o_hi = take(4ull * n), o_code = take(4ull * n);
-    CRT_CUDA(cudaMalloc(&mem, off));
+    if (cudaMalloc(&mem, off) != cudaSuccess) {   // nothing modified yet: the caller builds a radix tree
+        cudaGetLastError();
+        return -1;
+    }
     struct Free {
         char* p;
         ~Free() { cudaFree(p); }
@@ -1271,9 +1275,9 @@ void scene_build(crt_scene* s, const crt_entity_desc* ents, uint32_t n_ents) {
             std::swap(va, vb);
         }
         // after 4 passes the sorted data is back in (code_a, idx_a)
-        if (sah) {
-            root_index = sah_topology(ctx, (int)n, tbox, cen, keys, va, code_prim, child, range, parent);
-        } else if (n > 1) {
+        if (sah) root_index = sah_topology(ctx, (int)n, tbox, cen, keys, va, code_prim, child, range, parent);
+        if ((!sah || root_index < 0) && n > 1) {   // radix tree (also when the SAH temporaries do not fit)
+            root_index = 0;
             k_karras<<<cdiv(n - 1, BLOCK), BLOCK, 0, st>>>(ka, (int)n, child, range, parent);
             check_launch(ctx, "k_karras");
         }
