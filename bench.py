@@ -14,6 +14,7 @@ public `crt` API (BodyFixedGroup.render / lidar_scan) returning numpy arrays.
 Multi-GPU (torchrun): every rank runs the same workload on its own GPU (replicas; weak scaling).
 """
 import argparse
+import datetime
 import json
 import os
 import statistics
@@ -139,15 +140,19 @@ def percentile(xs, q):
 
 
 class ClockSampler:
-    """nvidia-smi clock / throttle sampling during the timed region."""
-    FIELDS = "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown," \
-             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown," \
-             "clocks_event_reasons.sw_power_cap,utilization.gpu"
+    """nvidia-smi clock / throttle sampling during the timed region: sampling starts before it (the
+    tool's start-up can hold this process's CUDA driver calls for tens of milliseconds) and only the
+    samples stamped between start() returning and stop() are summarised."""
+    FIELDS = "timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active," \
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown," \
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap,utilization.gpu"
 
-    def __init__(self, device):
+    def __init__(self, device, settle_s=1.5):
         self.device = device
+        self.settle_s = settle_s
         self.proc = None
         self.path = None
+        self.t0 = self.t1 = None
 
     def start(self):
         try:
@@ -158,10 +163,17 @@ class ClockSampler:
                                          stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
         except (OSError, FileNotFoundError):
             self.proc = None
+            return
+        t = time.perf_counter()
+        while time.perf_counter() - t < self.settle_s and self.proc.poll() is None:
+            time.sleep(0.02)
+        self.t0 = time.time()
 
     def stop(self):
         if not self.proc:
             return None
+        self.t1 = time.time()
+        time.sleep(0.25)   # the sample that covers the end of the window
         self.proc.terminate()
         try:
             self.proc.wait(timeout=5)
@@ -171,18 +183,27 @@ class ClockSampler:
         with open(self.path) as f:
             for line in f:
                 parts = [p.strip() for p in line.split(",")]
-                if len(parts) >= 9:
+                if len(parts) >= 10:
                     rows.append(parts)
         os.unlink(self.path)
+
+        def stamp(r):
+            try:
+                return datetime.datetime.strptime(r[0], "%Y/%m/%d %H:%M:%S.%f").timestamp()
+            except ValueError:
+                return None
+        inside = [r for r in rows if stamp(r) is not None and self.t0 - 0.2 <= stamp(r) <= self.t1 + 0.2]
+        rows = inside or rows
         if not rows:
             return None
-        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
-        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        num = lambda x: x.replace(".", "").isdigit()
+        sm = [float(r[2]) for r in rows if num(r[2])]
+        mx = [float(r[3]) for r in rows if num(r[3])]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower().startswith("active")})
-        util = [float(r[9]) for r in rows if len(r) > 9 and r[9].replace(".", "").isdigit()]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[6 + k].lower().startswith("active")})
+        util = [float(r[10]) for r in rows if len(r) > 10 and num(r[10])]
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(rows),
+                "reasons": reasons, "samples": len(rows), "window_s": round(self.t1 - self.t0, 3),
                 "gpu_busy_pct": round(statistics.mean(util), 1) if util else None}
 
 
@@ -398,7 +419,7 @@ def gpu_arm(args):
     traffic = profiled_traffic()
     roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
             "frac": round(achieved / peak, 4), "traffic": traffic, "peak_source": peak_kind,
-            "kernel": "k_trace<closest> on 2048^2 primary camera rays (crt_trace_closest)",
+            "kernel": "k_trace<closest> on 2048^2 primary camera rays in 8x4 tiles (crt_trace_closest)",
             "bytes_per_ray": round(b_ray, 1), "nodes_per_ray": round(nodes_ray, 2), "tris_per_ray": round(tris_ray, 2),
             "kernel_ms": round(t_kernel * 1e3, 3), "kernel_mrays_s": round(cnt["rays"] / t_kernel / 1e6, 1)}
 
@@ -438,7 +459,9 @@ def gpu_arm(args):
                 "latency_ms": {"render_p50": round(percentile(lat_render, 50), 3),
                                "render_p99": round(percentile(lat_render, 99), 3),
                                "lidar_p50": round(percentile(lat_lidar, 50), 3),
-                               "lidar_p99": round(percentile(lat_lidar, 99), 3)},
+                               "lidar_p99": round(percentile(lat_lidar, 99), 3),
+                               "step_p50": round(percentile(step_ms, 50), 3),
+                               "step_max": round(max(step_ms), 3)},
                 "roofline": roof, "gpu_launches": int(launches), "clocks": clk, "e2e": e2e, "batched": batched,
                 "served": served, "srp": srp, "cornell": cornell}
         if world == 1 and not args.no_cpu:
@@ -760,11 +783,27 @@ def srp_measure(args, ctx, stream):
             "ms_per_attitude": round(res[True] * 1e3 / n, 3), "nodes_per_ray": round(cnt["nodes"] / cnt["rays"], 2)}
 
 
+def tile_order(W, H):
+    """Pixel index of each path slot in the order the render path traces camera rays: 8 x 4 tiles in
+    row-major tile order (rows in bands of 4, the last band lower when H % 4 != 0, each band's last
+    tile W % 8 wide)."""
+    j = np.arange(W * H, dtype=np.int64)
+    y0 = j // (4 * W) * 4
+    hb = np.minimum(4, H - y0)
+    r = j - y0 * W
+    full = W >> 3
+    tx = np.minimum(r // (8 * hb), full)
+    rr = r - tx * 8 * hb
+    wt = np.where(tx < full, 8, max(W - 8 * full, 1))
+    return (y0 + rr // wt) * W + tx * 8 + rr % wt
+
+
 def scenes_camera_rays(cam):
-    """FP32 camera rays in crt_ray layout (o.xyz, tmin, d.xyz, tmax) as an [n, 8] float32 array, for
-    the roofline probe (the oracle's FP64 rays are laid out o.xyz, d.xyz, tmin, tmax)."""
+    """FP32 camera rays in crt_ray layout (o.xyz, tmin, d.xyz, tmax) as an [n, 8] float32 array in the
+    render path's 8 x 4 tile order, for the roofline probe (the oracle's FP64 rays are laid out
+    o.xyz, d.xyz, tmin, tmax, one per pixel in row-major order)."""
     import oracle
-    r64 = oracle.camera_rays(cam)
+    r64 = oracle.camera_rays(cam)[tile_order(int(cam["resolution"][0]), int(cam["resolution"][1]))]
     r = np.empty((r64.shape[0], 8), dtype=np.float32)
     r[:, 0:3] = r64[:, 0:3]
     r[:, 3] = 0.0

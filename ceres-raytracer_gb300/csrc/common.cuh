@@ -79,8 +79,11 @@ struct crt_context {
     uint64_t launches = 0;
     void* scratch[SCR_COUNT] = {};
     size_t scratch_bytes[SCR_COUNT] = {};
-    void* pinned = nullptr;
-    size_t pinned_bytes = 0;
+    // upload staging: a ring of two grow-only pinned buffers, each with the event after its last copy
+    void* pinned[2] = {nullptr, nullptr};
+    size_t pinned_bytes[2] = {0, 0};
+    cudaEvent_t pinned_ev[2] = {nullptr, nullptr};
+    int pinned_next = 0;
     // tuning (crt_context_set_tuning; the autotuner picks these per GPU and scene class)
     uint32_t queue_chunk = 1;        // 32-item groups per atomic grab of the ray queue
     uint32_t wave_paths = 1u << 23;  // render paths per wavefront wave
@@ -94,8 +97,22 @@ struct crt_context {
 
 // Grow-only device scratch buffer for one purpose.  Synchronises the stream before reallocating.
 void* ctx_scratch(crt_context* ctx, ScratchSlot slot, size_t bytes);
-// Pinned host staging buffer (grow-only).
-void* ctx_pinned(crt_context* ctx, size_t bytes);
+// Pinned host staging for one call's uploads, from a ring of two grow-only buffers.  Acquiring waits
+// only until the copies out of the buffer's previous use have run, not for the whole stream, so the
+// host prepares a call while the GPU still runs the previous one.  release() records that point on
+// the stream once the copies out of the buffer are enqueued (later reuse of the buffer within the
+// call must synchronise itself); the destructor records it if release() was not reached.
+struct PinnedStaging {
+    crt_context* ctx;
+    int slot;
+    char* p;
+    bool released = false;
+    PinnedStaging(crt_context* c, size_t bytes);
+    void release();
+    ~PinnedStaging();
+    PinnedStaging(const PinnedStaging&) = delete;
+    PinnedStaging& operator=(const PinnedStaging&) = delete;
+};
 bool is_device_ptr(const void* p);
 // Copy helpers: ensure `bytes` of `src` are readable on the device; return a device pointer.
 const void* to_device(crt_context* ctx, const void* src, size_t bytes, ScratchSlot slot);

@@ -21,19 +21,32 @@ void* ctx_scratch(crt_context* ctx, ScratchSlot slot, size_t bytes) {
     return ctx->scratch[slot];
 }
 
-void* ctx_pinned(crt_context* ctx, size_t bytes) {
-    if (ctx->pinned_bytes < bytes) {
-        if (ctx->pinned) {
-            CRT_CUDA(cudaStreamSynchronize(ctx->stream));
-            CRT_CUDA(cudaFreeHost(ctx->pinned));
-            ctx->pinned = nullptr;
-            ctx->pinned_bytes = 0;
+PinnedStaging::PinnedStaging(crt_context* c, size_t bytes) : ctx(c), slot(c->pinned_next), p(nullptr) {
+    ctx->pinned_next ^= 1;
+    if (!ctx->pinned_ev[slot]) CRT_CUDA(cudaEventCreateWithFlags(&ctx->pinned_ev[slot], cudaEventDisableTiming));
+    CRT_CUDA(cudaEventSynchronize(ctx->pinned_ev[slot]));   // copies of this buffer's previous use
+    if (ctx->pinned_bytes[slot] < bytes) {
+        if (ctx->pinned[slot]) {
+            CRT_CUDA(cudaFreeHost(ctx->pinned[slot]));
+            ctx->pinned[slot] = nullptr;
+            ctx->pinned_bytes[slot] = 0;
         }
         size_t cap = (bytes + bytes / 4 + 4095) & ~size_t(4095);
-        CRT_CUDA(cudaMallocHost(&ctx->pinned, cap));
-        ctx->pinned_bytes = cap;
+        CRT_CUDA(cudaMallocHost(&ctx->pinned[slot], cap));
+        ctx->pinned_bytes[slot] = cap;
     }
-    return ctx->pinned;
+    p = (char*)ctx->pinned[slot];
+}
+
+void PinnedStaging::release() {
+    CRT_CUDA(cudaEventRecord(ctx->pinned_ev[slot], ctx->stream));
+    released = true;
+}
+
+PinnedStaging::~PinnedStaging() {
+    // every exit path, also after an error: copies already enqueued from the buffer finish before
+    // its next use
+    if (!released) cudaEventRecord(ctx->pinned_ev[slot], ctx->stream);
 }
 
 bool is_device_ptr(const void* p) {
@@ -185,7 +198,10 @@ int crt_context_destroy(crt_context* ctx) {
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     for (int i = 0; i < SCR_COUNT; ++i)
         if (ctx->scratch[i]) cudaFree(ctx->scratch[i]);
-    if (ctx->pinned) cudaFreeHost(ctx->pinned);
+    for (int k = 0; k < 2; ++k) {
+        if (ctx->pinned[k]) cudaFreeHost(ctx->pinned[k]);
+        if (ctx->pinned_ev[k]) cudaEventDestroy(ctx->pinned_ev[k]);
+    }
     if (ctx->d_counters) cudaFree(ctx->d_counters);
     if (ctx->d_error) cudaFree(ctx->d_error);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);

@@ -84,6 +84,20 @@ def test_adaptive_sampling_matches_oracle(cornell):
     assert close.mean() > 0.9, close.mean()
 
 
+@pytest.mark.parametrize("res,spp,thr", [((37, 23), (4, 4), 0.0), ((29, 19), (2, 16), 2.0), ((5, 3), (3, 3), 0.0)])
+def test_odd_resolutions_match_oracle(cornell, res, spp, thr):
+    """Camera paths are traced in 8 x 4 pixel tiles: images whose sides are not multiples of 8 and 4
+    (partial tiles, a short last band) still sample every pixel once per sample, as the oracle."""
+    d, ents, sc, o = cornell
+    cam = dict(camera_from(d, "rcam"), resolution=list(res))
+    lights = lights_from(d["lights"])
+    _, rad = sc.render(cam, lights, spp[0], spp[1], thr, 2, seed=7)
+    orad, _, _ = o.render(cam, lights, spp[0], spp[1], thr, 2, seed=7)
+    assert rad.shape == (res[1], res[0], 4) and (rad[..., 3] == 1).all()
+    close = np.isclose(rad[..., :3], orad[..., :3], rtol=2e-3, atol=1e-3).all(-1)
+    assert close.mean() > 0.9, close.mean()
+
+
 def test_multiple_lights_and_no_bounce(cornell):
     d, ents, sc, o = cornell
     cam = dict(camera_from(d, "rcam"), resolution=[16, 16])
