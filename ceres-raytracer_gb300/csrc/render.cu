@@ -8,7 +8,8 @@
 //   shade     surface point, one shadow ray per light, bounce ray             (k_shade)
 //   shadow    any hit for the shadow queue                                     (persistent trace)
 //   accum     sum lights, clamp after the first bounce, times path weight      (k_accum; folded into
-//             k_update when the wave's only bounce is bounce 0)
+//             k_update when the wave has at most one bounce: bounce 0's weight is the constant
+//             2 pi and its radiance starts at zero, so neither is stored)
 //   bounce    closest hit for the continuing-path queue                        (persistent trace)
 //   update    per-pixel running mean and adaptive stop, samples in order       (k_update)
 //   finalize  RGBA float and clamp(v * 256, 0, 255) bytes per request          (k_finalize)
@@ -31,6 +32,7 @@
 
 #include <algorithm>
 #include <map>
+#include <mutex>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -104,9 +106,8 @@ struct Batch {
     float4* ray;
     uint32_t* skip;
     float4* hit;
-    float4* weight;
-    float4* wacc;
-    float4* rad;
+    float4* wgt[2];            // path weight at bounce b >= 1 in wgt[b & 1] (bounce 0: path_weight's constant)
+    float4* rad;               // radiance gathered so far (written from bounce 0's accumulation on)
     uint32_t* preq;
     uint32_t* ppix;
     uint32_t* psample;
@@ -260,9 +261,6 @@ struct PrimaryJob {
         }
         const uint32_t p = i - B.cur->n_lidar_items;
         B.hit[p] = make_float4(h.t, h.u, h.v, __uint_as_float(h.slot));
-        const float w0 = (float)(2.0 * 3.14159265358979323846);   // Color(2*M_PI), unidirectional.hpp:38
-        B.weight[p] = make_float4(w0, w0, w0, 0.f);
-        B.rad[p] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
 };
 
@@ -345,6 +343,13 @@ __global__ void k_queue_rotate(uint32_t* counts) {
     counts[2] = 0;
 }
 
+// Path weight at bounce b: Color(2*M_PI) at the camera vertex (unidirectional.hpp:38), then
+// multiplied by (1 - r1) per bounce (k_shade)
+__device__ __forceinline__ float4 path_weight(const Batch& B, uint32_t p, int bounce) {
+    const float w0 = (float)(2.0 * 3.14159265358979323846);
+    return bounce == 0 ? make_float4(w0, w0, w0, 0.f) : B.wgt[bounce & 1][p];
+}
+
 // ---------------------------------------------------------------- shade
 __global__ void k_shade(Batch B, int bounce, const uint32_t* __restrict__ q_in, uint32_t* __restrict__ q_out) {
     const uint32_t n = bounce == 0 ? B.cur->n_paths : B.counts[0];
@@ -396,7 +401,6 @@ __global__ void k_shade(Batch B, int bounce, const uint32_t* __restrict__ q_in, 
             B.sskip[e] = h.slot;
             B.sreq[e] = req;
         }
-        B.wacc[p] = B.weight[p];
         if (bounce < R.c.num_bounces - 1) {
             float r1, r2;
             rng2(R.c, pixel, sample, (uint32_t)bounce, 1u, r1, r2);
@@ -405,8 +409,8 @@ __global__ void k_shade(Batch B, int bounce, const uint32_t* __restrict__ q_in, 
             B.ray[2ull * p + 1] = make_float4(nd.x, nd.y, nd.z, 3.402823466e38f);
             B.skip[p] = h.slot;
             const float bc = 1.0f - r1;
-            const float4 wt = B.weight[p];
-            B.weight[p] = make_float4(wt.x * bc, wt.y * bc, wt.z * bc, 0.f);
+            const float4 wt = path_weight(B, p, bounce);
+            B.wgt[(bounce + 1) & 1][p] = make_float4(wt.x * bc, wt.y * bc, wt.z * bc, 0.f);
             q_out[warp_append(&B.counts[1], 1u)] = p;
         }
     }
@@ -429,7 +433,7 @@ __device__ __forceinline__ float4 add_light(const Batch& B, uint32_t p, uint32_t
         lr.y = fminf(fmaxf(lr.y, 0.f), 1.f);
         lr.z = fminf(fmaxf(lr.z, 0.f), 1.f);
     }
-    const float4 wa = B.wacc[p];
+    const float4 wa = path_weight(B, p, bounce);
     return make_float4(__fmaf_rn(lr.x, wa.x, r.x), __fmaf_rn(lr.y, wa.y, r.y), __fmaf_rn(lr.z, wa.z, r.z), 0.f);
 }
 
@@ -437,10 +441,14 @@ __global__ void k_accum(Batch B, int bounce, const uint32_t* __restrict__ q_in) 
     const uint32_t n = bounce == 0 ? B.cur->n_paths : B.counts[0];
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const uint32_t p = bounce == 0 ? i : q_in[i];
-        if (__float_as_uint(B.hit[p].w) == CRT_MISS) continue;
+        const bool hit = __float_as_uint(B.hit[p].w) != CRT_MISS;
         const RReq& R = B.rr[B.preq[p]];
-        if (bounce >= R.c.num_bounces) continue;
-        B.rad[p] = add_light(B, p, R.n_lights, bounce, B.rad[p]);
+        if (bounce == 0) {   // every path of the wave: its radiance starts here
+            const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+            B.rad[p] = hit && R.c.num_bounces > 0 ? add_light(B, p, R.n_lights, 0, zero) : zero;
+        } else if (hit && bounce < R.c.num_bounces) {
+            B.rad[p] = add_light(B, p, R.n_lights, bounce, B.rad[p]);
+        }
     }
 }
 
@@ -467,9 +475,14 @@ __global__ void k_update(Batch B) {
         for (uint32_t k = 0; k < S.ns; ++k) {
             const uint32_t sample = S.s0 + k + 1;   // 1-based as in the reference loop
             const size_t p = (size_t)S.path_base + (size_t)k * S.npix + a;
-            float4 L = B.rad[p];
-            if (ACC0 && R.c.num_bounces > 0 && __float_as_uint(B.hit[p].w) != CRT_MISS)
-                L = add_light(B, (uint32_t)p, R.n_lights, 0, L);
+            float4 L;
+            if (ACC0) {
+                L = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (R.c.num_bounces > 0 && __float_as_uint(B.hit[p].w) != CRT_MISS)
+                    L = add_light(B, (uint32_t)p, R.n_lights, 0, L);
+            } else {
+                L = B.rad[p];
+            }
             const float inv = 1.0f / (float)sample;
             const float dx = (L.x - m.x) * inv, dy = (L.y - m.y) * inv, dz = (L.z - m.z) * inv;
             m.x += dx; m.y += dy; m.z += dz;
@@ -540,9 +553,29 @@ __global__ void k_tan_table2(double* __restrict__ out, uint32_t nx, uint32_t ny,
     else if (i < nx + ny) out[i] = tan(-hy + ((i - nx) + 0.5) * 2.0 * hy / ny);
 }
 
-inline uint32_t grid_for(crt_context* ctx, size_t n, int block = 256) {
+// Grid of a grid-stride kernel: at most one resident wave (SMs x the kernel's resident blocks per SM
+// at this block size, from its register and shared-memory use), fewer blocks when n needs fewer.  A
+// larger grid would run a partial second wave of blocks on a part of the GPU.
+template <typename... Args>
+uint32_t grid_for(crt_context* ctx, void (*kernel)(Args...), size_t n, int block = 256) {
+    static std::mutex mu;
+    static std::map<const void*, int> per_sm_of;
+    int per_sm = 0;
+    {
+        std::lock_guard<std::mutex> lock(mu);
+        auto it = per_sm_of.find((const void*)kernel);
+        if (it != per_sm_of.end()) per_sm = it->second;
+    }
+    if (!per_sm) {
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, 0) != cudaSuccess || per_sm < 1) {
+            cudaGetLastError();
+            per_sm = 1;
+        }
+        std::lock_guard<std::mutex> lock(mu);
+        per_sm_of[(const void*)kernel] = per_sm;
+    }
     const size_t want = (n + block - 1) / block;
-    return (uint32_t)std::max<size_t>(1, std::min<size_t>(want, (size_t)ctx->sm_count * 8));
+    return (uint32_t)std::max<size_t>(1, std::min<size_t>(want, (size_t)ctx->sm_count * per_sm));
 }
 inline uint32_t tiles_items(uint32_t W, uint32_t H) { return ((W + 7) / 8) * ((H + 3) / 4) * 32u; }
 
@@ -553,21 +586,22 @@ inline uint32_t tiles_items(uint32_t W, uint32_t H) { return ((W + 7) / 8) * ((H
 void launch_wave_kernels(crt_context* ctx, const Batch& B, size_t P, size_t NL, uint32_t lidar_items,
                          int max_bounces, uint32_t* qa, uint32_t* qb, uint32_t* tqueue) {
     cudaStream_t st = ctx->stream;
-    const uint32_t gsz = grid_for(ctx, P);
+    const uint32_t g_shade = grid_for(ctx, k_shade, P), g_accum = grid_for(ctx, k_accum, P);
+    const uint32_t g_update = max_bounces <= 1 ? grid_for(ctx, k_update<true>, P) : grid_for(ctx, k_update<false>, P);
     k_wave_begin<<<1, 128, 0, st>>>(B);
     check_launch(ctx, "k_wave_begin");
     launch_trace<false>(ctx, SceneView{}, PrimaryJob{B}, (uint32_t)std::min<size_t>(P + lidar_items, 0xFFFFFF00u),
                         &B.cur->n_primary, tqueue);
     const uint32_t* q_in = nullptr;
     uint32_t* q_out = qa;
-    const bool fuse = max_bounces == 1;   // k_update adds the light of the only bounce
+    const bool fuse = max_bounces <= 1;   // k_update adds the light of the only bounce (if any)
     for (int b = 0; b < max_bounces; ++b) {
-        k_shade<<<gsz, 256, 0, st>>>(B, b, q_in, q_out);
+        k_shade<<<g_shade, 256, 0, st>>>(B, b, q_in, q_out);
         check_launch(ctx, "k_shade");
         launch_trace<true>(ctx, SceneView{}, ShadowJob{B}, (uint32_t)std::min<size_t>(P * NL, 0xFFFFFF00u),
                            &B.counts[2], tqueue);
         if (!fuse) {
-            k_accum<<<gsz, 256, 0, st>>>(B, b, q_in);
+            k_accum<<<g_accum, 256, 0, st>>>(B, b, q_in);
             check_launch(ctx, "k_accum");
         }
         if (b < max_bounces - 1) {
@@ -578,8 +612,8 @@ void launch_wave_kernels(crt_context* ctx, const Batch& B, size_t P, size_t NL, 
             q_out = (q_out == qa) ? qb : qa;
         }
     }
-    if (fuse) k_update<true><<<gsz, 256, 0, st>>>(B);
-    else k_update<false><<<gsz, 256, 0, st>>>(B);
+    if (fuse) k_update<true><<<g_update, 256, 0, st>>>(B);
+    else k_update<false><<<g_update, 256, 0, st>>>(B);
     check_launch(ctx, "k_update");
     k_wave_end<<<1, 1, 0, st>>>(B);
     check_launch(ctx, "k_wave_end");
@@ -776,8 +810,8 @@ void run_batch(crt_context* ctx, const crt_request* reqs, size_t n, crt_batch_st
         B.ray = (float4*)take(P * 32);
         B.skip = (uint32_t*)take(P * 4);
         B.hit = (float4*)take(P * 16);
-        B.weight = (float4*)take(P * 16);
-        B.wacc = (float4*)take(P * 16);
+        B.wgt[0] = (float4*)take(P * 16);
+        B.wgt[1] = (float4*)take(P * 16);
         B.rad = (float4*)take(P * 16);
         B.preq = (uint32_t*)take(P * 4);
         B.ppix = (uint32_t*)take(P * 4);
@@ -923,7 +957,7 @@ void run_batch(crt_context* ctx, const crt_request* reqs, size_t n, crt_batch_st
                 uint32_t* out = h->act_buf[h->act_sel];
                 CRT_CUDA(cudaMemsetAsync(acount, 0, 4, st));
                 const RReq& R = rr[h->rr_index];
-                k_compact<<<grid_for(ctx, h->n_active), 256, 0, st>>>(h->active, h->n_active, B.done, R.pix_base,
+                k_compact<<<grid_for(ctx, k_compact, h->n_active), 256, 0, st>>>(h->active, h->n_active, B.done, R.pix_base,
                                                                        R.c.W, R.c.H, out, acount);
                 check_launch(ctx, "k_compact");
                 uint32_t cnt = 0;
@@ -954,7 +988,7 @@ void run_batch(crt_context* ctx, const crt_request* reqs, size_t n, crt_batch_st
 
     // ---- finalize and copy host outputs
     if (pix_total) {
-        k_finalize<<<grid_for(ctx, pix_total), 256, 0, st>>>(B, (uint32_t)rr.size(), pix_total);
+        k_finalize<<<grid_for(ctx, k_finalize, pix_total), 256, 0, st>>>(B, (uint32_t)rr.size(), pix_total);
         check_launch(ctx, "k_finalize");
     }
     ri = 0;
@@ -1478,8 +1512,8 @@ void engine_step(WaveEngine* e, std::vector<uint64_t>& completed) {
         B.ray = (float4*)take(P * 32);
         B.skip = (uint32_t*)take(P * 4);
         B.hit = (float4*)take(P * 16);
-        B.weight = (float4*)take(P * 16);
-        B.wacc = (float4*)take(P * 16);
+        B.wgt[0] = (float4*)take(P * 16);
+        B.wgt[1] = (float4*)take(P * 16);
         B.rad = (float4*)take(P * 16);
         B.preq = (uint32_t*)take(P * 4);
         B.ppix = (uint32_t*)take(P * 4);
@@ -1520,7 +1554,7 @@ void engine_step(WaveEngine* e, std::vector<uint64_t>& completed) {
         CRT_CUDA(cudaMemsetAsync(e->d_acount, 0, 4 * compacting.size(), st));
         for (size_t k = 0; k < compacting.size(); ++k) {
             EReq& r = *compacting[k];
-            k_compact<<<grid_for(ctx, r.n_active), 256, 0, st>>>(r.active, r.n_active, B.done, (uint32_t)r.unit_off,
+            k_compact<<<grid_for(ctx, k_compact, r.n_active), 256, 0, st>>>(r.active, r.n_active, B.done, (uint32_t)r.unit_off,
                                                                  r.W, r.H, r.act_buf[r.act_sel], e->d_acount + k);
             check_launch(ctx, "k_compact");
         }
@@ -1640,7 +1674,7 @@ void engine_step(WaveEngine* e, std::vector<uint64_t>& completed) {
     }
     for (EReq& r : e->res) {
         if (r.lidar || !r.finished) continue;
-        k_finalize_one<<<grid_for(ctx, r.npix), 256, 0, st>>>(B, r.slot);
+        k_finalize_one<<<grid_for(ctx, k_finalize_one, r.npix), 256, 0, st>>>(B, r.slot);
         check_launch(ctx, "k_finalize_one");
         if (r.q.rgba8 && (void*)r.rgba != (void*)r.q.rgba8)
             engine_stage_out(e, f, r.q.rgba8, r.rgba, (size_t)r.npix * 4);
