@@ -351,68 +351,125 @@ __device__ __forceinline__ float4 path_weight(const Batch& B, uint32_t p, int bo
 }
 
 // ---------------------------------------------------------------- shade
-__global__ void k_shade(Batch B, int bounce, const uint32_t* __restrict__ q_in, uint32_t* __restrict__ q_out) {
+// Block-wide ordered append of two counts per thread (n0 <= 16 lights, n1 <= 1, 256-thread blocks: each
+// block total fits 16 bits of a packed word): one atomicAdd per counter and block instead of one per
+// warp, since every append of a stage goes to the same counter and atomics on one address serialise
+// in one L2 slice.  Every thread of the block calls it; returns the thread's first index in each queue.
+__device__ __forceinline__ uint2 block_append2(uint32_t* c0, uint32_t n0, uint32_t* c1, uint32_t n1) {
+    __shared__ uint32_t s_off[32];
+    __shared__ uint32_t s_base[2];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const uint32_t v = n0 | (n1 << 16);
+    uint32_t x = v;   // inclusive scan over the warp
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) s_off[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        const uint32_t w = lane < nw ? s_off[lane] : 0u;
+        uint32_t incl = w;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        if (lane < nw) s_off[lane] = incl - w;
+        if (lane == 31) {   // block totals
+            const uint32_t t0 = incl & 0xFFFFu, t1 = incl >> 16;
+            s_base[0] = t0 ? atomicAdd(c0, t0) : 0u;
+            s_base[1] = t1 ? atomicAdd(c1, t1) : 0u;
+        }
+    }
+    __syncthreads();
+    const uint32_t ex = s_off[warp] + x - v;
+    const uint2 r = make_uint2(s_base[0] + (ex & 0xFFFFu), s_base[1] + (ex >> 16));
+    __syncthreads();   // the shared words are rewritten by the next call
+    return r;
+}
+
+// One live path at bounce `bounce`: surface point, a shadow ray per light at shadow-queue index
+// sbase + l, and when the path continues its bounce ray, appended to q_out at qidx
+__device__ __forceinline__ void shade_path(const Batch& B, int bounce, uint32_t p, uint32_t req, const THit& h,
+                                           uint32_t sbase, bool cont, uint32_t* __restrict__ q_out, uint32_t qidx) {
+    const RReq& R = B.rr[req];
+    const uint32_t pixel = B.ppix[p], sample = B.psample[p];
+    const SceneView sv = R.sv;
+    const SurfacePoint sp = surface_point(sv, h);
+    const EntityDev& E = sv.entities[sp.entity];
+    const float3 col = f3(E.color[0], E.color[1], E.color[2]);
+    const float3 x = sp.x - origin_offset(sp.x) * sp.flat_n;   // intersect_point - 1e-4 normal
+    const uint32_t nl = R.n_lights;
+    for (uint32_t l = 0; l < nl; ++l) {
+        const LightDev& lt = B.lights[R.light_base + l];
+        float3 lp = f3(lt.pos[0], lt.pos[1], lt.pos[2]);
+        float inten;
+        if (lt.type == 1) {   // AreaLight::sample_ray / get_intensity (area_light.hpp:54-72)
+            float a, b;
+            rng2(R.c, pixel, sample, (uint32_t)bounce, 2u + l, a, b);
+            const float xc = lt.size[0] * a - lt.size[0] / 2, yc = lt.size[1] * b - lt.size[1] / 2;
+            lp = f3(lt.R[0] * xc + lt.R[1] * yc, lt.R[3] * xc + lt.R[4] * yc, lt.R[6] * xc + lt.R[7] * yc) + lp;
+            const float3 dd = x - lp;
+            inten = lt.intensity / dot3(dd, dd);
+        } else {              // PointLight (point_light.hpp:32-39)
+            const float3 dd = x - lp;
+            inten = fminf(lt.intensity / dot3(dd, dd), 10000.0f);
+        }
+        const float3 to = lp - x;
+        const float dist = sqrtf(dot3(to, to));
+        const float3 dir = to * (1.0f / dist);
+        // ColoredLambertianMaterial::compute (material.hpp:100-103): colour * (-L . N), unclamped
+        const float ldn = -dot3(dir, sp.shading_n);
+        const float3 cb = col * ldn;
+        B.contrib[(size_t)p * B.L + l] = make_float4(cb.x * inten, cb.y * inten, cb.z * inten, 0.f);
+        B.occ[(size_t)p * B.L + l] = 0;
+        const uint32_t e = sbase + l;
+        B.sray[2ull * e] = make_float4(x.x, x.y, x.z, 0.f);
+        B.sray[2ull * e + 1] = make_float4(dir.x, dir.y, dir.z, dist);
+        B.sidx[e] = p * B.L + l;
+        B.sskip[e] = h.slot;
+        B.sreq[e] = req;
+    }
+    if (cont) {
+        float r1, r2;
+        rng2(R.c, pixel, sample, (uint32_t)bounce, 1u, r1, r2);
+        const float3 nd = cosine_importance(sp.shading_n, r1, r2);
+        B.ray[2ull * p] = make_float4(x.x, x.y, x.z, 0.f);
+        B.ray[2ull * p + 1] = make_float4(nd.x, nd.y, nd.z, 3.402823466e38f);
+        B.skip[p] = h.slot;
+        const float bc = 1.0f - r1;
+        const float4 wt = path_weight(B, p, bounce);
+        B.wgt[(bounce + 1) & 1][p] = make_float4(wt.x * bc, wt.y * bc, wt.z * bc, 0.f);
+        q_out[qidx] = p;
+    }
+}
+
+// 256-thread blocks (block_append2); the loop's trip count is uniform over a block
+__global__ void __launch_bounds__(256) k_shade(Batch B, int bounce, const uint32_t* __restrict__ q_in,
+                                               uint32_t* __restrict__ q_out) {
     const uint32_t n = bounce == 0 ? B.cur->n_paths : B.counts[0];
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const uint32_t p = bounce == 0 ? i : q_in[i];
-        const float4 hv = B.hit[p];
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        const uint32_t i = base + threadIdx.x;
+        uint32_t p = 0, req = 0, nl = 0;
+        bool live = false, cont = false;
         THit h;
-        h.t = hv.x; h.u = hv.y; h.v = hv.z;
-        h.slot = __float_as_uint(hv.w);
-        if (h.slot == CRT_MISS) continue;
-        const uint32_t req = B.preq[p];
-        const RReq& R = B.rr[req];
-        if (bounce >= R.c.num_bounces) continue;
-        const uint32_t pixel = B.ppix[p], sample = B.psample[p];
-        const SceneView sv = R.sv;
-        const SurfacePoint sp = surface_point(sv, h);
-        const EntityDev& E = sv.entities[sp.entity];
-        const float3 col = f3(E.color[0], E.color[1], E.color[2]);
-        const float3 x = sp.x - origin_offset(sp.x) * sp.flat_n;   // intersect_point - 1e-4 normal
-        const uint32_t nl = R.n_lights;
-        const uint32_t sbase = nl ? warp_append(&B.counts[2], nl) : 0;
-        for (uint32_t l = 0; l < nl; ++l) {
-            const LightDev& lt = B.lights[R.light_base + l];
-            float3 lp = f3(lt.pos[0], lt.pos[1], lt.pos[2]);
-            float inten;
-            if (lt.type == 1) {   // AreaLight::sample_ray / get_intensity (area_light.hpp:54-72)
-                float a, b;
-                rng2(R.c, pixel, sample, (uint32_t)bounce, 2u + l, a, b);
-                const float xc = lt.size[0] * a - lt.size[0] / 2, yc = lt.size[1] * b - lt.size[1] / 2;
-                lp = f3(lt.R[0] * xc + lt.R[1] * yc, lt.R[3] * xc + lt.R[4] * yc, lt.R[6] * xc + lt.R[7] * yc) + lp;
-                const float3 dd = x - lp;
-                inten = lt.intensity / dot3(dd, dd);
-            } else {              // PointLight (point_light.hpp:32-39)
-                const float3 dd = x - lp;
-                inten = fminf(lt.intensity / dot3(dd, dd), 10000.0f);
+        h.t = h.u = h.v = 0.f;
+        h.slot = CRT_MISS;
+        if (i < n) {
+            p = bounce == 0 ? i : q_in[i];
+            const float4 hv = B.hit[p];
+            h.t = hv.x; h.u = hv.y; h.v = hv.z;
+            h.slot = __float_as_uint(hv.w);
+            if (h.slot != CRT_MISS) {
+                req = B.preq[p];
+                const RenderCtl& c = B.rr[req].c;
+                live = bounce < c.num_bounces;
+                cont = bounce < c.num_bounces - 1;
+                nl = live ? B.rr[req].n_lights : 0u;
             }
-            const float3 to = lp - x;
-            const float dist = sqrtf(dot3(to, to));
-            const float3 dir = to * (1.0f / dist);
-            // ColoredLambertianMaterial::compute (material.hpp:100-103): colour * (-L . N), unclamped
-            const float ldn = -dot3(dir, sp.shading_n);
-            const float3 cb = col * ldn;
-            B.contrib[(size_t)p * B.L + l] = make_float4(cb.x * inten, cb.y * inten, cb.z * inten, 0.f);
-            B.occ[(size_t)p * B.L + l] = 0;
-            const uint32_t e = sbase + l;
-            B.sray[2ull * e] = make_float4(x.x, x.y, x.z, 0.f);
-            B.sray[2ull * e + 1] = make_float4(dir.x, dir.y, dir.z, dist);
-            B.sidx[e] = p * B.L + l;
-            B.sskip[e] = h.slot;
-            B.sreq[e] = req;
         }
-        if (bounce < R.c.num_bounces - 1) {
-            float r1, r2;
-            rng2(R.c, pixel, sample, (uint32_t)bounce, 1u, r1, r2);
-            const float3 nd = cosine_importance(sp.shading_n, r1, r2);
-            B.ray[2ull * p] = make_float4(x.x, x.y, x.z, 0.f);
-            B.ray[2ull * p + 1] = make_float4(nd.x, nd.y, nd.z, 3.402823466e38f);
-            B.skip[p] = h.slot;
-            const float bc = 1.0f - r1;
-            const float4 wt = path_weight(B, p, bounce);
-            B.wgt[(bounce + 1) & 1][p] = make_float4(wt.x * bc, wt.y * bc, wt.z * bc, 0.f);
-            q_out[warp_append(&B.counts[1], 1u)] = p;
-        }
+        const uint2 at = block_append2(&B.counts[2], nl, &B.counts[1], cont ? 1u : 0u);
+        if (live) shade_path(B, bounce, p, req, h, at.x, cont, q_out, at.y);
     }
 }
 
