@@ -113,10 +113,8 @@ struct Batch {
     uint32_t* psample;
     float4* contrib;
     uint8_t* occ;
-    float4* sray;
-    uint32_t* sidx;
-    uint32_t* sskip;
-    uint32_t* sreq;
+    float4* sray;              // shadow ray of path p, light l at p * L + l: (origin, skip slot bits) (dir, tmax)
+    uint2* sidx;               // shadow queue: (p * L + l, request) of each shadow ray to trace, in path order
     float4* pix;               // per-pixel running mean (all render requests)
     uint32_t* taken;
     uint8_t* done;
@@ -267,21 +265,24 @@ struct PrimaryJob {
 struct ShadowJob {
     Batch B;
     struct Item {
-        uint32_t req;
+        uint32_t req, k;
     };
     __device__ SceneView view(const SceneView&, const Item& it) const { return B.rr[it.req].sv; }
     __device__ bool ray(uint32_t i, TRay& r, Item& it) const {
-        const float4 a = B.sray[2ull * i], b = B.sray[2ull * i + 1];
+        const uint2 q = B.sidx[i];
+        const uint32_t k = q.x;
+        const float4 a = B.sray[2ull * k], b = B.sray[2ull * k + 1];
         r.o = f3(a.x, a.y, a.z);
-        r.tmin = a.w;
+        r.tmin = 0.0f;
+        r.skip = __float_as_uint(a.w);
         r.d = f3(b.x, b.y, b.z);
         r.tmax = b.w;
-        r.skip = B.sskip[i];
-        it.req = B.sreq[i];
+        it.req = q.y;
+        it.k = k;
         return true;
     }
-    __device__ void write(const SceneView&, uint32_t i, const TRay&, const THit& h, const Item&) const {
-        if (h.slot != CRT_MISS) B.occ[B.sidx[i]] = 1;
+    __device__ void write(const SceneView&, uint32_t, const TRay&, const THit& h, const Item& it) const {
+        if (h.slot != CRT_MISS) B.occ[it.k] = 1;
     }
 };
 
@@ -388,10 +389,74 @@ __device__ __forceinline__ uint2 block_append2(uint32_t* c0, uint32_t n0, uint32
     return r;
 }
 
-// One live path at bounce `bounce`: surface point, a shadow ray per light at shadow-queue index
-// sbase + l, and when the path continues its bounce ray, appended to q_out at qidx
-__device__ __forceinline__ void shade_path(const Batch& B, int bounce, uint32_t p, uint32_t req, const THit& h,
-                                           uint32_t sbase, bool cont, uint32_t* __restrict__ q_out, uint32_t qidx) {
+__device__ __forceinline__ float maxabs3(float3 a) { return fmaxf(fabsf(a.x), fmaxf(fabsf(a.y), fabsf(a.z))); }
+
+// Flat unit normal of path p's current triangle (xyz) and the distance from its hit point to the
+// nearest edge of the triangle (barycentric x height), less an error margin for the gap between this
+// FP32 hit point and the reference's FP64 one (w): 4e-6 of the incoming ray's coordinates and length
+// over cos(incidence), plus 4e-6 |x| (10x the FP32 rounding of the ray, of the triangle and of the
+// point).  w is NaN for a degenerate triangle.  Reloads the hit and the triangle (cached) instead of
+// keeping them live in k_shade.
+__device__ __forceinline__ float4 edge_clearance(const Batch& B, int bounce, uint32_t p, const RReq& R) {
+    const float4 hv = B.hit[p];
+    const float4* tp = R.sv.tris + 3ull * __float_as_uint(hv.w);
+    const float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
+    const float3 p0 = f3(a.x, a.y, a.z), e1 = f3(a.w, b.x, b.y), e2 = f3(b.z, b.w, c.x), n = f3(c.y, c.z, c.w);
+    const float3 x = p0 - hv.y * e1 + hv.z * e2;   // as surface_point
+    const float an = sqrtf(dot3(n, n));            // twice the area
+    const float w = 1.0f - hv.y - hv.z;
+    const float d1 = hv.y * an / sqrtf(dot3(e2, e2));            // edge p0-p2, opposite p1
+    const float d2 = hv.z * an / sqrtf(dot3(e1, e1));            // edge p0-p1, opposite p2
+    const float d0 = w * an / sqrtf(dot3(e1 + e2, e1 + e2));     // edge p1-p2, opposite p0
+    float3 o_in;
+    if (bounce == 0) o_in = f3(R.cam.o[0], R.cam.o[1], R.cam.o[2]);
+    else {
+        const float4 ro = B.ray[2ull * p];   // this bounce's ray: called only when it was not replaced
+        o_in = f3(ro.x, ro.y, ro.z);
+    }
+    const float3 v_in = x - o_in;
+    const float t_in = sqrtf(dot3(v_in, v_in));
+    const float cos_in = fabsf(dot3(v_in, n)) / (t_in * an);
+    const float margin = 4e-6f * ((maxabs3(o_in) + t_in) / fmaxf(cos_in, 1e-3f) + maxabs3(x));
+    const float3 fn = n * (1.0f / an);   // normalize3(n), as surface_point
+    return make_float4(fn.x, fn.y, fn.z, fminf(fminf(d0, d1), d2) - margin);
+}
+
+// Whether the reference's shadow ray toward `dir` (light at distance `dist`) stops on the triangle it
+// leaves.  The reference starts it at x - 1e-4 n (unidirectional.hpp:55-57, n the flat normal), so
+// for c = d . n > 0 it meets that triangle's plane at t = 1e-4 / c, 1e-4 tan(theta) from x, and the
+// any-hit traversal stops there when that point lies inside the triangle (triangle.hpp:140-160, t in
+// [0, tmax]): the light is occluded by the surface itself.  The device ray starts farther off the
+// surface (origin_offset) and skips that triangle, so the crossing is decided here: inside when the
+// tangential shift is shorter than the edge clearance.  Rays whose crossing lies near an edge are traced.
+__device__ __forceinline__ bool shadow_self_occluded(float3 dir, float dist, float3 flat_n, float clear) {
+    const float c = dot3(dir, flat_n);
+    if (!(c > 1e-3f)) return false;
+    const float shift = 1.01e-4f * sqrtf(fmaxf(0.0f, 1.0f - c * c)) / c;   // 1e-4 tan(theta), +1 %
+    return shift < clear && 1e-4f < 0.5f * dist * c;                       // inside; t = 1e-4 / c < tmax
+}
+
+// Of the shadow rays of path p whose lights are in `into`, those that stop on the path's own triangle
+// (shadow_self_occluded): occluded now, and dropped from the returned mask of rays to trace
+__device__ __noinline__ uint32_t mark_self_occluded(const Batch& B, int bounce, uint32_t p, const RReq& R,
+                                                    uint32_t into, uint32_t keep) {
+    const float4 nc = edge_clearance(B, bounce, p, R);
+    for (uint32_t m = into; m; m &= m - 1) {
+        const uint32_t l = __ffs(m) - 1;
+        const size_t k = (size_t)p * B.L + l;
+        const float4 db = B.sray[2 * k + 1];   // direction and distance as written by shade_path
+        if (shadow_self_occluded(f3(db.x, db.y, db.z), db.w, f3(nc.x, nc.y, nc.z), nc.w)) {
+            B.occ[k] = 1;
+            keep &= ~(1u << l);
+        }
+    }
+    return keep;
+}
+
+// One live path at bounce `bounce`: surface point, a shadow ray per light at p * L + l, and when the
+// path continues its bounce ray.  Returns the lights whose shadow ray has to be traced.
+__device__ __forceinline__ uint32_t shade_path(const Batch& B, int bounce, uint32_t p, uint32_t req, const THit& h,
+                                               bool cont) {
     const RReq& R = B.rr[req];
     const uint32_t pixel = B.ppix[p], sample = B.psample[p];
     const SceneView sv = R.sv;
@@ -400,6 +465,7 @@ __device__ __forceinline__ void shade_path(const Batch& B, int bounce, uint32_t 
     const float3 col = f3(E.color[0], E.color[1], E.color[2]);
     const float3 x = sp.x - origin_offset(sp.x) * sp.flat_n;   // intersect_point - 1e-4 normal
     const uint32_t nl = R.n_lights;
+    uint32_t into = 0;   // lights whose shadow ray points into the surface
     for (uint32_t l = 0; l < nl; ++l) {
         const LightDev& lt = B.lights[R.light_base + l];
         float3 lp = f3(lt.pos[0], lt.pos[1], lt.pos[2]);
@@ -423,12 +489,10 @@ __device__ __forceinline__ void shade_path(const Batch& B, int bounce, uint32_t 
         const float3 cb = col * ldn;
         B.contrib[(size_t)p * B.L + l] = make_float4(cb.x * inten, cb.y * inten, cb.z * inten, 0.f);
         B.occ[(size_t)p * B.L + l] = 0;
-        const uint32_t e = sbase + l;
-        B.sray[2ull * e] = make_float4(x.x, x.y, x.z, 0.f);
-        B.sray[2ull * e + 1] = make_float4(dir.x, dir.y, dir.z, dist);
-        B.sidx[e] = p * B.L + l;
-        B.sskip[e] = h.slot;
-        B.sreq[e] = req;
+        if (ldn < 0.0f) into |= 1u << l;   // towards the surface (shading normal): checked below
+        const size_t k = (size_t)p * B.L + l;
+        B.sray[2 * k] = make_float4(x.x, x.y, x.z, __uint_as_float(h.slot));   // tmin 0; skip the origin triangle
+        B.sray[2 * k + 1] = make_float4(dir.x, dir.y, dir.z, dist);
     }
     if (cont) {
         float r1, r2;
@@ -440,17 +504,22 @@ __device__ __forceinline__ void shade_path(const Batch& B, int bounce, uint32_t 
         const float bc = 1.0f - r1;
         const float4 wt = path_weight(B, p, bounce);
         B.wgt[(bounce + 1) & 1][p] = make_float4(wt.x * bc, wt.y * bc, wt.z * bc, 0.f);
-        q_out[qidx] = p;
     }
+    // self-occluded shadow rays: at bounce 0 (incoming ray from the camera) and at the path's last
+    // bounce (its ray is not replaced above); middle bounces of longer paths are traced as they are
+    const uint32_t all = nl >= 32 ? 0xFFFFFFFFu : (1u << nl) - 1u;
+    return into && (bounce == 0 || !cont) ? mark_self_occluded(B, bounce, p, R, into, all) : all;
 }
 
-// 256-thread blocks (block_append2); the loop's trip count is uniform over a block
+// 256-thread blocks (block_append2); the loop's trip count is uniform over a block.  The shadow queue
+// receives the shadow rays still to trace after the shade, in path order within a block; rays that
+// their own triangle stops (mark_self_occluded) are not queued.
 __global__ void __launch_bounds__(256) k_shade(Batch B, int bounce, const uint32_t* __restrict__ q_in,
                                                uint32_t* __restrict__ q_out) {
     const uint32_t n = bounce == 0 ? B.cur->n_paths : B.counts[0];
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
         const uint32_t i = base + threadIdx.x;
-        uint32_t p = 0, req = 0, nl = 0;
+        uint32_t p = 0, req = 0;
         bool live = false, cont = false;
         THit h;
         h.t = h.u = h.v = 0.f;
@@ -465,11 +534,13 @@ __global__ void __launch_bounds__(256) k_shade(Batch B, int bounce, const uint32
                 const RenderCtl& c = B.rr[req].c;
                 live = bounce < c.num_bounces;
                 cont = bounce < c.num_bounces - 1;
-                nl = live ? B.rr[req].n_lights : 0u;
             }
         }
-        const uint2 at = block_append2(&B.counts[2], nl, &B.counts[1], cont ? 1u : 0u);
-        if (live) shade_path(B, bounce, p, req, h, at.x, cont, q_out, at.y);
+        const uint32_t keep = live ? shade_path(B, bounce, p, req, h, cont) : 0u;
+        const uint2 at = block_append2(&B.counts[2], __popc(keep), &B.counts[1], cont ? 1u : 0u);
+        uint32_t e = at.x;
+        for (uint32_t m = keep; m; m &= m - 1) B.sidx[e++] = make_uint2(p * B.L + (uint32_t)(__ffs(m) - 1), req);
+        if (cont) q_out[at.y] = p;
     }
 }
 
@@ -876,9 +947,7 @@ void run_batch(crt_context* ctx, const crt_request* reqs, size_t n, crt_batch_st
         B.contrib = (float4*)take(P * NL * 16);
         B.occ = (uint8_t*)take(P * NL);
         B.sray = (float4*)take(P * NL * 32);
-        B.sidx = (uint32_t*)take(P * NL * 4);
-        B.sskip = (uint32_t*)take(P * NL * 4);
-        B.sreq = (uint32_t*)take(P * NL * 4);
+        B.sidx = (uint2*)take(P * NL * 8);
         B.pix = (float4*)take((size_t)std::max<uint32_t>(pix_total, 1) * 16);
         B.taken = (uint32_t*)take((size_t)std::max<uint32_t>(pix_total, 1) * 4);
         B.done = (uint8_t*)take(std::max<uint32_t>(pix_total, 1));
@@ -1210,7 +1279,7 @@ struct WaveEngine {
     uint32_t* taken() const { return (uint32_t*)(units_mem + up256(units.cap() * 16)); }
     uint8_t* done() const { return (uint8_t*)(units_mem + up256(units.cap() * 16) + up256(units.cap() * 4)); }
     static size_t path_bytes(size_t P, size_t NL) {
-        return P * (32 + 4 + 16 * 5 + 12 + 8) + P * NL * (16 + 1 + 32 + 12) + 64 * 256;
+        return P * (32 + 4 + 16 * 5 + 12 + 8) + P * NL * (16 + 1 + 32 + 8) + 64 * 256;
     }
 };
 
@@ -1578,12 +1647,10 @@ void engine_step(WaveEngine* e, std::vector<uint64_t>& completed) {
         B.contrib = (float4*)take(P * NL * 16);
         B.occ = (uint8_t*)take(P * NL);
         B.sray = (float4*)take(P * NL * 32);
-        B.sidx = (uint32_t*)take(P * NL * 4);
-        B.sskip = (uint32_t*)take(P * NL * 4);
-        B.sreq = (uint32_t*)take(P * NL * 4);
+        B.sidx = (uint2*)take(P * NL * 8);
     }
     // the two path queues follow the path buffers (path_bytes reserves 8 bytes per path for them)
-    uint32_t* qa = (uint32_t*)((char*)B.sreq + up256(P * NL * 4));
+    uint32_t* qa = (uint32_t*)((char*)B.sidx + up256(P * NL * 8));
     uint32_t* qb = qa + P;
     B.rr = e->d_rr;
     B.lr = e->d_lr;

@@ -125,3 +125,59 @@ def test_asteroid_sun_render_vs_oracle(ctx):
     assert close.mean() > 0.98, close.mean()
     lit = orad[..., 0] > 0
     assert 0.2 < lit.mean() < 0.9
+
+
+def test_open_quad_self_occlusion_matches_oracle(ctx):
+    """A shadow ray that points into the surface it leaves stops on its own triangle in the reference
+    (its origin is 1e-4 off the surface along -n, unidirectional.hpp:55-57), so on an open quad only
+    a light on the offset side contributes; a light on the other side adds nothing, not its negative
+    Lambert term.  Such rays are resolved in the shade stage and never traced."""
+    quad = scenes.quad_mesh((-1.0, 0.0, -0.7), (0.9, 0.0, -1.0), (1.1, 0.0, 0.8), (-0.8, 0.0, 1.0))
+    ents = [scenes.EntitySpec("q", quad, (0.7, 0.5, 0.3))]
+    sc, o = ctx.scene(ents), oracle.Scene(ents)
+    cam = scenes.fov_camera(0.5, (48, 40), (0.05, 3.0, 0.03), (0.0, 0.0, 0.0))
+    blocked = dict(type="point", intensity=3.0, position=[0.3, 2.0, 0.2])    # camera side: behind n's offset
+    lit = dict(type="point", intensity=2.0, position=[-0.2, -2.0, 0.1])
+    _, rad = sc.render(cam, [blocked], 1, 1, 0.0, 1)
+    assert (rad[..., :3] == 0).mean() > 0.995, (rad[..., :3] != 0).mean()
+    _, rad2 = sc.render(cam, [blocked, lit], 1, 1, 0.0, 1)
+    orad2, _, _ = o.render(cam, [blocked, lit], 1, 1, 0.0, 1)
+    assert (orad2[..., 0] > 0).mean() > 0.3
+    close = np.isclose(rad2[..., :3], orad2[..., :3], rtol=1e-4, atol=1e-6).all(-1)
+    assert close.mean() > 0.995, close.mean()
+    # counting build: the blocked light's shadow rays are not traced (at most an edge band is)
+    ctx.set_counting(True)
+    try:
+        ctx.reset_counters()
+        sc.render(cam, [blocked], 1, 1, 0.0, 1)
+        rays = ctx.counters()["rays"]
+    finally:
+        ctx.set_counting(False)
+    hits = int((orad2[..., 0] > 0).sum())
+    assert 48 * 40 <= rays < 48 * 40 + 0.05 * hits, (rays, hits)
+
+
+def test_terminator_shadow_rays_resolved_in_shade(ctx):
+    """Asteroid with the terminator across the view: shadow rays from the night side stop on their
+    own triangle (closed mesh: the traced result would be 'occluded' too), so fewer shadow rays are
+    traced than primary rays hit, and the image equals the oracle's as before."""
+    ents = [scenes.EntitySpec("a", scenes.asteroid(100_000, seed=3), (0.1, 0.1, 0.1))]
+    sc = ctx.scene(ents)
+    view = scenes.unit_vector(12)
+    sun = np.cross(view, scenes.unit_vector(11))
+    sun /= np.linalg.norm(sun)
+    lights = [dict(type="point", intensity=1.0e18, position=1.0e9 * sun)]
+    cam = scenes.fov_camera(scenes.TAN5 * 2.4, (128, 128), 5000.0 * view, (0.0, 0.0, 0.0))
+    ctx.set_counting(True)
+    try:
+        ctx.reset_counters()
+        _, rad = sc.render(cam, lights, 1, 1, 1.0, 1)
+        rays = ctx.counters()["rays"]
+    finally:
+        ctx.set_counting(False)
+    xyz, ids, _ = sc.passes(cam)
+    hits = int((ids > 0).sum())
+    lit = int((rad[..., 0] > 0).sum())
+    shadow = rays - 128 * 128
+    assert lit <= shadow < hits, (lit, shadow, hits)
+    assert shadow < 0.9 * hits
