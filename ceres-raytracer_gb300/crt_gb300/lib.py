@@ -140,6 +140,7 @@ SIGNATURES = {
     "crt_srp": ([vp, ctypes.POINTER(SrpDesc), vp, sz, vp, vp, vp], i32),
     "crt_srp_static": ([vp, ctypes.POINTER(SrpDesc), vp, sz, vp, vp], i32),
     "crt_batch": ([vp, vp, sz, ctypes.POINTER(BatchStats)], i32),
+    "crt_batch_mixed": ([vp, vp, sz, ctypes.POINTER(BatchStats)], i32),
     "crt_context_set_tuning": ([vp, ctypes.POINTER(Tuning)], i32),
     "crt_context_get_tuning": ([vp, ctypes.POINTER(Tuning)], i32),
     "crt_host_alloc": ([sz, ctypes.POINTER(vp)], i32),
@@ -190,6 +191,24 @@ def fill_camera(cam):
     c.sensor_size[:] = [float(x) for x in cam["sensor_size"]]
     c.z_positive = int(bool(cam.get("z_positive", False)))
     return c
+
+
+def fill_srp_request(q, sr, outputs, keep):
+    """Fills the SRP fields of a ServerRequest from a request dict ({"sun_dir", "quaternions", "grid",
+    "num_bounces", "flux", "c", "center_of_mass"}); returns the (force, torque) outputs."""
+    d = SrpDesc()
+    d.sun_dir_inertial[:] = [float(x) for x in q["sun_dir"]]
+    d.flux, d.c = float(q.get("flux", 1361.0)), float(q.get("c", 299792458.0))
+    d.center_of_mass[:] = [float(x) for x in q.get("center_of_mass", (0.0, 0.0, 0.0))]
+    d.grid, d.num_bounces = int(q["grid"]), int(q.get("num_bounces", 2))
+    quats = np.ascontiguousarray(q["quaternions"], dtype=np.float64).reshape(-1, 4)
+    out = outputs or (np.empty((len(quats), 3)), np.empty((len(quats), 3)))
+    keep += [d, quats]
+    sr.base.kind = REQUEST_SRP
+    sr.base.scene = q["scene"].h
+    sr.srp, sr.quaternions, sr.n_att = ctypes.pointer(d), quats.ctypes.data, len(quats)
+    sr.force, sr.torque = ptr(out[0]), ptr(out[1])
+    return out
 
 
 def fill_lights(lights):
@@ -272,16 +291,22 @@ class Context:
                     build_sah=bool(t.build_sah), collapse_tri_cost=round(float(t.collapse_tri_cost), 4))
 
     def batch(self, requests, outputs=None):
-        """Run render / LiDAR requests in one batch.  Each request is a dict:
+        """Run render / LiDAR / SRP requests in one batch.  Each request is a dict:
         {"kind": "render", "scene": Scene, "camera": cam, "lights": [...], "min_samples", "max_samples",
          "noise_threshold", "num_bounces", "seed", "request", "radiance": bool}
         {"kind": "lidar", "scene": Scene, "position", "rotation", "nx", "ny", "half_x", "half_y", "z_positive"}
-        Returns (outputs, stats): outputs[i] = (rgba, radiance) or (range, prim)."""
+        {"kind": "srp", "scene": Scene, "sun_dir", "quaternions", "grid", "num_bounces", "flux", "c",
+         "center_of_mass"}
+        Render / LiDAR only: crt_batch; with SRP requests: crt_batch_mixed (their sun rays share the waves'
+        primary traces).  Returns (outputs, stats): outputs[i] = (rgba, radiance), (range, prim) or
+        (force, torque)."""
         n = len(requests)
-        arr = (Request * max(1, n))()
+        mixed = any(q["kind"] == "srp" for q in requests)
+        sarr = (ServerRequest * max(1, n))() if mixed else None
+        arr = None if mixed else (Request * max(1, n))()
         keep, outs = [], []
         for i, q in enumerate(requests):
-            r = arr[i]
+            r = sarr[i].base if mixed else arr[i]
             r.scene = q["scene"].h
             given = outputs[i] if outputs is not None else None
             if q["kind"] == "render":
@@ -303,6 +328,8 @@ class Context:
                 r.rgba8 = ptr(rgba)
                 r.radiance = ptr(rad)
                 outs.append((rgba, rad))
+            elif q["kind"] == "srp":
+                outs.append(fill_srp_request(q, sarr[i], given, keep))
             else:
                 g = LidarGridDesc()
                 g.position[:] = [float(x) for x in np.asarray(q["position"], dtype=np.float64).ravel()]
@@ -318,7 +345,10 @@ class Context:
                 r.prim = ptr(prim)
                 outs.append((rng, prim))
         st = BatchStats()
-        self._check(self.L.crt_batch(self.h, arr, n, ctypes.byref(st)))
+        if mixed:
+            self._check(self.L.crt_batch_mixed(self.h, sarr, n, ctypes.byref(st)))
+        else:
+            self._check(self.L.crt_batch(self.h, arr, n, ctypes.byref(st)))
         del keep
         return outs, dict(waves=st.waves, render_paths=st.render_paths, lidar_beams=st.lidar_beams)
 
@@ -523,17 +553,7 @@ class Server:
             keep.append(g)
             r.kind, r.lidar, r.range, r.prim = REQUEST_LIDAR, ctypes.pointer(g), ptr(out[0]), ptr(out[1])
         else:
-            d = SrpDesc()
-            d.sun_dir_inertial[:] = [float(x) for x in q["sun_dir"]]
-            d.flux, d.c = float(q.get("flux", 1361.0)), float(q.get("c", 299792458.0))
-            d.center_of_mass[:] = [float(x) for x in q.get("center_of_mass", (0.0, 0.0, 0.0))]
-            d.grid, d.num_bounces = int(q["grid"]), int(q.get("num_bounces", 2))
-            quats = np.ascontiguousarray(q["quaternions"], dtype=np.float64).reshape(-1, 4)
-            out = outputs or (np.empty((len(quats), 3)), np.empty((len(quats), 3)))
-            keep += [d, quats]
-            r.kind = REQUEST_SRP
-            sr.srp, sr.quaternions, sr.n_att = ctypes.pointer(d), quats.ctypes.data, len(quats)
-            sr.force, sr.torque = ptr(out[0]), ptr(out[1])
+            out = fill_srp_request(q, sr, outputs, keep)
         t = ctypes.c_uint64()
         rc = self.L.crt_server_submit(self.h, ctypes.byref(sr), ctypes.byref(t))
         if rc != CRT_OK:

@@ -28,6 +28,7 @@
 // is not re-tested (in FP64 the reference only meets it again when the ray points into the
 // surface, which on closed meshes the rest of the mesh occludes anyway).
 #include "common.cuh"
+#include "srp.cuh"
 #include "trace.cuh"
 
 #include <algorithm>
@@ -35,6 +36,7 @@
 #include <mutex>
 #include <cmath>
 #include <cstring>
+#include <functional>
 #include <vector>
 
 namespace {
@@ -89,8 +91,10 @@ struct Slice {
 
 struct WaveDesc {
     uint32_t n_lidar_items, n_lreq, n_paths, n_primary;
-    uint32_t n_slices, n_update, pad0, pad1;
+    uint32_t n_slices, n_update, n_srp_items, pad0;
     Slice slices[MAX_SLICES];
+    SceneView srp_sv;     // SRP items of the wave (crt_batch_mixed): one request's sun rays, after the
+    SrpWave srp;          // LiDAR beams and camera paths in the primary trace
 };
 
 struct Batch {
@@ -184,13 +188,19 @@ __device__ __forceinline__ bool tile_px(uint32_t i, uint32_t W, uint32_t H, uint
 }
 
 // ---------------------------------------------------------------- primary stage
-struct PrimaryJob {
+// Primary segment of a wave: items [0, LiDAR) are beams, then camera paths, then (SRP) the sun rays
+// of the wave's SRP request.  Batches without SRP requests use the SRP = false instantiation.
+template <bool SRP>
+struct PrimaryJobT {
     Batch B;
     struct Item {
         uint32_t req;
-        uint32_t lidar;
+        uint32_t lidar;   // 0 camera path, 1 LiDAR beam, 2 SRP sun ray
     };
-    __device__ SceneView view(const SceneView&, const Item& it) const { return it.lidar ? B.lr[it.req].sv : B.rr[it.req].sv; }
+    __device__ SceneView view(const SceneView&, const Item& it) const {
+        if (SRP && it.lidar == 2) return B.cur->srp_sv;
+        return it.lidar ? B.lr[it.req].sv : B.rr[it.req].sv;
+    }
     __device__ void beam64(const LReq& L, uint32_t px, uint32_t py, double d[3]) const {
         const double s0 = B.tan[L.tan_base + px], s1 = B.tan[L.tan_base + L.nx + py], s2 = L.zsign;
         const double inv = rsqrt64(s0 * s0 + s1 * s1 + s2 * s2);
@@ -218,6 +228,13 @@ struct PrimaryJob {
             it.lidar = 1;
             return true;
         }
+        if (SRP && i >= w.n_lidar_items + w.n_paths) {
+            const uint32_t k = i - w.n_lidar_items - w.n_paths;
+            if (!srp_primary_ray(w.srp, k, r)) return false;
+            it.req = k;
+            it.lidar = 2;
+            return true;
+        }
         const uint32_t p = i - w.n_lidar_items;
         const Slice& S = w.slices[find_slice_by_path(w, p)];
         const uint32_t q = p - S.path_base;
@@ -241,6 +258,10 @@ struct PrimaryJob {
         return true;
     }
     __device__ void write(const SceneView&, uint32_t i, const TRay&, const THit& h, const Item& it) const {
+        if (SRP && it.lidar == 2) {
+            B.cur->srp.hit[it.req] = make_float4(h.t, h.u, h.v, __uint_as_float(h.slot));
+            return;
+        }
         if (it.lidar) {
             const LReq& L = B.lr[it.req];
             uint32_t px, py;
@@ -711,15 +732,26 @@ inline uint32_t tiles_items(uint32_t W, uint32_t H) { return ((W + 7) / 8) * ((H
 // The stage sequence of one wave on the context stream.  Every launch reads the wave from B.cur
 // (filled by k_wave_begin from B.descs[*B.wave_idx]), so the sequence can be captured once and
 // replayed.  P: path capacity, NL: light stride, lidar_items: bound on the wave's LiDAR items.
+// srp_items: bound on the wave's SRP items (crt_batch_mixed); when non-zero the primary trace also
+// traces the wave's SRP sun rays and srp_stages (host launches of that wave's SRP shade and
+// specular segments) runs right after it, so such waves are launched one by one, not replayed.
 void launch_wave_kernels(crt_context* ctx, const Batch& B, size_t P, size_t NL, uint32_t lidar_items,
-                         int max_bounces, uint32_t* qa, uint32_t* qb, uint32_t* tqueue) {
+                         int max_bounces, uint32_t* qa, uint32_t* qb, uint32_t* tqueue, uint32_t srp_items = 0,
+                         const std::function<void()>* srp_stages = nullptr) {
     cudaStream_t st = ctx->stream;
     const uint32_t g_shade = grid_for(ctx, k_shade, P), g_accum = grid_for(ctx, k_accum, P);
     const uint32_t g_update = max_bounces <= 1 ? grid_for(ctx, k_update<true>, P) : grid_for(ctx, k_update<false>, P);
     k_wave_begin<<<1, 128, 0, st>>>(B);
     check_launch(ctx, "k_wave_begin");
-    launch_trace<false>(ctx, SceneView{}, PrimaryJob{B}, (uint32_t)std::min<size_t>(P + lidar_items, 0xFFFFFF00u),
-                        &B.cur->n_primary, tqueue);
+    if (srp_items) {
+        launch_trace<false>(ctx, SceneView{}, PrimaryJobT<true>{B},
+                            (uint32_t)std::min<size_t>(P + lidar_items + srp_items, 0xFFFFFF00u), &B.cur->n_primary,
+                            tqueue);
+        if (srp_stages) (*srp_stages)();
+    } else {
+        launch_trace<false>(ctx, SceneView{}, PrimaryJobT<false>{B},
+                            (uint32_t)std::min<size_t>(P + lidar_items, 0xFFFFFF00u), &B.cur->n_primary, tqueue);
+    }
     const uint32_t* q_in = nullptr;
     uint32_t* q_out = qa;
     const bool fuse = max_bounces <= 1;   // k_update adds the light of the only bounce (if any)
@@ -779,13 +811,25 @@ void check_request(const crt_request& q) {
     }
 }
 
-void run_batch(crt_context* ctx, const crt_request* reqs, size_t n, crt_batch_stats* stats) {
+// srps: SRP requests of a mixed batch (crt_batch_mixed); their sun rays ride in the waves' primary
+// traces after the LiDAR beams and camera paths, one request's item range per wave.
+void run_batch(crt_context* ctx, const crt_request* reqs, size_t n, crt_batch_stats* stats,
+               const crt_server_request* const* srps = nullptr, size_t n_srp = 0) {
     for (size_t i = 0; i < n; ++i) {
         check_request(reqs[i]);
         CRT_CHECK(reqs[i].scene->ctx && reqs[i].scene->ctx->device == ctx->device, CRT_ERR_INVALID,
                   "request scene lives on another device");
     }
-    if (!n) return;
+    std::vector<SrpPlan> splans(n_srp);
+    for (size_t j = 0; j < n_srp; ++j) {
+        const crt_server_request& q = *srps[j];
+        CRT_CHECK(q.base.scene && q.srp && (q.n_att == 0 || (q.quaternions && q.force && q.torque)), CRT_ERR_INVALID,
+                  "incomplete SRP request");
+        CRT_CHECK(q.base.scene->ctx && q.base.scene->ctx->device == ctx->device, CRT_ERR_INVALID,
+                  "request scene lives on another device");
+        srp_plan(q.base.scene, q.srp, q.quaternions, q.n_att, splans[j]);
+    }
+    if (!n && !n_srp) return;
     CRT_CUDA(cudaSetDevice(ctx->device));
     cudaStream_t st = ctx->stream;
 
@@ -903,8 +947,30 @@ void run_batch(crt_context* ctx, const crt_request* reqs, size_t n, crt_batch_st
     if (plan.back().n_slices == 0 && plan.size() > 1) plan.pop_back();
     plan[0].n_lidar_items = lidar_items;
     plan[0].n_lreq = (uint32_t)lr.size();
+    // SRP: each request's items cut into ranges of at most the wave size (whole attitudes, or a part of
+    // one attitude); range k rides in wave k, with waves of SRP items only when there are more ranges
+    struct SrpRange {
+        size_t req;
+        uint64_t i0, n;
+    };
+    std::vector<SrpRange> sranges;
+    uint64_t srp_max = 0;
+    uint32_t srp_nb = 0;
+    const uint64_t srp_cap = std::max<uint64_t>((uint64_t)cap / SRP_BLOCK_ITEMS * SRP_BLOCK_ITEMS, SRP_BLOCK_ITEMS);
+    for (size_t j = 0; j < n_srp; ++j) {
+        const SrpPlan& SP = splans[j];
+        for (uint64_t i0 = 0; i0 < SP.total;) {
+            const uint64_t m = srp_wave_items(SP, srp_cap, i0);
+            sranges.push_back(SrpRange{j, i0, m});
+            srp_max = std::max(srp_max, m);
+            i0 += m;
+        }
+        srp_nb = std::max(srp_nb, SP.nb);
+    }
+    while (plan.size() < sranges.size()) new_wave();
+    for (size_t k = 0; k < sranges.size(); ++k) plan[k].n_srp_items = (uint32_t)sranges[k].n;
     for (WaveDesc& w : plan) {
-        w.n_primary = w.n_lidar_items + w.n_paths;
+        w.n_primary = w.n_lidar_items + w.n_paths + w.n_srp_items;
         max_paths = std::max(max_paths, w.n_paths);
     }
     bool any_adaptive = false;
@@ -919,6 +985,11 @@ void run_batch(crt_context* ctx, const crt_request* reqs, size_t n, crt_batch_st
     char* base = nullptr;
     Batch B;
     std::memset(&B, 0, sizeof(B));
+    std::vector<SrpAtt*> s_att(n_srp);
+    std::vector<double*> s_partial(n_srp), s_force(n_srp), s_torque(n_srp);
+    char* s_state = nullptr;
+    uint32_t* s_bq = nullptr;
+    uint32_t* s_bcount = nullptr;
     auto carve = [&](char* b) {
         size_t off = 0;
         auto take = [&](size_t bytes) {
@@ -951,6 +1022,19 @@ void run_batch(crt_context* ctx, const crt_request* reqs, size_t n, crt_batch_st
         B.pix = (float4*)take((size_t)std::max<uint32_t>(pix_total, 1) * 16);
         B.taken = (uint32_t*)take((size_t)std::max<uint32_t>(pix_total, 1) * 4);
         B.done = (uint8_t*)take(std::max<uint32_t>(pix_total, 1));
+        for (size_t j = 0; j < n_srp; ++j) {   // SRP: attitude table, partial sums, staged outputs
+            const SrpPlan& SP = splans[j];
+            const size_t na = std::max<size_t>(SP.n_att(), 1);
+            s_att[j] = (SrpAtt*)take(sizeof(SrpAtt) * na);
+            s_partial[j] = (double*)take(sizeof(double) * 6 * std::max<uint64_t>(SP.blocks_per_att, 1) * na);
+            s_force[j] = is_device_ptr(srps[j]->force) ? srps[j]->force : (double*)take(24 * na);
+            s_torque[j] = is_device_ptr(srps[j]->torque) ? srps[j]->torque : (double*)take(24 * na);
+        }
+        if (n_srp) {   // one wave's SRP item state, shared by the requests' ranges
+            s_state = (char*)take(std::max<uint64_t>(srp_max, 1) * (srp_nb ? 16 + 16 + 16 + 1 : 16) + 1024);
+            s_bq = srp_nb ? (uint32_t*)take(srp_max * 4 + 256) : nullptr;
+            s_bcount = (uint32_t*)take(256);
+        }
         return off;
     };
     const size_t total_bytes = carve(nullptr);
@@ -991,9 +1075,17 @@ void run_batch(crt_context* ctx, const crt_request* reqs, size_t n, crt_batch_st
     }
     if (host_out_bytes) CRT_CHECK(stage_off <= host_out_bytes + 64 * n, CRT_ERR_INVALID, "staging overflow");
 
+    for (size_t k = 0; k < sranges.size(); ++k) {
+        const SrpRange& R = sranges[k];
+        plan[k].srp_sv = scene_view(srps[R.req]->base.scene);
+        plan[k].srp = srp_wave(splans[R.req], s_att[R.req], s_state, srp_max, R.i0, R.n);
+    }
+
     // ---- uploads (pinned staging ring: no wait for the previous call's kernels)
+    size_t srp_up = 0;
+    for (const SrpPlan& SP : splans) srp_up += sizeof(SrpAtt) * SP.n_att() + 256;
     const size_t up_bytes = sizeof(RReq) * rr.size() + sizeof(LReq) * lr.size() + sizeof(LightDev) * lights.size() +
-                            WD * plan.size() + 1024;
+                            WD * plan.size() + srp_up + 1024;
     PinnedStaging staging(ctx, up_bytes);
     char* pin = staging.p;
     size_t po = 0;
@@ -1007,6 +1099,7 @@ void run_batch(crt_context* ctx, const crt_request* reqs, size_t n, crt_batch_st
     up(B.lr, lr.data(), sizeof(LReq) * lr.size());
     up(B.lights, lights.data(), sizeof(LightDev) * lights.size());
     up(B.descs, plan.data(), WD * plan.size());
+    for (size_t j = 0; j < n_srp; ++j) up(s_att[j], splans[j].att.data(), sizeof(SrpAtt) * splans[j].n_att());
     staging.release();   // the adaptive loop below rewrites `pin` only after synchronising the stream
     CRT_CUDA(cudaMemsetAsync(B.wave_idx, 0, 4, st));
     if (pix_total) {
@@ -1033,7 +1126,7 @@ void run_batch(crt_context* ctx, const crt_request* reqs, size_t n, crt_batch_st
     auto launch_wave = [&]() { launch_wave_kernels(ctx, B, P, NL, lidar_items, max_bounces, qa, qb, tqueue); };
 
     size_t waves_run = 0;
-    const bool graph_ok = ctx->use_graphs && !ctx->counting && plan.size() > 1;
+    const bool graph_ok = ctx->use_graphs && !ctx->counting && plan.size() > 1 && n_srp == 0;
     if (graph_ok) {
         // capture one wave, replay it for every wave of the plan
         cudaGraph_t g = nullptr;
@@ -1057,6 +1150,22 @@ void run_batch(crt_context* ctx, const crt_request* reqs, size_t n, crt_batch_st
             ctx->launches += per_wave;
         }
         cudaGraphExecDestroy(ge);
+        waves_run = plan.size();
+    } else if (n_srp) {
+        // waves with SRP items: the SRP stages of the wave's range follow its primary trace
+        for (size_t w = 0; w < plan.size(); ++w) {
+            std::function<void()> stages;
+            if (w < sranges.size()) {
+                const SrpRange& R = sranges[w];
+                crt_scene* sc = srps[R.req]->base.scene;
+                stages = [&, w, sc]() {
+                    srp_wave_stages(ctx, scene_view(sc), plan[w].srp, (uint32_t)R.n, splans[R.req], s_partial[R.req],
+                                    nullptr, (uint32_t)sc->n_tris, s_bq, s_bcount);
+                };
+            }
+            launch_wave_kernels(ctx, B, P, NL, lidar_items, max_bounces, qa, qb, tqueue,
+                                (uint32_t)std::max<uint64_t>(srp_max, 1), stages ? &stages : nullptr);
+        }
         waves_run = plan.size();
     } else {
         for (size_t w = 0; w < plan.size(); ++w) launch_wave();
@@ -1131,6 +1240,12 @@ void run_batch(crt_context* ctx, const crt_request* reqs, size_t n, crt_batch_st
             if ((void*)Lq.range != (void*)q.range) { out_finish(ctx, q.range, Lq.range, (size_t)Lq.nx * Lq.ny * 8); host_out = true; }
             if (q.prim && (void*)Lq.prim != (void*)q.prim) { out_finish(ctx, q.prim, Lq.prim, (size_t)Lq.nx * Lq.ny * 4); host_out = true; }
         }
+    }
+    for (size_t j = 0; j < n_srp; ++j) {   // per-attitude totals in a fixed order, as crt_srp
+        const crt_server_request& q = *srps[j];
+        srp_reduce(ctx, s_partial[j], splans[j], s_force[j], s_torque[j]);
+        if (s_force[j] != q.force) { out_finish(ctx, q.force, s_force[j], q.n_att * 24); host_out = true; }
+        if (s_torque[j] != q.torque) { out_finish(ctx, q.torque, s_torque[j], q.n_att * 24); host_out = true; }
     }
     if (stats) {
         stats->waves = waves_run;
@@ -1839,6 +1954,19 @@ void batch_check_request(const crt_request& q) { check_request(q); }
 extern "C" int crt_batch(crt_context* ctx, const crt_request* reqs, size_t n, crt_batch_stats* stats) {
     if (!ctx || (n && !reqs)) return CRT_ERR_INVALID;
     return crt_guard(ctx, [&] { run_batch(ctx, reqs, n, stats); });
+}
+
+extern "C" int crt_batch_mixed(crt_context* ctx, const crt_server_request* reqs, size_t n, crt_batch_stats* stats) {
+    if (!ctx || (n && !reqs)) return CRT_ERR_INVALID;
+    return crt_guard(ctx, [&] {
+        std::vector<crt_request> base;
+        std::vector<const crt_server_request*> srp;
+        for (size_t i = 0; i < n; ++i) {
+            if (reqs[i].base.kind == CRT_REQUEST_SRP) srp.push_back(&reqs[i]);
+            else base.push_back(reqs[i].base);
+        }
+        run_batch(ctx, base.data(), base.size(), stats, srp.data(), srp.size());
+    });
 }
 
 extern "C" int crt_render(crt_scene* s, const crt_camera_desc* cam, const crt_light_desc* lights, uint32_t n_lights,

@@ -21,6 +21,7 @@
 // facet powers are summed per facet within a warp (FP32, at most 32 terms) and added with FP64
 // atomics (reproducible up to the order of additions); warps whose rays all missed skip that step.
 #include "common.cuh"
+#include "srp.cuh"
 #include "trace.cuh"
 
 #include <cmath>
@@ -29,15 +30,6 @@
 namespace {
 
 constexpr uint32_t CHUNK = 16;   // tiles per work grab (at most)
-
-struct SrpAtt {
-    float org[3];   // centre of cell (0, 0)
-    float du[3];    // step to the next cell in x
-    float dv[3];    // step to the next cell in y
-    float dir[3];   // -s_b
-    float E0;       // flux * cell area
-    float pad;
-};
 
 struct SrpArgs {
     const SrpAtt* att;
@@ -201,56 +193,11 @@ __global__ void k_srp_reduce(const double* __restrict__ partial, uint32_t grabs_
 // torque of items [b * SRP_BLOCK_ITEMS, (b + 1) * SRP_BLOCK_ITEMS) in a fixed order into partial slot
 // b of the attitude.  Specular continuations stay at their item index, so every sum is independent
 // of scheduling and the results are bitwise reproducible.
-constexpr uint32_t SRP_BLOCK_ITEMS = 1024;
 constexpr uint32_t SRP_SHADE_THREADS = 256;
-
-struct SrpWave {
-    const SrpAtt* att;
-    uint32_t G, tiles_x, tiles;
-    uint32_t items_per_att;   // multiple of SRP_BLOCK_ITEMS
-    uint64_t i0;              // first item of the wave
-    uint32_t a0, r0;          // i0 = a0 * items_per_att + r0
-    uint32_t multi;           // the wave holds whole attitudes (r0 == 0) rather than part of one
-    float4* hit;              // per wave item: t, u, v, slot
-    float4* st_o;             // continuing ray: origin, power
-    float4* st_d;             // continuing ray: direction, triangle it leaves
-    uint8_t* alive;           // continuing ray present
-};
-
-// attitude of wave item i (32-bit arithmetic: a wave is whole attitudes or a part of one)
-__device__ __forceinline__ uint32_t srp_att(const SrpWave& W, uint32_t i, uint32_t& local) {
-    if (W.multi) {
-        const uint32_t q = i / W.items_per_att;
-        local = i - q * W.items_per_att;
-        return W.a0 + q;
-    }
-    local = W.r0 + i;
-    return W.a0;
-}
-
-__device__ __forceinline__ bool srp_item(const SrpWave& W, uint32_t i, uint32_t& a, uint32_t& px, uint32_t& py) {
-    uint32_t local;
-    a = srp_att(W, i, local);
-    const uint32_t tile = local >> 5, lane = local & 31u;
-    if (tile >= W.tiles) return false;
-    px = (tile % W.tiles_x) * 8u + (lane & 7u);
-    py = (tile / W.tiles_x) * 4u + (lane >> 3);
-    return px < W.G && py < W.G;
-}
 
 struct SrpPrimaryJob : JobBase {
     SrpWave W;
-    __device__ bool ray(uint32_t i, TRay& r, Item&) const {
-        uint32_t a, px, py;
-        if (!srp_item(W, i, a, px, py)) return false;
-        const SrpAtt& P = W.att[a];
-        r.o = f3(P.org[0] + px * P.du[0] + py * P.dv[0], P.org[1] + px * P.du[1] + py * P.dv[1],
-                 P.org[2] + px * P.du[2] + py * P.dv[2]);
-        r.d = f3(P.dir[0], P.dir[1], P.dir[2]);
-        r.tmin = 0.f;
-        r.tmax = 3.402823466e38f;
-        return true;
-    }
+    __device__ bool ray(uint32_t i, TRay& r, Item&) const { return srp_primary_ray(W, i, r); }
     __device__ void write(const SceneView&, uint32_t i, const TRay&, const THit& h, const Item&) const {
         W.hit[i] = make_float4(h.t, h.u, h.v, __uint_as_float(h.slot));
     }
@@ -416,149 +363,177 @@ __global__ void __launch_bounds__(SRP_SHADE_THREADS) k_srp_shade(SceneView sv, S
 
 }  // namespace
 
+void srp_plan(crt_scene* s, const crt_srp_desc* desc, const double* quats, size_t n_att, SrpPlan& P) {
+    CRT_CHECK(n_att == 0 || quats, CRT_ERR_INVALID, "null buffer");
+    CRT_CHECK(desc->grid > 0 && desc->grid <= 32768, CRT_ERR_INVALID, "grid must be in [1, 32768]");
+    CRT_CHECK(desc->c > 0 && std::isfinite(desc->flux), CRT_ERR_INVALID, "bad flux or speed of light");
+    CRT_CHECK(desc->num_bounces <= 16, CRT_ERR_INVALID, "at most 16 specular bounces");
+    const double sl = std::sqrt(desc->sun_dir_inertial[0] * desc->sun_dir_inertial[0] +
+                                desc->sun_dir_inertial[1] * desc->sun_dir_inertial[1] +
+                                desc->sun_dir_inertial[2] * desc->sun_dir_inertial[2]);
+    CRT_CHECK(sl > 0 && std::isfinite(sl), CRT_ERR_INVALID, "sun direction must be a non-zero vector");
+    const double si[3] = {desc->sun_dir_inertial[0] / sl, desc->sun_dir_inertial[1] / sl,
+                          desc->sun_dir_inertial[2] / sl};
+    // body-frame box of the scene
+    double lo[3], hi[3], ctr[3];
+    for (int k = 0; k < 3; ++k) {
+        lo[k] = s->bounds[k];
+        hi[k] = s->bounds[3 + k];
+        ctr[k] = 0.5 * (lo[k] + hi[k]);
+    }
+    const double Rb = 0.5 * std::sqrt((hi[0] - lo[0]) * (hi[0] - lo[0]) + (hi[1] - lo[1]) * (hi[1] - lo[1]) +
+                                      (hi[2] - lo[2]) * (hi[2] - lo[2]));
+    const uint32_t G = desc->grid;
+    const double h = 2.0 * Rb / G;
+    std::vector<double> hq(4 * n_att);
+    if (n_att && is_device_ptr(quats)) {
+        CRT_CUDA(cudaMemcpy(hq.data(), quats, 32 * n_att, cudaMemcpyDeviceToHost));
+    } else {
+        std::copy(quats, quats + 4 * n_att, hq.begin());
+    }
+    P.att.resize(n_att);
+    for (size_t a = 0; a < n_att; ++a) {
+        double w = hq[4 * a], x = hq[4 * a + 1], y = hq[4 * a + 2], z = hq[4 * a + 3];
+        const double qn = std::sqrt(w * w + x * x + y * y + z * z);
+        CRT_CHECK(qn > 0 && std::isfinite(qn), CRT_ERR_INVALID, "attitude quaternion must be non-zero");
+        w /= qn; x /= qn; y /= qn; z /= qn;
+        // R(q) maps body vectors into the inertial frame; s_b = R^T s_i
+        const double R[9] = {1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y),
+                             2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x),
+                             2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)};
+        double sb[3];
+        for (int k = 0; k < 3; ++k) sb[k] = R[k] * si[0] + R[3 + k] * si[1] + R[6 + k] * si[2];
+        // grid basis perpendicular to s_b (same construction as the oracle)
+        double ax[3] = {1, 0, 0};
+        if (std::fabs(sb[0]) >= 0.9) { ax[0] = 0; ax[1] = 1; }
+        double e1[3] = {sb[1] * ax[2] - sb[2] * ax[1], sb[2] * ax[0] - sb[0] * ax[2], sb[0] * ax[1] - sb[1] * ax[0]};
+        const double l1 = std::sqrt(e1[0] * e1[0] + e1[1] * e1[1] + e1[2] * e1[2]);
+        for (int k = 0; k < 3; ++k) e1[k] /= l1;
+        const double e2[3] = {sb[1] * e1[2] - sb[2] * e1[1], sb[2] * e1[0] - sb[0] * e1[2], sb[0] * e1[1] - sb[1] * e1[0]};
+        for (int k = 0; k < 3; ++k) {
+            const double o0 = ctr[k] + sb[k] * (2.0 * Rb + 1.0) + e1[k] * (-Rb + 0.5 * h) + e2[k] * (-Rb + 0.5 * h);
+            P.att[a].org[k] = (float)o0;
+            P.att[a].du[k] = (float)(e1[k] * h);
+            P.att[a].dv[k] = (float)(e2[k] * h);
+            P.att[a].dir[k] = (float)(-sb[k]);
+        }
+        P.att[a].E0 = (float)(desc->flux * h * h);
+        P.att[a].pad = 0.f;
+    }
+    P.G = G;
+    P.tiles_x = (G + 7) / 8;
+    P.tiles = P.tiles_x * ((G + 3) / 4);
+    P.ipa = ((uint64_t)P.tiles * 32 + SRP_BLOCK_ITEMS - 1) / SRP_BLOCK_ITEMS * SRP_BLOCK_ITEMS;
+    P.total = P.ipa * n_att;
+    P.blocks_per_att = P.ipa / SRP_BLOCK_ITEMS;
+    CRT_CHECK(P.blocks_per_att * n_att < (1ull << 31), CRT_ERR_INVALID, "too many rays in one call");
+    // specular continuations only when some entity reflects specularly
+    bool specular = false;
+    for (const EntityDev& E : s->host_entities) specular |= E.rho_s > 0.f;
+    P.nb = specular ? desc->num_bounces : 0u;
+    P.inv_c = (float)(1.0 / desc->c);
+    for (int k = 0; k < 3; ++k) P.cm[k] = (float)desc->center_of_mass[k];
+}
+
+uint64_t srp_wave_items(const SrpPlan& P, uint64_t cap, uint64_t i0) {
+    const uint64_t att_per_wave = P.ipa <= cap ? cap / P.ipa : 0;
+    return att_per_wave ? std::min<uint64_t>(att_per_wave * P.ipa, P.total - i0)
+                        : std::min<uint64_t>(cap, P.ipa - i0 % P.ipa);
+}
+
+SrpWave srp_wave(const SrpPlan& P, const SrpAtt* d_att, char* state, uint64_t cap, uint64_t i0, uint64_t n) {
+    SrpWave W;
+    W.att = d_att;
+    W.G = P.G;
+    W.tiles_x = P.tiles_x;
+    W.tiles = P.tiles;
+    W.items_per_att = (uint32_t)P.ipa;
+    W.i0 = i0;
+    W.a0 = (uint32_t)(i0 / P.ipa);
+    W.r0 = (uint32_t)(i0 % P.ipa);
+    W.multi = (W.r0 == 0 && n >= P.ipa) ? 1u : 0u;   // whole attitudes, else a part of one
+    W.hit = (float4*)state;
+    W.st_o = P.nb ? (float4*)(state + cap * 16) : nullptr;
+    W.st_d = P.nb ? (float4*)(state + cap * 32) : nullptr;
+    W.alive = P.nb ? (uint8_t*)(state + cap * 48) : nullptr;
+    return W;
+}
+
+void srp_wave_stages(crt_context* ctx, const SceneView& sv, const SrpWave& W, uint32_t n, const SrpPlan& P,
+                     double* partial, double* facet, uint32_t n_tris, uint32_t* bq, uint32_t* bcount) {
+    cudaStream_t st = ctx->stream;
+    SrpShadeArgs A;
+    A.n_items = n;
+    A.nb = P.nb;
+    A.inv_c = P.inv_c;
+    for (int k = 0; k < 3; ++k) A.cm[k] = P.cm[k];
+    A.partial = partial;
+    A.facet = facet;
+    A.n_tris = n_tris;
+    A.q_out = bq;
+    const uint32_t nblk = (n + SRP_BLOCK_ITEMS - 1) / SRP_BLOCK_ITEMS;
+    for (uint32_t seg = 0; seg <= P.nb; ++seg) {
+        A.seg = seg;
+        A.q_count = bcount + (seg & 1);          // filled by this segment's shade
+        if (seg < P.nb) CRT_CUDA(cudaMemsetAsync(A.q_count, 0, sizeof(uint32_t), st));
+        if (seg == 0) {
+            k_srp_shade<true><<<nblk, SRP_SHADE_THREADS, 0, st>>>(sv, W, A);
+        } else {
+            // the queue filled by the previous segment's shade; its count stays on the device
+            SrpBounceJob J;
+            J.W = W;
+            J.q = bq;
+            launch_trace<false>(ctx, sv, J, n, bcount + ((seg - 1) & 1));
+            k_srp_shade<false><<<nblk, SRP_SHADE_THREADS, 0, st>>>(sv, W, A);
+        }
+        check_launch(ctx, "k_srp_shade");
+    }
+}
+
+void srp_reduce(crt_context* ctx, const double* partial, const SrpPlan& P, double* force, double* torque) {
+    if (!P.n_att()) return;
+    k_srp_reduce<<<(uint32_t)P.n_att(), 256, 0, ctx->stream>>>(partial, (uint32_t)P.blocks_per_att, force, torque);
+    check_launch(ctx, "k_srp_reduce");
+}
+
 // Runs on `ctx` (stream, scratch, error word), which may differ from the scene's own context on the
 // same device (serving lanes).  Throws CrtError.
 void srp_run(crt_context* ctx, crt_scene* s, const crt_srp_desc* desc, const double* quats, size_t n_att,
              double* force, double* torque, double* facet_power) {
     [&] {
         CRT_CHECK(n_att == 0 || (quats && force && torque), CRT_ERR_INVALID, "null buffer");
-        CRT_CHECK(desc->grid > 0 && desc->grid <= 32768, CRT_ERR_INVALID, "grid must be in [1, 32768]");
-        CRT_CHECK(desc->c > 0 && std::isfinite(desc->flux), CRT_ERR_INVALID, "bad flux or speed of light");
-        CRT_CHECK(desc->num_bounces <= 16, CRT_ERR_INVALID, "at most 16 specular bounces");
-        if (!n_att) return;
         CRT_CUDA(cudaSetDevice(ctx->device));
+        SrpPlan P;
+        srp_plan(s, desc, quats, n_att, P);
+        if (!n_att) return;
         cudaStream_t st = ctx->stream;
-        const double sl = std::sqrt(desc->sun_dir_inertial[0] * desc->sun_dir_inertial[0] +
-                                    desc->sun_dir_inertial[1] * desc->sun_dir_inertial[1] +
-                                    desc->sun_dir_inertial[2] * desc->sun_dir_inertial[2]);
-        CRT_CHECK(sl > 0 && std::isfinite(sl), CRT_ERR_INVALID, "sun direction must be a non-zero vector");
-        const double si[3] = {desc->sun_dir_inertial[0] / sl, desc->sun_dir_inertial[1] / sl,
-                              desc->sun_dir_inertial[2] / sl};
-        // body-frame box of the scene
-        double lo[3], hi[3], ctr[3];
-        for (int k = 0; k < 3; ++k) {
-            lo[k] = s->bounds[k];
-            hi[k] = s->bounds[3 + k];
-            ctr[k] = 0.5 * (lo[k] + hi[k]);
-        }
-        const double Rb = 0.5 * std::sqrt((hi[0] - lo[0]) * (hi[0] - lo[0]) + (hi[1] - lo[1]) * (hi[1] - lo[1]) +
-                                          (hi[2] - lo[2]) * (hi[2] - lo[2]));
-        const uint32_t G = desc->grid;
-        const double h = 2.0 * Rb / G;
-        std::vector<double> hq(4 * n_att);
-        if (is_device_ptr(quats)) {
-            CRT_CUDA(cudaMemcpy(hq.data(), quats, 32 * n_att, cudaMemcpyDeviceToHost));
-        } else {
-            std::copy(quats, quats + 4 * n_att, hq.begin());
-        }
-        std::vector<SrpAtt> att(n_att);
-        for (size_t a = 0; a < n_att; ++a) {
-            double w = hq[4 * a], x = hq[4 * a + 1], y = hq[4 * a + 2], z = hq[4 * a + 3];
-            const double qn = std::sqrt(w * w + x * x + y * y + z * z);
-            CRT_CHECK(qn > 0 && std::isfinite(qn), CRT_ERR_INVALID, "attitude quaternion must be non-zero");
-            w /= qn; x /= qn; y /= qn; z /= qn;
-            // R(q) maps body vectors into the inertial frame; s_b = R^T s_i
-            const double R[9] = {1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y),
-                                 2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x),
-                                 2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)};
-            double sb[3];
-            for (int k = 0; k < 3; ++k) sb[k] = R[k] * si[0] + R[3 + k] * si[1] + R[6 + k] * si[2];
-            // grid basis perpendicular to s_b (same construction as the oracle)
-            double ax[3] = {1, 0, 0};
-            if (std::fabs(sb[0]) >= 0.9) { ax[0] = 0; ax[1] = 1; }
-            double e1[3] = {sb[1] * ax[2] - sb[2] * ax[1], sb[2] * ax[0] - sb[0] * ax[2], sb[0] * ax[1] - sb[1] * ax[0]};
-            const double l1 = std::sqrt(e1[0] * e1[0] + e1[1] * e1[1] + e1[2] * e1[2]);
-            for (int k = 0; k < 3; ++k) e1[k] /= l1;
-            const double e2[3] = {sb[1] * e1[2] - sb[2] * e1[1], sb[2] * e1[0] - sb[0] * e1[2], sb[0] * e1[1] - sb[1] * e1[0]};
-            for (int k = 0; k < 3; ++k) {
-                const double o0 = ctr[k] + sb[k] * (2.0 * Rb + 1.0) + e1[k] * (-Rb + 0.5 * h) + e2[k] * (-Rb + 0.5 * h);
-                att[a].org[k] = (float)o0;
-                att[a].du[k] = (float)(e1[k] * h);
-                att[a].dv[k] = (float)(e2[k] * h);
-                att[a].dir[k] = (float)(-sb[k]);
-            }
-            att[a].E0 = (float)(desc->flux * h * h);
-            att[a].pad = 0.f;
-        }
-        const uint32_t tiles_x = (G + 7) / 8, tiles = tiles_x * ((G + 3) / 4);
-        const uint64_t ipa = ((uint64_t)tiles * 32 + SRP_BLOCK_ITEMS - 1) / SRP_BLOCK_ITEMS * SRP_BLOCK_ITEMS;
-        const uint64_t total = ipa * n_att;
-        const uint64_t blocks_per_att = ipa / SRP_BLOCK_ITEMS;
-        CRT_CHECK(blocks_per_att * n_att < (1ull << 31), CRT_ERR_INVALID, "too many rays in one call");
         // a wave: whole attitudes, or a part of one attitude, of up to 2^24 items (about 50 bytes of
         // state each); always a multiple of the reduction block
-        const uint32_t wave_cap = 1u << 24;
-        const uint64_t att_per_wave = ipa <= wave_cap ? wave_cap / ipa : 0;
-        // specular continuations only when some entity reflects specularly
-        bool specular = false;
-        for (const EntityDev& E : s->host_entities) specular |= E.rho_s > 0.f;
-        const uint32_t nb = specular ? desc->num_bounces : 0u;
-        const uint64_t wave_items = att_per_wave ? std::min<uint64_t>(att_per_wave * ipa, total) : wave_cap;
+        const uint64_t wave_cap = 1u << 24;
+        const uint64_t wave_items = srp_wave_items(P, wave_cap, 0);
         SrpAtt* d_att = (SrpAtt*)ctx_scratch(ctx, SCR_IN1, sizeof(SrpAtt) * n_att);
-        CRT_CUDA(cudaMemcpyAsync(d_att, att.data(), sizeof(SrpAtt) * n_att, cudaMemcpyHostToDevice, st));
-        double* d_partial = (double*)ctx_scratch(ctx, SCR_WAVE3, sizeof(double) * 6 * blocks_per_att * n_att);
-        char* state = (char*)ctx_scratch(ctx, SCR_WAVE4, wave_items * (nb ? 16 + 16 + 16 + 1 : 16) + 1024);
-        uint32_t* bq = nb ? (uint32_t*)ctx_scratch(ctx, SCR_WAVE5, wave_items * 4 + 256) : nullptr;
+        CRT_CUDA(cudaMemcpyAsync(d_att, P.att.data(), sizeof(SrpAtt) * n_att, cudaMemcpyHostToDevice, st));
+        double* d_partial = (double*)ctx_scratch(ctx, SCR_WAVE3, sizeof(double) * 6 * P.blocks_per_att * n_att);
+        char* state = (char*)ctx_scratch(ctx, SCR_WAVE4, wave_items * P.state_bytes_per_item() + 1024);
+        uint32_t* bq = P.nb ? (uint32_t*)ctx_scratch(ctx, SCR_WAVE5, wave_items * 4 + 256) : nullptr;
         uint32_t* bcount = (uint32_t*)ctx_scratch(ctx, SCR_WAVE6, 256);
         double* d_force = (double*)out_device(ctx, force, n_att * 24, SCR_OUT0);
         double* d_torque = (double*)out_device(ctx, torque, n_att * 24, SCR_OUT1);
         double* d_facet = facet_power ? (double*)out_device(ctx, facet_power, n_att * s->n_tris * 8, SCR_OUT2) : nullptr;
         if (d_facet) CRT_CUDA(cudaMemsetAsync(d_facet, 0, n_att * s->n_tris * 8, st));
         const SceneView sv = scene_view(s);
-        SrpWave W;
-        W.att = d_att;
-        W.G = G;
-        W.tiles_x = tiles_x;
-        W.tiles = tiles;
-        W.items_per_att = (uint32_t)ipa;
-        W.hit = (float4*)state;
-        W.st_o = nb ? (float4*)(state + wave_items * 16) : nullptr;
-        W.st_d = nb ? (float4*)(state + wave_items * 32) : nullptr;
-        W.alive = nb ? (uint8_t*)(state + wave_items * 48) : nullptr;
-        SrpShadeArgs A;
-        A.nb = nb;
-        A.inv_c = (float)(1.0 / desc->c);
-        for (int k = 0; k < 3; ++k) A.cm[k] = (float)desc->center_of_mass[k];
-        A.partial = d_partial;
-        A.facet = d_facet;
-        A.n_tris = (uint32_t)s->n_tris;
-        A.q_out = bq;
-        for (uint64_t i0 = 0; i0 < total;) {
-            // whole attitudes, or the rest of the current attitude
-            const uint64_t r0 = i0 % ipa;
-            const uint32_t n = (uint32_t)(att_per_wave ? std::min<uint64_t>(wave_items, total - i0)
-                                                       : std::min<uint64_t>(wave_cap, ipa - r0));
-            W.i0 = i0;
-            W.a0 = (uint32_t)(i0 / ipa);
-            W.r0 = (uint32_t)r0;
-            W.multi = att_per_wave ? 1u : 0u;
+        for (uint64_t i0 = 0; i0 < P.total;) {
+            const uint32_t n = (uint32_t)srp_wave_items(P, wave_cap, i0);
+            const SrpWave W = srp_wave(P, d_att, state, wave_items, i0, n);
             i0 += n;
-            A.n_items = n;
-            const uint32_t nblk = (n + SRP_BLOCK_ITEMS - 1) / SRP_BLOCK_ITEMS;
-            for (uint32_t seg = 0; seg <= nb; ++seg) {
-                A.seg = seg;
-                A.q_count = bcount + (seg & 1);          // filled by this segment's shade
-                if (seg < nb) CRT_CUDA(cudaMemsetAsync(A.q_count, 0, sizeof(uint32_t), st));
-                if (seg == 0) {
-                    SrpPrimaryJob J;
-                    J.W = W;
-                    // single 32-ray grabs keep the warps on a narrow band of the grid, so BVH nodes
-                    // are reused from L1/L2 (measured: larger grabs were slower on the 2M asteroid)
-                    launch_trace<false>(ctx, sv, J, n);
-                    k_srp_shade<true><<<nblk, SRP_SHADE_THREADS, 0, st>>>(sv, W, A);
-                } else {
-                    // the queue filled by the previous segment's shade; its count stays on the device
-                    SrpBounceJob J;
-                    J.W = W;
-                    J.q = bq;
-                    launch_trace<false>(ctx, sv, J, n, bcount + ((seg - 1) & 1));
-                    k_srp_shade<false><<<nblk, SRP_SHADE_THREADS, 0, st>>>(sv, W, A);
-                }
-                check_launch(ctx, "k_srp_shade");
-            }
+            // single 32-ray grabs keep the warps on a narrow band of the grid, so BVH nodes are reused
+            // from L1/L2 (measured: larger grabs were slower on the 2M asteroid)
+            SrpPrimaryJob J;
+            J.W = W;
+            launch_trace<false>(ctx, sv, J, n);
+            srp_wave_stages(ctx, sv, W, n, P, d_partial, d_facet, (uint32_t)s->n_tris, bq, bcount);
         }
-        k_srp_reduce<<<(uint32_t)n_att, 256, 0, st>>>(d_partial, (uint32_t)blocks_per_att, d_force, d_torque);
-        check_launch(ctx, "k_srp_reduce");
+        srp_reduce(ctx, d_partial, P, d_force, d_torque);
         out_finish(ctx, force, d_force, n_att * 24);
         out_finish(ctx, torque, d_torque, n_att * 24);
         if (facet_power) out_finish(ctx, facet_power, d_facet, n_att * s->n_tris * 8);

@@ -1,0 +1,102 @@
+// Solar radiation pressure: the sun-ray grid items shared by crt_srp (srp.cu) and the batched
+// wavefront (render.cu, SRP requests riding in a wave's primary trace), and the host stages both run.
+//
+// Items are (attitude, 8 x 4 tile, lane) with each attitude's items padded to SRP_BLOCK_ITEMS.  A
+// wave is a range of one request's items aligned to SRP_BLOCK_ITEMS: whole attitudes, or a part of
+// one attitude.  Force and torque are summed per block of SRP_BLOCK_ITEMS items into a partial slot
+// indexed by the block's place in the request (not in the wave), in a fixed order, so the totals do
+// not depend on how the items are cut into waves.
+#pragma once
+
+#include "common.cuh"
+#include "trace.cuh"
+
+#include <vector>
+
+constexpr uint32_t SRP_BLOCK_ITEMS = 1024;
+
+struct SrpAtt {
+    float org[3];   // centre of cell (0, 0)
+    float du[3];    // step to the next cell in x
+    float dv[3];    // step to the next cell in y
+    float dir[3];   // -s_b
+    float E0;       // flux * cell area
+    float pad;
+};
+
+struct SrpWave {
+    const SrpAtt* att;
+    uint32_t G, tiles_x, tiles;
+    uint32_t items_per_att;   // multiple of SRP_BLOCK_ITEMS
+    uint64_t i0;              // first item of the wave
+    uint32_t a0, r0;          // i0 = a0 * items_per_att + r0
+    uint32_t multi;           // the wave holds whole attitudes (r0 == 0) rather than part of one
+    float4* hit;              // per wave item: t, u, v, slot
+    float4* st_o;             // continuing ray: origin, power
+    float4* st_d;             // continuing ray: direction, triangle it leaves
+    uint8_t* alive;           // continuing ray present
+};
+
+// attitude of wave item i (32-bit arithmetic: a wave is whole attitudes or a part of one)
+__device__ __forceinline__ uint32_t srp_att(const SrpWave& W, uint32_t i, uint32_t& local) {
+    if (W.multi) {
+        const uint32_t q = i / W.items_per_att;
+        local = i - q * W.items_per_att;
+        return W.a0 + q;
+    }
+    local = W.r0 + i;
+    return W.a0;
+}
+
+__device__ __forceinline__ bool srp_item(const SrpWave& W, uint32_t i, uint32_t& a, uint32_t& px, uint32_t& py) {
+    uint32_t local;
+    a = srp_att(W, i, local);
+    const uint32_t tile = local >> 5, lane = local & 31u;
+    if (tile >= W.tiles) return false;
+    px = (tile % W.tiles_x) * 8u + (lane & 7u);
+    py = (tile / W.tiles_x) * 4u + (lane >> 3);
+    return px < W.G && py < W.G;
+}
+
+// sun ray of wave item i (false: padding item)
+__device__ __forceinline__ bool srp_primary_ray(const SrpWave& W, uint32_t i, TRay& r) {
+    uint32_t a, px, py;
+    if (!srp_item(W, i, a, px, py)) return false;
+    const SrpAtt& P = W.att[a];
+    r.o = f3(P.org[0] + px * P.du[0] + py * P.dv[0], P.org[1] + px * P.du[1] + py * P.dv[1],
+             P.org[2] + px * P.du[2] + py * P.dv[2]);
+    r.d = f3(P.dir[0], P.dir[1], P.dir[2]);
+    r.tmin = 0.f;
+    r.tmax = 3.402823466e38f;
+    return true;
+}
+
+// One request's attitude table and item geometry (host side)
+struct SrpPlan {
+    std::vector<SrpAtt> att;
+    uint32_t G = 0, tiles_x = 0, tiles = 0;
+    uint32_t nb = 0;                  // specular segments actually traced (0 when no entity reflects)
+    uint64_t ipa = 0;                 // items per attitude (multiple of SRP_BLOCK_ITEMS)
+    uint64_t total = 0;               // ipa * attitudes
+    uint64_t blocks_per_att = 0;
+    float inv_c = 0.f, cm[3] = {0.f, 0.f, 0.f};
+    size_t n_att() const { return att.size(); }
+    // bytes of per-item wave state (hits, and continuation state when there are specular segments)
+    size_t state_bytes_per_item() const { return nb ? 16 + 16 + 16 + 1 : 16; }
+};
+
+// Validates an SRP request and builds its plan; quaternions may be host or device memory.  Throws
+// CrtError.
+void srp_plan(crt_scene* s, const crt_srp_desc* desc, const double* quats, size_t n_att, SrpPlan& P);
+// Wave descriptor over `state` (room for `cap` items) for items [i0, i0 + n) of the request
+// (d_att: its attitude table on the device)
+SrpWave srp_wave(const SrpPlan& P, const SrpAtt* d_att, char* state, uint64_t cap, uint64_t i0, uint64_t n);
+// Largest wave at most `cap` items long that starts at item i0: whole attitudes when one fits,
+// else the rest of the current attitude
+uint64_t srp_wave_items(const SrpPlan& P, uint64_t cap, uint64_t i0);
+// After the primary segment's hits are in W.hit: its shade, then the specular segments (trace of
+// the compacted continuation queue + shade).  bq: room for n entries; bcount: 2 counters.
+void srp_wave_stages(crt_context* ctx, const SceneView& sv, const SrpWave& W, uint32_t n, const SrpPlan& P,
+                     double* partial, double* facet, uint32_t n_tris, uint32_t* bq, uint32_t* bcount);
+// Per-attitude force and torque from the request's partial sums (device outputs)
+void srp_reduce(crt_context* ctx, const double* partial, const SrpPlan& P, double* force, double* torque);

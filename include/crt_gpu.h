@@ -298,6 +298,17 @@ typedef struct {
     double* force;                        /* n_att * 3 */
     double* torque;                       /* n_att * 3 */
 } crt_server_request;
+/* Mixed batch (no counterpart in the reference, which renders one camera per call and names SRP only
+ * in its README): render, LiDAR and SRP requests in one call, given as crt_server_request (kind SRP:
+ * srp / quaternions / n_att / force / torque; quaternions and outputs host or device memory).  The
+ * SRP requests' sun rays ride in the waves' primary trace launches beside the camera paths and LiDAR
+ * beams (one shared ray queue), each wave carrying a range of one SRP request's items, and that
+ * range's shade and specular segments follow in the same wave.  Render and LiDAR results equal
+ * crt_batch's; force and torque equal crt_srp's bit for bit (partial sums are kept per block of the
+ * request's items, whatever the waves).  Waves that carry SRP items are launched one by one (no
+ * CUDA-graph replay). */
+int crt_batch_mixed(crt_context* ctx, const crt_server_request* requests, size_t n, crt_batch_stats* stats);
+
 typedef struct {
     int status;                           /* CRT_OK or the failure of the wave that ran it */
     double submit_s, start_s, end_s;      /* steady-clock seconds: submitted, admitted, completed */

@@ -56,6 +56,9 @@ def make_requests(d, cornell, ast):
 
 def standalone(q):
     sc = q["scene"]
+    if q["kind"] == "srp":
+        f, t, _ = sc.srp(q["sun_dir"], q["quaternions"], q["grid"], num_bounces=q["num_bounces"])
+        return f, t
     if q["kind"] == "render":
         return sc.render(q["camera"], q["lights"], q["min_samples"], q["max_samples"], q["noise_threshold"],
                          q["num_bounces"], seed=q["seed"], request=q["request"])
@@ -121,3 +124,55 @@ def test_bad_request_rejected(setup):
              half_y=0.1)
     with pytest.raises(lib.CrtError):
         ctx.batch([q])
+
+
+def srp_requests(ctx, ast):
+    craft = ctx.scene(scenes.spacecraft(bus_cell=0.25, panel_cell=0.2, dish_rings=16, dish_segments=16))
+    return [
+        # 256^2: one attitude per 65,536-item wave at the smallest wave size; specular panels
+        dict(kind="srp", scene=craft, sun_dir=[1.0, 0.2, -0.1], quaternions=scenes.random_quaternions(3, seed=2),
+             grid=256, num_bounces=2),
+        # 600^2: one attitude spans several waves (parts of an attitude)
+        dict(kind="srp", scene=craft, sun_dir=[0.0, 1.0, 0.0], quaternions=scenes.random_quaternions(1, seed=3),
+             grid=600, num_bounces=1),
+        # no specular entity: primary segment only, several attitudes per wave
+        dict(kind="srp", scene=ast, sun_dir=[0.3, -0.5, 0.8], quaternions=scenes.random_quaternions(5, seed=4),
+             grid=128, num_bounces=2),
+    ]
+
+
+@pytest.mark.parametrize("wave_paths", [1 << 23, 1 << 16])
+def test_mixed_batch_with_srp_equals_standalone(setup, wave_paths):
+    """crt_batch_mixed: SRP requests ride in the waves' primary traces beside camera paths and LiDAR
+    beams.  Renders and LiDAR scans equal their standalone calls bit for bit, and force and torque
+    equal crt_srp's bit for bit however the sun-ray grids are cut into waves (partial sums are kept
+    per block of the request's items)."""
+    ctx, d, cornell, ast = setup
+    reqs = make_requests(d, cornell, ast)[:8]
+    srps = srp_requests(ctx, ast)
+    mixed = reqs[:3] + [srps[0]] + reqs[3:6] + srps[1:] + reqs[6:]
+    ctx.set_tuning(queue_chunk=1, wave_paths=1 << 23, use_graphs=True)
+    alone = [standalone(q) for q in mixed]
+    ctx.set_tuning(queue_chunk=1, wave_paths=wave_paths, use_graphs=True)
+    outs, st = ctx.batch(mixed)
+    ctx.set_tuning()
+    for q, a, b in zip(mixed, alone, outs):
+        assert_same(a, b)
+    f, t = outs[3]
+    assert np.isfinite(f).all() and (np.abs(f).sum(1) > 0).all()
+    if wave_paths == 1 << 16:
+        assert st["waves"] >= 6 + 3
+
+
+def test_srp_only_batch_and_device_outputs(setup):
+    """A batch of SRP requests alone, with force / torque in device memory, equals crt_srp."""
+    torch = pytest.importorskip("torch")
+    ctx, d, cornell, ast = setup
+    q = srp_requests(ctx, ast)[0]
+    f_dev = torch.zeros((3, 3), dtype=torch.float64, device="cuda")
+    t_dev = torch.zeros((3, 3), dtype=torch.float64, device="cuda")
+    ctx.batch([q], outputs=[(f_dev, t_dev)])
+    torch.cuda.synchronize()
+    f, t = standalone(q)
+    np.testing.assert_array_equal(f_dev.cpu().numpy(), f)
+    np.testing.assert_array_equal(t_dev.cpu().numpy(), t)
