@@ -548,8 +548,10 @@ def batched_measure(ctx, ents, stream, reps=1):
     lat = [a.elapsed_time(b) for a, b in ev]
     # per-call latency of a request submitted with the whole set: its completion time in the sequence
     done = np.cumsum(lat)
+    mixed = mixed_measure(ctx, breqs, outs, stream)
     sc.close()
-    return {"workload": "64 requests on the 2M asteroid: 32 renders (128^2..2048^2, 1..64 spp, 2 bounces, "
+    return {"mixed": mixed,
+            "workload": "64 requests on the 2M asteroid: 32 renders (128^2..2048^2, 1..64 spp, 2 bounces, "
                         "sun light) + 32 LiDAR scans (64^2..1024^2); scene built with collapse_tri_cost 0.5",
             "rays": int(rays), "per_call_mrays_s": round(rays / (pc_ms / 1e3) / 1e6, 1),
             "batched_mrays_s": round(rays / (bt_ms / 1e3) / 1e6, 1), "speedup": round(pc_ms / bt_ms, 3),
@@ -561,6 +563,68 @@ def batched_measure(ctx, ents, stream, reps=1):
             "batched_completion_ms": round(bt_ms, 2),
             "tuning": knobs, "tuning_trials_ms": [[t[0]["queue_chunk"], t[0]["wave_paths"], round(t[1], 2)]
                                                   for t in rep["trials"]]}
+
+
+def mixed_measure(ctx, breqs, outs, stream):
+    """The 64 requests above plus 16 SRP queries on the spacecraft (grid 512^2..2048^2, 1..4 attitudes,
+    2 specular bounces) as per-call GPU requests (crt_render / crt_lidar_grid / crt_srp, in sequence)
+    and as one crt_batch_mixed, whose waves carry the SRP sun rays in their primary traces; device
+    outputs in both cases."""
+    import torch
+    from crt_gb300 import scenes
+    craft = ctx.scene(scenes.spacecraft())
+    rng = np.random.Generator(np.random.PCG64(11))
+    dev = torch.device("cuda", torch.cuda.current_device())
+    sreqs, souts = [], []
+    for k in range(16):
+        q = scenes.random_quaternions(int(rng.integers(1, 5)), seed=500 + k)
+        sreqs.append(dict(kind="srp", scene=craft, sun_dir=[1.0, 0.0, 0.0], quaternions=q,
+                          grid=int(rng.choice([512, 1024, 2048])), num_bounces=2))
+        souts.append((torch.empty((len(q), 3), dtype=torch.float64, device=dev),
+                      torch.empty((len(q), 3), dtype=torch.float64, device=dev)))
+    mreqs, mouts = list(breqs), list(outs)
+    for k, (q, o) in enumerate(zip(sreqs, souts)):   # spread the SRP queries through the request list
+        at = (k * len(mreqs)) // len(sreqs) + k
+        mreqs.insert(at, q)
+        mouts.insert(at, o)
+    sc = next(q["scene"] for q in breqs)
+
+    def per_call():
+        for q, o in zip(mreqs, mouts):
+            if q["kind"] == "render":
+                sc.render(q["camera"], q["lights"], q["min_samples"], q["max_samples"], 0.0, q["num_bounces"],
+                          seed=q["seed"], request=q["request"], want_radiance=False, out_rgba=o[0])
+            elif q["kind"] == "lidar":
+                sc.lidar_grid(q["position"], q["rotation"], q["nx"], q["ny"], q["half_x"], q["half_y"],
+                              out_range=o[0], out_prim=o[1])
+            else:
+                craft.srp_into(q["sun_dir"], q["quaternions"], q["grid"], o[0], o[1], num_bounces=q["num_bounces"])
+
+    with torch.cuda.stream(stream):
+        ctx.reset_counters()
+        ctx.set_counting(True)
+        _, st = ctx.batch(mreqs, outputs=mouts)
+        rays = ctx.counters()["rays"]
+        ctx.set_counting(False)
+        ctx.batch(mreqs, outputs=mouts)      # warm-up
+        per_call()
+        torch.cuda.synchronize()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        ev[0].record(stream)
+        per_call()
+        ev[1].record(stream)
+        ev[2].record(stream)
+        _, st = ctx.batch(mreqs, outputs=mouts)
+        ev[3].record(stream)
+    torch.cuda.synchronize()
+    pc_ms, bt_ms = ev[0].elapsed_time(ev[1]), ev[2].elapsed_time(ev[3])
+    craft.close()
+    return {"workload": "the 64 requests + 16 SRP queries on the spacecraft (48,728 triangles; grid 512^2..2048^2, "
+                        "1..4 attitudes, 2 bounces; 46 attitudes), one crt_batch_mixed vs per-call",
+            "rays": int(rays), "per_call_ms": round(pc_ms, 2), "batched_ms": round(bt_ms, 2),
+            "per_call_mrays_s": round(rays / (pc_ms / 1e3) / 1e6, 1),
+            "batched_mrays_s": round(rays / (bt_ms / 1e3) / 1e6, 1), "speedup": round(pc_ms / bt_ms, 3),
+            "waves": st["waves"]}
 
 
 def served_measure(args, device):
