@@ -190,6 +190,8 @@ struct WaveEngine;
 WaveEngine* engine_create(crt_context* ctx, size_t budget_bytes);
 void engine_destroy(WaveEngine* e);
 bool engine_admit(WaveEngine* e, const crt_request& q, uint64_t tag);
+bool engine_admit_srp(WaveEngine* e, crt_scene* scene, const crt_srp_desc& desc, const double* quats, size_t n_att,
+                      double* force, double* torque, uint64_t tag);
 void engine_step(WaveEngine* e, std::vector<uint64_t>& completed);
 void engine_abort(WaveEngine* e, std::vector<uint64_t>& dropped);
 // srp.cu: radiation pressure on an explicit context

@@ -33,6 +33,7 @@
 
 #include <algorithm>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <cmath>
 #include <cstring>
@@ -1331,7 +1332,18 @@ struct EReq {
     double* range = nullptr;
     uint32_t* prim = nullptr;
     double* tan = nullptr;
+    // SRP query: its sun-ray items ride in the waves' primary traces, one range per wave
+    bool srp = false;
+    std::shared_ptr<SrpPlan> splan;
+    uint64_t srp_next = 0;                // next item to put in a wave
+    SrpAtt* d_att = nullptr;
+    double* partial = nullptr;
+    double* force = nullptr;              // device: the caller's memory or arena staging
+    double* torque = nullptr;
+    double* out_force = nullptr;          // the caller's buffers
+    double* out_torque = nullptr;
     uint64_t remaining() const {
+        if (srp) return splan ? splan->total - srp_next : 0;
         if (lidar) return 0;
         return (uint64_t)(total - next_sample) * (adaptive && next_sample >= upto ? n_active : npix);
     }
@@ -1389,6 +1401,11 @@ struct WaveEngine {
     uint32_t* d_counts = nullptr;
     uint32_t* d_acount = nullptr;
     uint32_t* d_tqueue = nullptr;
+    // SRP items of one wave (allocated at the first SRP admission): state, continuation queue, counters
+    uint64_t srp_cap = 0;
+    char* srp_state = nullptr;
+    uint32_t* srp_bq = nullptr;
+    uint32_t* srp_bcount = nullptr;
 
     float4* pix() const { return (float4*)units_mem; }
     uint32_t* taken() const { return (uint32_t*)(units_mem + up256(units.cap() * 16)); }
@@ -1516,7 +1533,7 @@ void engine_stage_out(WaveEngine* e, WaveEngine::Flight& f, void* dst, const voi
 void engine_release(WaveEngine* e, EReq& r) {
     if (r.units) e->units.release(r.unit_off, r.units);
     if (r.bytes) e->bytes.release(r.byte_off, r.bytes);
-    if (!r.lidar) e->free_slots.push_back(r.slot);
+    if (!r.lidar && !r.srp) e->free_slots.push_back(r.slot);
     r.units = r.bytes = 0;
 }
 
@@ -1573,6 +1590,7 @@ void engine_destroy(WaveEngine* e) {
     cudaFree(e->units_mem);
     cudaFree(e->bytes_mem);
     cudaFree(e->fixed);
+    cudaFree(e->srp_state);
     for (char* p : e->pinned)
         if (p) cudaFreeHost(p);
     if (e->hout) cudaFreeHost(e->hout);
@@ -1694,6 +1712,61 @@ bool engine_admit(WaveEngine* e, const crt_request& q, uint64_t tag) {
     return true;
 }
 
+// Admits an SRP query when its attitude table, partial sums and output staging fit the byte arena; its
+// sun-ray items then ride in the waves' primary traces, one range of at most srp_cap items per wave
+// (earliest admitted query first).  The SRP wave state (srp_cap items, 53 bytes each) is allocated at
+// the engine's first SRP admission.
+bool engine_admit_srp(WaveEngine* e, crt_scene* scene, const crt_srp_desc& desc, const double* quats, size_t n_att,
+                      double* force, double* torque, uint64_t tag) {
+    CRT_CHECK(scene && scene->ctx && scene->ctx->device == e->ctx->device, CRT_ERR_INVALID,
+              "request scene lives on another device");
+    CRT_CHECK(n_att == 0 || (quats && force && torque), CRT_ERR_INVALID, "incomplete SRP request");
+    cudaStream_t st = e->ctx->stream;
+    auto plan = std::make_shared<SrpPlan>();
+    srp_plan(scene, &desc, quats, n_att, *plan);
+    if (!e->srp_state) {
+        const uint64_t cap = std::max<uint64_t>((uint64_t)e->want_P / SRP_BLOCK_ITEMS * SRP_BLOCK_ITEMS, SRP_BLOCK_ITEMS);
+        const size_t b_state = up256(cap * (16 + 16 + 16 + 1)), b_q = up256(cap * 4);
+        CRT_CUDA(cudaMalloc(&e->srp_state, b_state + b_q + 256));
+        e->srp_cap = cap;
+        e->srp_bq = (uint32_t*)(e->srp_state + b_state);
+        e->srp_bcount = (uint32_t*)(e->srp_state + b_state + b_q);
+    }
+    EReq r;
+    std::memset(&r.q, 0, sizeof(r.q));
+    r.q.kind = CRT_REQUEST_SRP;
+    r.q.scene = scene;
+    r.tag = tag;
+    r.srp = true;
+    r.splan = plan;
+    const size_t na = std::max<size_t>(n_att, 1);
+    const bool host_f = !is_device_ptr(force), host_t = !is_device_ptr(torque);
+    const size_t b_att = up256(sizeof(SrpAtt) * na);
+    const size_t b_part = up256(sizeof(double) * 6 * std::max<uint64_t>(plan->blocks_per_att, 1) * na);
+    const size_t b_f = host_f ? up256(24 * na) : 0, b_t = host_t ? up256(24 * na) : 0;
+    r.bytes = b_att + b_part + b_f + b_t;
+    if (r.bytes > e->bytes.cap() && e->res.empty()) {
+        CRT_CUDA(cudaStreamSynchronize(st));   // a completed wave's copies may still be in flight
+        engine_alloc_bytes(e, r.bytes + r.bytes / 4);
+    }
+    if (!e->bytes.alloc(r.bytes, r.byte_off)) return false;
+    char* b = e->bytes_mem + r.byte_off;
+    r.d_att = (SrpAtt*)b;
+    b += b_att;
+    r.partial = (double*)b;
+    b += b_part;
+    r.force = host_f ? (double*)b : force;
+    b += b_f;
+    r.torque = host_t ? (double*)b : torque;
+    r.out_force = force;
+    r.out_torque = torque;
+    if (n_att) engine_upload(e, r.d_att, plan->att.data(), sizeof(SrpAtt) * n_att);
+    r.finished = plan->total == 0;
+    r.seq = e->seq++;
+    e->res.push_back(r);
+    return true;
+}
+
 // Drops every resident request and the waves in flight (after a failed step); returns their tags.
 void engine_abort(WaveEngine* e, std::vector<uint64_t>& dropped) {
     cudaStreamSynchronize(e->ctx->stream);
@@ -1780,13 +1853,14 @@ void engine_step(WaveEngine* e, std::vector<uint64_t>& completed) {
     B.taken = e->taken();
     B.done = e->done();
     for (EReq& r : e->res)
-        if (!r.lidar && r.next_sample >= r.total && (!r.adaptive || r.next_sample >= r.upto)) r.finished = true;
+        if (!r.lidar && !r.srp && r.next_sample >= r.total && (!r.adaptive || r.next_sample >= r.upto))
+            r.finished = true;
 
     // adaptive requests past their fixed prefix: compact the still-active pixels (reads counts back,
     // so the wave in flight is completed first)
     std::vector<EReq*> compacting;
     for (EReq& r : e->res)
-        if (!r.lidar && r.adaptive && r.next_sample >= r.upto && r.next_sample < r.total && r.n_active > 0)
+        if (!r.lidar && !r.srp && r.adaptive && r.next_sample >= r.upto && r.next_sample < r.total && r.n_active > 0)
             compacting.push_back(&r);
     if (!compacting.empty()) {
         engine_drain_all(e, completed);
@@ -1841,7 +1915,7 @@ void engine_step(WaveEngine* e, std::vector<uint64_t>& completed) {
     w.n_lreq = (uint32_t)lreqs.size();
     std::vector<EReq*> order;
     for (EReq& r : e->res)
-        if (!r.lidar && !r.finished && r.next_sample < r.total) order.push_back(&r);
+        if (!r.lidar && !r.srp && !r.finished && r.next_sample < r.total) order.push_back(&r);
     // least remaining work first; a request passed over for 4 waves goes first (no starvation)
     std::stable_sort(order.begin(), order.end(), [](const EReq* a, const EReq* b) {
         const bool sa = a->skipped >= 4, sb = b->skipped >= 4;
@@ -1888,7 +1962,20 @@ void engine_step(WaveEngine* e, std::vector<uint64_t>& completed) {
         max_bounces = std::max(max_bounces, r.num_bounces);
         if (r.next_sample >= r.total) r.finished = true;
     }
-    w.n_primary = w.n_lidar_items + w.n_paths;
+    // one SRP range per wave, from the earliest admitted query with items left
+    EReq* sq = nullptr;
+    for (EReq& r : e->res)
+        if (r.srp && !r.finished && r.srp_next < r.splan->total && (!sq || r.seq < sq->seq)) sq = &r;
+    uint64_t srp_n = 0;
+    if (sq) {
+        const SrpPlan& SP = *sq->splan;
+        srp_n = srp_wave_items(SP, e->srp_cap, sq->srp_next);
+        w.n_srp_items = (uint32_t)srp_n;
+        w.srp_sv = scene_view(sq->q.scene);
+        w.srp = srp_wave(SP, sq->d_att, e->srp_state, e->srp_cap, sq->srp_next, srp_n);
+        sq->srp_next += srp_n;
+    }
+    w.n_primary = w.n_lidar_items + w.n_paths + w.n_srp_items;
 
     // run it
     // launch
@@ -1900,7 +1987,24 @@ void engine_step(WaveEngine* e, std::vector<uint64_t>& completed) {
     engine_flush_uploads(e);
     if (any_work) {
         CRT_CUDA(cudaMemsetAsync(e->d_wave_idx, 0, 4, st));
-        launch_wave_kernels(ctx, B, P, NL, lidar_items, max_bounces, qa, qb, e->d_tqueue);
+        std::function<void()> stages;
+        if (sq) {
+            const SrpWave W = w.srp;
+            stages = [&, W]() {
+                srp_wave_stages(ctx, scene_view(sq->q.scene), W, (uint32_t)srp_n, *sq->splan, sq->partial, nullptr,
+                                (uint32_t)sq->q.scene->n_tris, e->srp_bq, e->srp_bcount);
+            };
+        }
+        launch_wave_kernels(ctx, B, P, NL, lidar_items, max_bounces, qa, qb, e->d_tqueue,
+                            sq ? (uint32_t)e->srp_cap : 0u, sq ? &stages : nullptr);
+    }
+    // an SRP query whose last range ran in this wave: per-attitude totals, outputs staged
+    if (sq && sq->srp_next >= sq->splan->total) {
+        const size_t na = sq->splan->n_att();
+        srp_reduce(ctx, sq->partial, *sq->splan, sq->force, sq->torque);
+        if (sq->force != sq->out_force) engine_stage_out(e, f, sq->out_force, sq->force, na * 24);
+        if (sq->torque != sq->out_torque) engine_stage_out(e, f, sq->out_torque, sq->torque, na * 24);
+        sq->finished = true;
     }
     // completions of this wave: finalize, stage host outputs, release device state (later work on
     // the stream reuses it only after these copies)
@@ -1912,7 +2016,7 @@ void engine_step(WaveEngine* e, std::vector<uint64_t>& completed) {
         r->finished = true;
     }
     for (EReq& r : e->res) {
-        if (r.lidar || !r.finished) continue;
+        if (r.lidar || r.srp || !r.finished) continue;
         k_finalize_one<<<grid_for(ctx, k_finalize_one, r.npix), 256, 0, st>>>(B, r.slot);
         check_launch(ctx, "k_finalize_one");
         if (r.q.rgba8 && (void*)r.rgba != (void*)r.q.rgba8)

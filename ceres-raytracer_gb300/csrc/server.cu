@@ -75,8 +75,9 @@ void publish(crt_server* S, Pending* p, int status, double start_s, double end_s
     delete p;
 }
 
-// One lane: admits queued requests into its wave engine whenever their state fits (FIFO), runs SRP
-// queries between waves, and runs one wave per iteration.  Requests leave when their last wave is done.
+// One lane: admits queued requests (renders, LiDAR scans, SRP queries) into its wave engine whenever
+// their state fits (FIFO), and runs one wave per iteration; an SRP query's sun rays ride in the waves'
+// primary traces, one range per wave.  Requests leave when their last wave is done.
 void lane_loop(crt_server* S, size_t lane) {
     crt_context* ctx = S->lanes[lane];
     WaveEngine* E = S->engines[lane];
@@ -84,7 +85,6 @@ void lane_loop(crt_server* S, size_t lane) {
     std::unordered_map<uint64_t, std::pair<Pending*, double>> resident;   // tag -> (request, admitted at)
     std::vector<uint64_t> finished;
     while (true) {
-        std::vector<Pending*> srp;
         {
             std::unique_lock<std::mutex> lk(S->mu);
             S->cv_work.wait(lk, [&] { return S->stop || !S->queue.empty() || !resident.empty(); });
@@ -92,14 +92,13 @@ void lane_loop(crt_server* S, size_t lane) {
             const double now = now_s();
             while (!S->queue.empty() && resident.size() < S->cfg.max_batch) {
                 Pending* p = S->queue.front();
-                if (p->srp) {
-                    srp.push_back(p);
-                    S->queue.pop_front();
-                    continue;
-                }
                 bool ok = false;
-                const int rc = crt_guard(ctx, [&] { ok = engine_admit(E, p->req, p->ticket); });
-                if (rc != CRT_OK) {   // validated at submission, so only a CUDA failure gets here
+                const int rc = crt_guard(ctx, [&] {
+                    ok = p->srp ? engine_admit_srp(E, p->req.scene, p->srp_desc, p->quats.data(), p->quats.size() / 4,
+                                                   p->force, p->torque, p->ticket)
+                                : engine_admit(E, p->req, p->ticket);
+                });
+                if (rc != CRT_OK) {   // a CUDA failure, or an attitude quaternion of zero length
                     S->queue.pop_front();
                     publish(S, p, rc, now, now_s(), 0);
                     continue;
@@ -112,29 +111,7 @@ void lane_loop(crt_server* S, size_t lane) {
         S->cv_done.notify_all();
         crt_counters c0{}, c1{};
         if (S->cfg.count_rays) crt_context_get_counters(ctx, &c0);
-        for (Pending* p : srp) {
-            const double t0 = now_s();
-            int rc = crt_guard(ctx, [&] {
-                srp_run(ctx, p->req.scene, &p->srp_desc, p->quats.data(), p->quats.size() / 4, p->force, p->torque,
-                        nullptr);
-            });
-            const int sync = crt_context_synchronize(ctx);
-            if (rc == CRT_OK) rc = sync;
-            const double t1 = now_s();
-            std::lock_guard<std::mutex> lk(S->mu);
-            publish(S, p, rc, t0, t1, 1);
-            S->stats.batches++;
-            S->stats.busy_s += t1 - t0;
-        }
-        if (!srp.empty()) S->cv_done.notify_all();
-        if (resident.empty()) {
-            if (S->cfg.count_rays && !srp.empty()) {
-                crt_context_get_counters(ctx, &c1);
-                std::lock_guard<std::mutex> lk(S->mu);
-                S->stats.rays += c1.rays - c0.rays;
-            }
-            continue;
-        }
+        if (resident.empty()) continue;
         const double t0 = now_s();
         const size_t sharing = resident.size();
         finished.clear();

@@ -279,7 +279,8 @@ int crt_host_free(void* ptr);
  * call), with continuous batching: requests are submitted from any thread and queued; each of
  * `lanes` lanes (own stream, own wave engine) admits them in arrival order while their device state
  * fits its budget, and runs one wavefront wave at a time over all of its resident requests,
- * shortest remaining work first.  A request that arrives while others are on the GPU joins the next
+ * shortest remaining work first; an SRP query's sun rays ride in the waves' primary traces, one range
+ * of its items per wave (as in crt_batch_mixed).  A request that arrives while others are on the GPU joins the next
  * wave and leaves when its own last wave is done.  Results equal the same requests run alone. */
 typedef struct crt_server crt_server;
 enum { CRT_REQUEST_SRP = 2 };
@@ -315,7 +316,7 @@ typedef struct {
     uint32_t batch_size;                  /* requests resident in the lane during its last wave */
 } crt_server_result;
 typedef struct {
-    uint64_t submitted, completed, batches, failed;   /* batches: waves and SRP launches run */
+    uint64_t submitted, completed, batches, failed;   /* batches: waves run */
     uint64_t rays;                        /* rays traced by completed batches (count_rays only) */
     double busy_s;                        /* summed lane time */
 } crt_server_stats;

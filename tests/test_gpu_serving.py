@@ -127,6 +127,38 @@ def test_adaptive_and_long_renders_share_waves():
         srv.close()
 
 
+def test_srp_query_spans_waves_shared_with_renders():
+    """An SRP query larger than one wave (2 attitudes of 600^2 sun rays, 65,536 items per wave) rides in
+    the waves' primary traces one range per wave, while a render and a LiDAR scan share those waves;
+    force and torque equal crt_srp's bit for bit, the render and the scan their standalone calls."""
+    srv = lib.Server(0, lanes=1, lane_budget_bytes=1 << 30, max_batch=64, count_rays=True, wave_paths=1 << 16)
+    try:
+        d = load_golden("cornell")
+        cornell = srv.scene(entities_from(d))
+        craft = srv.scene(scenes.spacecraft(bus_cell=0.25, panel_cell=0.2, dish_rings=16, dish_segments=16))
+        cam = camera_from(d, "rcam")
+        reqs = [dict(kind="srp", scene=craft, sun_dir=[0.2, 1.0, 0.1], quaternions=scenes.random_quaternions(2, seed=8),
+                     grid=600, num_bounces=2),
+                dict(kind="render", scene=cornell, camera=dict(cam, resolution=[64, 48]), lights=lights_from(d["lights"]),
+                     min_samples=8, max_samples=8, noise_threshold=0.0, num_bounces=2, seed=3, request=2, radiance=True),
+                dict(kind="lidar", scene=cornell, position=[0.5, 0.5, 2.4], rotation=np.eye(3), nx=9, ny=7, half_x=0.1,
+                     half_y=0.1),
+                dict(kind="srp", scene=craft, sun_dir=[1.0, 0.0, 0.0], quaternions=scenes.random_quaternions(3, seed=9),
+                     grid=128, num_bounces=1)]
+        expected = [alone(q) for q in reqs]
+        tickets = [srv.submit(q) for q in reqs]
+        results = [srv.wait(t, timeout=120.0) for t in tickets]
+        for (res, out), e in zip(results, expected):
+            assert res["status"] == 0
+            for a, b in zip(out, e):
+                if b is not None:
+                    np.testing.assert_array_equal(a, b)
+        assert results[1][0]["batch_size"] > 1 and results[2][0]["batch_size"] > 1
+        assert srv.stats()["batches"] >= 12   # 6 ranges per 600^2 attitude
+    finally:
+        srv.close()
+
+
 def test_admission_budget_runs_large_requests_alone():
     srv = lib.Server(0, lanes=1, lane_budget_bytes=1, max_batch=64)
     try:
