@@ -411,6 +411,37 @@ __device__ __forceinline__ uint2 block_append2(uint32_t* c0, uint32_t n0, uint32
     return r;
 }
 
+// Block-wide append of at most one entry per thread into 8 buckets (key 0..7; 8: none), for 256-thread
+// blocks: one atomicAdd per block; within the block's range the entries are ordered by bucket, then
+// by thread.  Every thread of the block calls it; returns the thread's index (undefined for key 8).
+__device__ __forceinline__ uint32_t block_append_buckets8(uint32_t* counter, uint32_t key) {
+    __shared__ uint32_t s_cnt[8][8];   // [warp][bucket]: counts, then offsets
+    __shared__ uint32_t s_base;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t rank = 0;
+#pragma unroll
+    for (uint32_t k = 0; k < 8; ++k) {
+        const uint32_t m = __ballot_sync(0xFFFFFFFFu, key == k);
+        if (lane == 0) s_cnt[warp][k] = __popc(m);
+        if (key == k) rank = __popc(m & ((1u << lane) - 1u));
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t t = 0;
+        for (int k = 0; k < 8; ++k)
+            for (int w = 0; w < 8; ++w) {
+                const uint32_t c = s_cnt[w][k];
+                s_cnt[w][k] = t;
+                t += c;
+            }
+        s_base = t ? atomicAdd(counter, t) : 0u;
+    }
+    __syncthreads();
+    const uint32_t r = key < 8u ? s_base + s_cnt[warp][key] + rank : 0u;
+    __syncthreads();   // the shared words are rewritten by the next call
+    return r;
+}
+
 __device__ __forceinline__ float maxabs3(float3 a) { return fmaxf(fabsf(a.x), fmaxf(fabsf(a.y), fabsf(a.z))); }
 
 // Flat unit normal of path p's current triangle (xyz) and the distance from its hit point to the
@@ -476,7 +507,8 @@ __device__ __noinline__ uint32_t mark_self_occluded(const Batch& B, int bounce, 
 }
 
 // One live path at bounce `bounce`: surface point, a shadow ray per light at p * L + l, and when the
-// path continues its bounce ray.  Returns the lights whose shadow ray has to be traced.
+// path continues its bounce ray.  Returns the lights whose shadow ray has to be traced (bits 0..15)
+// and the octant of the bounce ray (bits 16..18).
 __device__ __forceinline__ uint32_t shade_path(const Batch& B, int bounce, uint32_t p, uint32_t req, const THit& h,
                                                bool cont) {
     const RReq& R = B.rr[req];
@@ -488,6 +520,7 @@ __device__ __forceinline__ uint32_t shade_path(const Batch& B, int bounce, uint3
     const float3 x = sp.x - origin_offset(sp.x) * sp.flat_n;   // intersect_point - 1e-4 normal
     const uint32_t nl = R.n_lights;
     uint32_t into = 0;   // lights whose shadow ray points into the surface
+    uint32_t oct = 0;    // octant of the bounce ray
     for (uint32_t l = 0; l < nl; ++l) {
         const LightDev& lt = B.lights[R.light_base + l];
         float3 lp = f3(lt.pos[0], lt.pos[1], lt.pos[2]);
@@ -526,18 +559,20 @@ __device__ __forceinline__ uint32_t shade_path(const Batch& B, int bounce, uint3
         const float bc = 1.0f - r1;
         const float4 wt = path_weight(B, p, bounce);
         B.wgt[(bounce + 1) & 1][p] = make_float4(wt.x * bc, wt.y * bc, wt.z * bc, 0.f);
+        oct = (__float_as_uint(nd.x) >> 31) | ((__float_as_uint(nd.y) >> 31) << 1) | ((__float_as_uint(nd.z) >> 31) << 2);
     }
     // self-occluded shadow rays: at bounce 0 (incoming ray from the camera) and at the path's last
     // bounce (its ray is not replaced above); middle bounces of longer paths are traced as they are
-    const uint32_t all = nl >= 32 ? 0xFFFFFFFFu : (1u << nl) - 1u;
-    return into && (bounce == 0 || !cont) ? mark_self_occluded(B, bounce, p, R, into, all) : all;
+    const uint32_t all = (1u << nl) - 1u;   // nl <= 16
+    const uint32_t keep = into && (bounce == 0 || !cont) ? mark_self_occluded(B, bounce, p, R, into, all) : all;
+    return keep | (oct << 16);
 }
 
 // 256-thread blocks (block_append2); the loop's trip count is uniform over a block.  The shadow queue
 // receives the shadow rays still to trace after the shade, in path order within a block; rays that
 // their own triangle stops (mark_self_occluded) are not queued.
 __global__ void __launch_bounds__(256) k_shade(Batch B, int bounce, const uint32_t* __restrict__ q_in,
-                                               uint32_t* __restrict__ q_out) {
+                                               uint32_t* __restrict__ q_out, bool any_cont) {
     const uint32_t n = bounce == 0 ? B.cur->n_paths : B.counts[0];
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
         const uint32_t i = base + threadIdx.x;
@@ -558,11 +593,17 @@ __global__ void __launch_bounds__(256) k_shade(Batch B, int bounce, const uint32
                 cont = bounce < c.num_bounces - 1;
             }
         }
-        const uint32_t keep = live ? shade_path(B, bounce, p, req, h, cont) : 0u;
-        const uint2 at = block_append2(&B.counts[2], __popc(keep), &B.counts[1], cont ? 1u : 0u);
+        const uint32_t sp = live ? shade_path(B, bounce, p, req, h, cont) : 0u;
+        const uint32_t keep = sp & 0xFFFFu;
+        const uint2 at = block_append2(&B.counts[2], __popc(keep), &B.counts[1], 0u);
         uint32_t e = at.x;
         for (uint32_t m = keep; m; m &= m - 1) B.sidx[e++] = make_uint2(p * B.L + (uint32_t)(__ffs(m) - 1), req);
-        if (cont) q_out[at.y] = p;
+        // bounce queue grouped by ray octant within the block: warps of the bounce trace take rays
+        // with one near-to-far child order
+        if (any_cont) {   // false at the wave's last bounce: no path continues
+            const uint32_t qi = block_append_buckets8(&B.counts[1], cont ? (sp >> 16) & 7u : 8u);
+            if (cont) q_out[qi] = p;
+        }
     }
 }
 
@@ -757,7 +798,7 @@ void launch_wave_kernels(crt_context* ctx, const Batch& B, size_t P, size_t NL, 
     uint32_t* q_out = qa;
     const bool fuse = max_bounces <= 1;   // k_update adds the light of the only bounce (if any)
     for (int b = 0; b < max_bounces; ++b) {
-        k_shade<<<g_shade, 256, 0, st>>>(B, b, q_in, q_out);
+        k_shade<<<g_shade, 256, 0, st>>>(B, b, q_in, q_out, b < max_bounces - 1);
         check_launch(ctx, "k_shade");
         launch_trace<true>(ctx, SceneView{}, ShadowJob{B}, (uint32_t)std::min<size_t>(P * NL, 0xFFFFFF00u),
                            &B.counts[2], tqueue);
