@@ -176,3 +176,20 @@ def test_srp_only_batch_and_device_outputs(setup):
     f, t = standalone(q)
     np.testing.assert_array_equal(f_dev.cpu().numpy(), f)
     np.testing.assert_array_equal(t_dev.cpu().numpy(), t)
+
+
+def test_mixed_batch_with_adaptive_render(setup):
+    """Adaptive renders run their later samples in waves planned after the SRP ranges: results still
+    equal the standalone calls."""
+    ctx, d, cornell, ast = setup
+    cam = camera_from(d, "rcam")
+    reqs = [dict(kind="render", scene=cornell, camera=dict(cam, resolution=[20, 16]), lights=lights_from(d["lights"]),
+                 min_samples=2, max_samples=16, noise_threshold=1.5, num_bounces=2, seed=7, request=3, radiance=True),
+            srp_requests(ctx, ast)[1]]
+    alone = [standalone(q) for q in reqs]
+    ctx.set_tuning(queue_chunk=1, wave_paths=1 << 16, use_graphs=True)
+    outs, st = ctx.batch(reqs)
+    ctx.set_tuning()
+    for a, b in zip(alone, outs):
+        assert_same(a, b)
+    assert st["waves"] > 6

@@ -190,6 +190,18 @@ def test_malformed_request_refused_and_service_continues(server):
     np.testing.assert_array_equal(out[0], alone(good)[0])
 
 
+def test_bad_srp_attitude_fails_alone(server):
+    """An SRP query with a zero quaternion fails at admission (status != 0); the lane keeps serving."""
+    srv, d, cornell, ast = server
+    bad = dict(kind="srp", scene=ast, sun_dir=[1.0, 0.0, 0.0], quaternions=np.zeros((1, 4)), grid=64, num_bounces=1)
+    res, _ = srv.wait(srv.submit(bad), timeout=60.0)
+    assert res["status"] != 0
+    good = dict(bad, quaternions=scenes.random_quaternions(1, seed=1))
+    res, out = srv.wait(srv.submit(good), timeout=60.0)
+    assert res["status"] == 0
+    np.testing.assert_array_equal(out[0], alone(good)[0])
+
+
 def test_wait_is_bounded(server):
     srv, *_ = server
     t = time.perf_counter()
