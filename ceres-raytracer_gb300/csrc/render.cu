@@ -660,9 +660,12 @@ __global__ void k_update(Batch B) {
         const RReq& R = B.rr[S.req];
         const uint32_t pixel = S.active ? S.active[a] : tile_slot_pixel(a, R.c.W, R.c.H);
         const size_t g = (size_t)R.pix_base + pixel;
-        if (B.done[g]) continue;
-        float4 m = B.pix[g];
-        uint32_t t = B.taken[g];
+        // a slice that starts at sample 0 holds the pixel's first samples: its state is still the
+        // zeroed one (running mean, count and done flag), so it is not read
+        const bool fresh = S.s0 == 0;
+        if (!fresh && B.done[g]) continue;
+        float4 m = fresh ? make_float4(0.f, 0.f, 0.f, 0.f) : B.pix[g];
+        uint32_t t = fresh ? 0u : B.taken[g];
         for (uint32_t k = 0; k < S.ns; ++k) {
             const uint32_t sample = S.s0 + k + 1;   // 1-based as in the reference loop
             const size_t p = (size_t)S.path_base + (size_t)k * S.npix + a;
