@@ -1148,8 +1148,14 @@ void run_batch(crt_context* ctx, const crt_request* reqs, size_t n, crt_batch_st
     staging.release();   // the adaptive loop below rewrites `pin` only after synchronising the stream
     CRT_CUDA(cudaMemsetAsync(B.wave_idx, 0, 4, st));
     if (pix_total) {
-        CRT_CUDA(cudaMemsetAsync(B.pix, 0, (size_t)pix_total * 16, st));
-        CRT_CUDA(cudaMemsetAsync(B.taken, 0, (size_t)pix_total * 4, st));
+        // every pixel of a request that takes samples gets its mean and count from its first slice
+        // (k_update); only requests without samples (max_samples 0) read the zeroed state
+        bool unsampled = false;
+        for (const HostReq& h : hreq) unsampled |= h.total == 0;
+        if (unsampled) {
+            CRT_CUDA(cudaMemsetAsync(B.pix, 0, (size_t)pix_total * 16, st));
+            CRT_CUDA(cudaMemsetAsync(B.taken, 0, (size_t)pix_total * 4, st));
+        }
         CRT_CUDA(cudaMemsetAsync(B.done, 0, pix_total, st));
     }
     for (size_t k = 0; k < lr.size(); ++k) {
@@ -1721,8 +1727,10 @@ bool engine_admit(WaveEngine* e, const crt_request& q, uint64_t tag) {
         }
         engine_upload(e, e->d_rr + r.slot, &R, sizeof(R));
         if (q.n_lights) engine_upload(e, e->d_lights + R.light_base, lights, sizeof(LightDev) * q.n_lights);
-        CRT_CUDA(cudaMemsetAsync(e->pix() + r.unit_off, 0, (size_t)r.npix * 16, st));
-        CRT_CUDA(cudaMemsetAsync(e->taken() + r.unit_off, 0, (size_t)r.npix * 4, st));
+        if (r.total == 0) {   // otherwise the first slice writes the mean and count (k_update)
+            CRT_CUDA(cudaMemsetAsync(e->pix() + r.unit_off, 0, (size_t)r.npix * 16, st));
+            CRT_CUDA(cudaMemsetAsync(e->taken() + r.unit_off, 0, (size_t)r.npix * 4, st));
+        }
         CRT_CUDA(cudaMemsetAsync(e->done() + r.unit_off, 0, r.npix, st));
         e->want_P = std::max(e->want_P, r.npix);
         e->want_NL = std::max(e->want_NL, std::max<uint32_t>(q.n_lights, 1));
