@@ -5,6 +5,8 @@
 //
 //   begin     copy this wave's descriptor, reset the queue counters          (k_wave_begin)
 //   primary   LiDAR beams of the batch + camera ray per (pixel, sample)       (persistent trace)
+//             (+ the sun rays of one SRP range in crt_batch_mixed waves, whose shade and specular
+//             segments follow: srp_wave_stages)
 //   shade     surface point, one shadow ray per light, bounce ray             (k_shade)
 //   shadow    any hit for the shadow queue                                     (persistent trace)
 //   accum     sum lights, clamp after the first bounce, times path weight      (k_accum; folded into
@@ -25,8 +27,9 @@
 // FP32 secondary-ray origins: the reference offsets the hit point by 1e-4 along the flat normal
 // (unidirectional.hpp:59-61).  In FP32 at kilometre coordinates 1e-4 is about one ulp, so the
 // offset used here is max(1e-4, 4 ulp of the largest coordinate) and the triangle the ray leaves
-// is not re-tested (in FP64 the reference only meets it again when the ray points into the
-// surface, which on closed meshes the rest of the mesh occludes anyway).
+// is not re-tested.  In FP64 the reference meets that triangle again when the ray points into the
+// surface; for shadow rays the shade stage decides that case itself (mark_self_occluded), other
+// rays meet the rest of the mesh, which on closed meshes occludes them anyway.
 #include "common.cuh"
 #include "srp.cuh"
 #include "trace.cuh"
