@@ -263,7 +263,7 @@ struct PrimaryJobT {
     }
     __device__ void write(const SceneView&, uint32_t i, const TRay&, const THit& h, const Item& it) const {
         if (SRP && it.lidar == 2) {
-            B.cur->srp.hit[it.req] = make_float4(h.t, h.u, h.v, __uint_as_float(h.slot));
+            srp_store_primary(B.cur->srp, it.req, h);
             return;
         }
         if (it.lidar) {
@@ -1079,7 +1079,7 @@ void run_batch(crt_context* ctx, const crt_request* reqs, size_t n, crt_batch_st
             s_torque[j] = is_device_ptr(srps[j]->torque) ? srps[j]->torque : (double*)take(24 * na);
         }
         if (n_srp) {   // one wave's SRP item state, shared by the requests' ranges
-            s_state = (char*)take(std::max<uint64_t>(srp_max, 1) * (srp_nb ? 16 + 16 + 16 + 1 : 16) + 1024);
+            s_state = (char*)take(srp_state_bytes(std::max<uint64_t>(srp_max, 1), srp_nb));
             s_bq = srp_nb ? (uint32_t*)take(srp_max * 4 + 256) : nullptr;
             s_bcount = (uint32_t*)take(256);
         }
@@ -1212,6 +1212,7 @@ void run_batch(crt_context* ctx, const crt_request* reqs, size_t n, crt_batch_st
             if (w < sranges.size()) {
                 const SrpRange& R = sranges[w];
                 crt_scene* sc = srps[R.req]->base.scene;
+                CRT_CUDA(cudaMemsetAsync(plan[w].srp.hitmask, 0, srp_mask_bytes(R.n), st));   // before the trace
                 stages = [&, w, sc]() {
                     srp_wave_stages(ctx, scene_view(sc), plan[w].srp, (uint32_t)R.n, splans[R.req], s_partial[R.req],
                                     nullptr, (uint32_t)sc->n_tris, s_bq, s_bcount);
@@ -1781,7 +1782,7 @@ bool engine_admit_srp(WaveEngine* e, crt_scene* scene, const crt_srp_desc& desc,
     srp_plan(scene, &desc, quats, n_att, *plan);
     if (!e->srp_state) {
         const uint64_t cap = std::max<uint64_t>((uint64_t)e->want_P / SRP_BLOCK_ITEMS * SRP_BLOCK_ITEMS, SRP_BLOCK_ITEMS);
-        const size_t b_state = up256(cap * (16 + 16 + 16 + 1)), b_q = up256(cap * 4);
+        const size_t b_state = up256(srp_state_bytes(cap, 1)), b_q = up256(cap * 4);
         CRT_CUDA(cudaMalloc(&e->srp_state, b_state + b_q + 256));
         e->srp_cap = cap;
         e->srp_bq = (uint32_t*)(e->srp_state + b_state);
@@ -2045,6 +2046,7 @@ void engine_step(WaveEngine* e, std::vector<uint64_t>& completed) {
         std::function<void()> stages;
         if (sq) {
             const SrpWave W = w.srp;
+            CRT_CUDA(cudaMemsetAsync(W.hitmask, 0, srp_mask_bytes(srp_n), st));   // before the trace
             stages = [&, W]() {
                 srp_wave_stages(ctx, scene_view(sq->q.scene), W, (uint32_t)srp_n, *sq->splan, sq->partial, nullptr,
                                 (uint32_t)sq->q.scene->n_tris, e->srp_bq, e->srp_bcount);

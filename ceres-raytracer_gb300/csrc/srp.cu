@@ -199,7 +199,7 @@ struct SrpPrimaryJob : JobBase {
     SrpWave W;
     __device__ bool ray(uint32_t i, TRay& r, Item&) const { return srp_primary_ray(W, i, r); }
     __device__ void write(const SceneView&, uint32_t i, const TRay&, const THit& h, const Item&) const {
-        W.hit[i] = make_float4(h.t, h.u, h.v, __uint_as_float(h.slot));
+        srp_store_primary(W, i, h);
     }
 };
 
@@ -266,8 +266,8 @@ __global__ void __launch_bounds__(SRP_SHADE_THREADS) k_srp_shade(SceneView sv, S
         uint32_t a = 0, px = 0, py = 0, local = 0;
         bool alive = false;
         if (i < A.n_items) {
-            if (FIRST) {
-                alive = srp_item(W, i, a, px, py);
+            if (FIRST) {   // only the hits of the primary segment are stored (hit mask)
+                alive = srp_item(W, i, a, px, py) && ((W.hitmask[i >> 5] >> (i & 31u)) & 1u);
             } else {
                 alive = W.alive[i] != 0;
                 if (alive) a = srp_att(W, i, local);
@@ -453,6 +453,7 @@ SrpWave srp_wave(const SrpPlan& P, const SrpAtt* d_att, char* state, uint64_t ca
     W.r0 = (uint32_t)(i0 % P.ipa);
     W.multi = (W.r0 == 0 && n >= P.ipa) ? 1u : 0u;   // whole attitudes, else a part of one
     W.hit = (float4*)state;
+    W.hitmask = (uint32_t*)(state + srp_mask_offset(cap, P.nb));
     W.st_o = P.nb ? (float4*)(state + cap * 16) : nullptr;
     W.st_d = P.nb ? (float4*)(state + cap * 32) : nullptr;
     W.alive = P.nb ? (uint8_t*)(state + cap * 48) : nullptr;
@@ -514,7 +515,7 @@ void srp_run(crt_context* ctx, crt_scene* s, const crt_srp_desc* desc, const dou
         SrpAtt* d_att = (SrpAtt*)ctx_scratch(ctx, SCR_IN1, sizeof(SrpAtt) * n_att);
         CRT_CUDA(cudaMemcpyAsync(d_att, P.att.data(), sizeof(SrpAtt) * n_att, cudaMemcpyHostToDevice, st));
         double* d_partial = (double*)ctx_scratch(ctx, SCR_WAVE3, sizeof(double) * 6 * P.blocks_per_att * n_att);
-        char* state = (char*)ctx_scratch(ctx, SCR_WAVE4, wave_items * P.state_bytes_per_item() + 1024);
+        char* state = (char*)ctx_scratch(ctx, SCR_WAVE4, srp_state_bytes(wave_items, P.nb));
         uint32_t* bq = P.nb ? (uint32_t*)ctx_scratch(ctx, SCR_WAVE5, wave_items * 4 + 256) : nullptr;
         uint32_t* bcount = (uint32_t*)ctx_scratch(ctx, SCR_WAVE6, 256);
         double* d_force = (double*)out_device(ctx, force, n_att * 24, SCR_OUT0);
@@ -530,6 +531,7 @@ void srp_run(crt_context* ctx, crt_scene* s, const crt_srp_desc* desc, const dou
             // from L1/L2 (measured: larger grabs were slower on the 2M asteroid)
             SrpPrimaryJob J;
             J.W = W;
+            CRT_CUDA(cudaMemsetAsync(W.hitmask, 0, srp_mask_bytes(n), st));
             launch_trace<false>(ctx, sv, J, n);
             srp_wave_stages(ctx, sv, W, n, P, d_partial, d_facet, (uint32_t)s->n_tris, bq, bcount);
         }

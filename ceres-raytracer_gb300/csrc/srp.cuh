@@ -31,7 +31,8 @@ struct SrpWave {
     uint64_t i0;              // first item of the wave
     uint32_t a0, r0;          // i0 = a0 * items_per_att + r0
     uint32_t multi;           // the wave holds whole attitudes (r0 == 0) rather than part of one
-    float4* hit;              // per wave item: t, u, v, slot
+    float4* hit;              // per wave item: t, u, v, slot (primary segment: written for hits only)
+    uint32_t* hitmask;        // primary segment: one bit per wave item that hit (zeroed before the trace)
     float4* st_o;             // continuing ray: origin, power
     float4* st_d;             // continuing ray: direction, triangle it leaves
     uint8_t* alive;           // continuing ray present
@@ -81,9 +82,22 @@ struct SrpPlan {
     uint64_t blocks_per_att = 0;
     float inv_c = 0.f, cm[3] = {0.f, 0.f, 0.f};
     size_t n_att() const { return att.size(); }
-    // bytes of per-item wave state (hits, and continuation state when there are specular segments)
-    size_t state_bytes_per_item() const { return nb ? 16 + 16 + 16 + 1 : 16; }
 };
+
+// Per-wave SRP state for waves of at most `cap` items: hits (16 B per item), continuation state when
+// there are specular segments (33 B per item), then the primary segment's hit mask (1 bit per item).
+inline size_t srp_mask_offset(uint64_t cap, uint32_t nb) { return ((size_t)cap * (nb ? 49 : 16) + 255) & ~size_t(255); }
+inline size_t srp_state_bytes(uint64_t cap, uint32_t nb) {
+    return srp_mask_offset(cap, nb) + ((((size_t)cap + 31) / 32 * 4 + 255) & ~size_t(255)) + 256;
+}
+inline size_t srp_mask_bytes(uint64_t n) { return ((size_t)n + 31) / 32 * 4; }
+
+// Primary-segment result of wave item i: hits are stored and flagged in the mask; misses leave both
+__device__ __forceinline__ void srp_store_primary(const SrpWave& W, uint32_t i, const THit& h) {
+    if (h.slot == CRT_MISS) return;
+    W.hit[i] = make_float4(h.t, h.u, h.v, __uint_as_float(h.slot));
+    atomicOr(W.hitmask + (i >> 5), 1u << (i & 31u));
+}
 
 // Validates an SRP request and builds its plan; quaternions may be host or device memory.  Throws
 // CrtError.
