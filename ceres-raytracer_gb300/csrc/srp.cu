@@ -433,6 +433,13 @@ void srp_plan(crt_scene* s, const crt_srp_desc* desc, const double* quats, size_
     P.nb = specular ? desc->num_bounces : 0u;
     P.inv_c = (float)(1.0 / desc->c);
     for (int k = 0; k < 3; ++k) P.cm[k] = (float)desc->center_of_mass[k];
+    // rays that miss this box miss every triangle by far more than the FP32 error of the tests
+    const double ext = std::max(hi[0] - lo[0], std::max(hi[1] - lo[1], hi[2] - lo[2]));
+    const double m = 1e-4 * ext + 1e-5;
+    for (int k = 0; k < 3; ++k) {
+        P.box_lo[k] = (float)(lo[k] - m - 1e-6 * std::fabs(lo[k]));
+        P.box_hi[k] = (float)(hi[k] + m + 1e-6 * std::fabs(hi[k]));
+    }
 }
 
 uint64_t srp_wave_items(const SrpPlan& P, uint64_t cap, uint64_t i0) {
@@ -452,6 +459,10 @@ SrpWave srp_wave(const SrpPlan& P, const SrpAtt* d_att, char* state, uint64_t ca
     W.a0 = (uint32_t)(i0 / P.ipa);
     W.r0 = (uint32_t)(i0 % P.ipa);
     W.multi = (W.r0 == 0 && n >= P.ipa) ? 1u : 0u;   // whole attitudes, else a part of one
+    for (int k = 0; k < 3; ++k) {
+        W.box_lo[k] = P.box_lo[k];
+        W.box_hi[k] = P.box_hi[k];
+    }
     W.hit = (float4*)state;
     W.hitmask = (uint32_t*)(state + srp_mask_offset(cap, P.nb));
     W.st_o = P.nb ? (float4*)(state + cap * 16) : nullptr;
