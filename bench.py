@@ -821,17 +821,14 @@ def srp_measure(args, ctx, stream):
     t = torch.empty((n, 3), dtype=torch.float64, device=q.device)
     fp = torch.empty((n, n_tris), dtype=torch.float64, device=q.device)
 
-    def run(facet, bounces=cfg["num_bounces"]):
-        sc.srp_into(cfg["sun"], q, cfg["grid"], f, t, fp if facet else None, num_bounces=bounces)
+    def run(facet):
+        sc.srp_into(cfg["sun"], q, cfg["grid"], f, t, fp if facet else None, num_bounces=cfg["num_bounces"])
 
     with torch.cuda.stream(stream):
-        # traced rays (counting build): the primary segment alone, then with the specular segments;
-        # sun rays that miss the scene box are resolved without a trace (not counted there)
+        # rays (counting build): every sun ray of the grids, traced or resolved as a miss by the
+        # scene-box test, and the specular continuations
         ctx.reset_counters()
         ctx.set_counting(True)
-        run(False, 0)
-        primary = ctx.counters()["rays"]
-        ctx.reset_counters()
         run(True)
         cnt = ctx.counters()
         ctx.set_counting(False)
@@ -845,14 +842,11 @@ def srp_measure(args, ctx, stream):
             torch.cuda.synchronize()
             res[facet] = a.elapsed_time(b) / 1e3
     sc.close()
-    grid_rays = n * cfg["grid"] ** 2
-    resolved = grid_rays + (cnt["rays"] - primary)   # every sun ray + the specular continuations
     return {"workload": "SRP batch: spacecraft %d triangles, %d attitudes x %d^2 sun rays, %d bounces"
                         % (n_tris, n, cfg["grid"], cfg["num_bounces"]),
-            "rays": int(resolved), "mrays_s": round(resolved / res[True] / 1e6, 1),
+            "rays": int(cnt["rays"]), "mrays_s": round(cnt["rays"] / res[True] / 1e6, 1),
             "rays_note": "sun rays of the grids (traced, or resolved as misses by the scene-box test) + "
                          "specular continuations traced",
-            "rays_traced": int(cnt["rays"]), "primary_rays_traced": int(primary),
             "ms": round(res[True] * 1e3, 2), "ms_without_facet_power": round(res[False] * 1e3, 2),
             "ms_per_attitude": round(res[True] * 1e3 / n, 3), "nodes_per_ray": round(cnt["nodes"] / cnt["rays"], 2)}
 

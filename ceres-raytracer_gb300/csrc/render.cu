@@ -210,7 +210,7 @@ struct PrimaryJobT {
         const double inv = rsqrt64(s0 * s0 + s1 * s1 + s2 * s2);
         for (int k = 0; k < 3; ++k) d[k] = (L.rt[3 * k] * s0 + L.rt[3 * k + 1] * s1 + L.rt[3 * k + 2] * s2) * inv;
     }
-    __device__ bool ray(uint32_t i, TRay& r, Item& it) const {
+    __device__ int ray(uint32_t i, TRay& r, Item& it) const {   // k_trace job contract (0, 1, 2)
         const WaveDesc& w = *B.cur;
         if (i < w.n_lidar_items) {
             uint32_t lo = 0, hi = w.n_lreq;
@@ -234,10 +234,9 @@ struct PrimaryJobT {
         }
         if (SRP && i >= w.n_lidar_items + w.n_paths) {
             const uint32_t k = i - w.n_lidar_items - w.n_paths;
-            if (!srp_primary_ray(w.srp, k, r)) return false;
             it.req = k;
             it.lidar = 2;
-            return true;
+            return srp_primary_ray(w.srp, k, r);
         }
         const uint32_t p = i - w.n_lidar_items;
         const Slice& S = w.slices[find_slice_by_path(w, p)];

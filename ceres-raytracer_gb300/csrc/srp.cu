@@ -197,7 +197,7 @@ constexpr uint32_t SRP_SHADE_THREADS = 256;
 
 struct SrpPrimaryJob : JobBase {
     SrpWave W;
-    __device__ bool ray(uint32_t i, TRay& r, Item&) const { return srp_primary_ray(W, i, r); }
+    __device__ int ray(uint32_t i, TRay& r, Item&) const { return srp_primary_ray(W, i, r); }
     __device__ void write(const SceneView&, uint32_t i, const TRay&, const THit& h, const Item&) const {
         srp_store_primary(W, i, h);
     }

@@ -60,11 +60,12 @@ __device__ __forceinline__ bool srp_item(const SrpWave& W, uint32_t i, uint32_t&
     return px < W.G && py < W.G;
 }
 
-// sun ray of wave item i (false: padding item, or a ray that misses the enlarged scene box and so
-// every triangle: most of a grid around a spacecraft, whose 8-wide root test costs ~10x this one)
-__device__ __forceinline__ bool srp_primary_ray(const SrpWave& W, uint32_t i, TRay& r) {
+// sun ray of wave item i: 1 to trace, 0 for a padding item, 2 for a ray that misses the enlarged
+// scene box and so every triangle (resolved as a miss without a traversal: most of a grid around a
+// spacecraft, whose 8-wide root test costs ~10x this one); the job-contract values of k_trace
+__device__ __forceinline__ int srp_primary_ray(const SrpWave& W, uint32_t i, TRay& r) {
     uint32_t a, px, py;
-    if (!srp_item(W, i, a, px, py)) return false;
+    if (!srp_item(W, i, a, px, py)) return 0;
     const SrpAtt& P = W.att[a];
     r.o = f3(P.org[0] + px * P.du[0] + py * P.dv[0], P.org[1] + px * P.du[1] + py * P.dv[1],
              P.org[2] + px * P.du[2] + py * P.dv[2]);
@@ -77,7 +78,7 @@ __device__ __forceinline__ bool srp_primary_ray(const SrpWave& W, uint32_t i, TR
     const float z0 = (W.box_lo[2] - r.o.z) * iz, z1 = (W.box_hi[2] - r.o.z) * iz;
     const float tn = fmaxf(fmaxf(fminf(x0, x1), fminf(y0, y1)), fmaxf(fminf(z0, z1), 0.f));
     const float tf = fminf(fminf(fmaxf(x0, x1), fmaxf(y0, y1)), fmaxf(z0, z1));
-    return tn <= tf;
+    return tn <= tf ? 1 : 2;
 }
 
 // One request's attitude table and item geometry (host side)

@@ -63,9 +63,12 @@ __device__ __forceinline__ SurfacePoint surface_point(const SceneView& sv, const
     return sp;
 }
 
-// Jobs: ray(i, r, item) builds the ray of work item i (false: nothing to trace), view(sv, item)
-// names the scene to traverse (requests of one launch may use different resident scenes), and
-// write(sv, i, r, hit, item) stores the result.  JobBase supplies the single-scene defaults.
+// Jobs: ray(i, r, item) builds the ray of work item i and returns 1 to trace it, 0 when the item has
+// no ray (padding), or 2 when the ray is resolved without a traversal (a miss known from a bounding
+// test; the job has nothing to store, and the counting build counts it as a ray of zero nodes);
+// bool results mean 1 / 0.  view(sv, item) names the scene to traverse (requests of one launch may
+// use different resident scenes), and write(sv, i, r, hit, item) stores the result.  JobBase
+// supplies the single-scene defaults.
 struct JobBase {
     struct Item {};
     __device__ __forceinline__ const SceneView& view(const SceneView& sv, const Item&) const { return sv; }
@@ -103,11 +106,12 @@ __global__ void __launch_bounds__(CRT_TRACE_BLOCK, 8) k_trace(SceneView sv, Job 
             const uint32_t i = base + 32u * c + lane;
             TRay r;
             typename Job::Item it;
-            if (i < n_items && job.ray(i, r, it)) {
+            const int kind = i < n_items ? (int)job.ray(i, r, it) : 0;
+            if (kind == 1) {
                 const THit h = traverse<ANY, COUNT>(job.view(sv, it), r, sstack + threadIdx.x, CRT_TRACE_BLOCK, st, err);
                 job.write(sv, i, r, h, it);
-                if (COUNT) ++nrays;
             }
+            if (COUNT && kind != 0) ++nrays;
         }
     }
     if (COUNT) {
