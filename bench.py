@@ -354,7 +354,7 @@ def gpu_arm(args):
         c_scan = ctx.counters()
         ctx.set_counting(False)
         ctx.synchronize()
-    rays_step = int(c_render["rays"] + c_scan["rays"])
+    rays_step = int(c_render["answered"] + c_scan["answered"])
 
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True),
            torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
@@ -525,7 +525,7 @@ def batched_measure(ctx, ents, stream, reps=1):
         ctx.reset_counters()
         ctx.set_counting(True)
         ctx.batch(breqs, outputs=outs)
-        rays = ctx.counters()["rays"]
+        rays = ctx.counters()["answered"]
         ctx.set_counting(False)
         ctx.batch(breqs, outputs=outs)      # warm-up (scratch sized, graph path exercised)
         per_call()
@@ -604,7 +604,7 @@ def mixed_measure(ctx, breqs, outs, stream):
         ctx.reset_counters()
         ctx.set_counting(True)
         _, st = ctx.batch(mreqs, outputs=mouts)
-        rays = ctx.counters()["rays"]
+        rays = ctx.counters()["answered"]
         ctx.set_counting(False)
         ctx.batch(mreqs, outputs=mouts)      # warm-up
         per_call()
@@ -662,7 +662,7 @@ def served_measure(args, device):
     srv.ctx.set_counting(True)
     for _, q in items:
         call(q)
-    rays = int(srv.ctx.counters()["rays"])
+    rays = int(srv.ctx.counters()["answered"])
     srv.ctx.set_counting(False)
     for _, q in items[:64]:                       # warm-up of both paths
         call(q)
@@ -779,7 +779,7 @@ def cornell_measure(ctx, stream, cpu=True):
         ctx.reset_counters()
         ctx.set_counting(True)
         render()
-        rays = int(ctx.counters()["rays"])
+        rays = int(ctx.counters()["answered"])
         ctx.set_counting(False)
         times = {}
         for name, fn, reps in (("render", render, 10), ("passes", passes, 20)):
@@ -844,7 +844,8 @@ def srp_measure(args, ctx, stream):
     sc.close()
     return {"workload": "SRP batch: spacecraft %d triangles, %d attitudes x %d^2 sun rays, %d bounces"
                         % (n_tris, n, cfg["grid"], cfg["num_bounces"]),
-            "rays": int(cnt["rays"]), "mrays_s": round(cnt["rays"] / res[True] / 1e6, 1),
+            "rays": int(cnt["answered"]), "mrays_s": round(cnt["answered"] / res[True] / 1e6, 1),
+            "rays_traversed": int(cnt["rays"]),
             "rays_note": "sun rays of the grids (traced, or resolved as misses by the scene-box test) + "
                          "specular continuations traced",
             "ms": round(res[True] * 1e3, 2), "ms_without_facet_power": round(res[False] * 1e3, 2),

@@ -104,7 +104,7 @@ class SceneStats(ctypes.Structure):
 
 class Counters(ctypes.Structure):
     _fields_ = [("rays", ctypes.c_uint64), ("nodes", ctypes.c_uint64), ("tris", ctypes.c_uint64),
-                ("launches", ctypes.c_uint64)]
+                ("launches", ctypes.c_uint64), ("resolved", ctypes.c_uint64)]
 
 
 RAY_DTYPE = np.dtype([("o", np.float32, 3), ("tmin", np.float32), ("d", np.float32, 3), ("tmax", np.float32)])
@@ -271,7 +271,9 @@ class Context:
     def counters(self):
         c = Counters()
         self._check(self.L.crt_context_get_counters(self.h, ctypes.byref(c)))
-        return dict(rays=c.rays, nodes=c.nodes, tris=c.tris, launches=c.launches)
+        # rays: traversed; resolved: answered without a traversal; answered: both
+        return dict(rays=c.rays, nodes=c.nodes, tris=c.tris, launches=c.launches, resolved=c.resolved,
+                    answered=c.rays + c.resolved)
 
     def reset_counters(self):
         self._check(self.L.crt_context_reset_counters(self.h))

@@ -240,6 +240,7 @@ int crt_context_get_counters(crt_context* ctx, crt_counters* out) {
         out->nodes = h[1];
         out->tris = h[2];
         out->launches = ctx->launches;
+        out->resolved = h[3];
     });
 }
 

@@ -572,9 +572,11 @@ __device__ __forceinline__ uint32_t shade_path(const Batch& B, int bounce, uint3
 
 // 256-thread blocks (block_append2); the loop's trip count is uniform over a block.  The shadow queue
 // receives the shadow rays still to trace after the shade, in path order within a block; rays that
-// their own triangle stops (mark_self_occluded) are not queued.
+// their own triangle stops (mark_self_occluded) are not queued, and the counting build (counters
+// non-null) counts them among the rays resolved without a traversal (counters[3]).
 __global__ void __launch_bounds__(256) k_shade(Batch B, int bounce, const uint32_t* __restrict__ q_in,
-                                               uint32_t* __restrict__ q_out, bool any_cont) {
+                                               uint32_t* __restrict__ q_out, bool any_cont,
+                                               unsigned long long* __restrict__ counters) {
     const uint32_t n = bounce == 0 ? B.cur->n_paths : B.counts[0];
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
         const uint32_t i = base + threadIdx.x;
@@ -597,6 +599,11 @@ __global__ void __launch_bounds__(256) k_shade(Batch B, int bounce, const uint32
         }
         const uint32_t sp = live ? shade_path(B, bounce, p, req, h, cont) : 0u;
         const uint32_t keep = sp & 0xFFFFu;
+        if (counters) {   // uniform: a kernel argument
+            const uint32_t resolved = live ? B.rr[req].n_lights - __popc(keep) : 0u;
+            const uint32_t wsum = __reduce_add_sync(0xFFFFFFFFu, resolved);
+            if ((threadIdx.x & 31) == 0 && wsum) atomicAdd(counters + 3, (unsigned long long)wsum);
+        }
         const uint2 at = block_append2(&B.counts[2], __popc(keep), &B.counts[1], 0u);
         uint32_t e = at.x;
         for (uint32_t m = keep; m; m &= m - 1) B.sidx[e++] = make_uint2(p * B.L + (uint32_t)(__ffs(m) - 1), req);
@@ -803,7 +810,8 @@ void launch_wave_kernels(crt_context* ctx, const Batch& B, size_t P, size_t NL, 
     uint32_t* q_out = qa;
     const bool fuse = max_bounces <= 1;   // k_update adds the light of the only bounce (if any)
     for (int b = 0; b < max_bounces; ++b) {
-        k_shade<<<g_shade, 256, 0, st>>>(B, b, q_in, q_out, b < max_bounces - 1);
+        k_shade<<<g_shade, 256, 0, st>>>(B, b, q_in, q_out, b < max_bounces - 1,
+                                         ctx->counting ? ctx->d_counters : nullptr);
         check_launch(ctx, "k_shade");
         launch_trace<true>(ctx, SceneView{}, ShadowJob{B}, (uint32_t)std::min<size_t>(P * NL, 0xFFFFFF00u),
                            &B.counts[2], tqueue);

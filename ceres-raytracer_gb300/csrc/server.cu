@@ -132,7 +132,7 @@ void lane_loop(crt_server* S, size_t lane) {
             }
             S->stats.batches++;
             S->stats.busy_s += t1 - t0;
-            if (S->cfg.count_rays) S->stats.rays += c1.rays - c0.rays;
+            if (S->cfg.count_rays) S->stats.rays += (c1.rays + c1.resolved) - (c0.rays + c0.resolved);
         }
         S->cv_done.notify_all();
     }

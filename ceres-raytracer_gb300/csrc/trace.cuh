@@ -65,7 +65,7 @@ __device__ __forceinline__ SurfacePoint surface_point(const SceneView& sv, const
 
 // Jobs: ray(i, r, item) builds the ray of work item i and returns 1 to trace it, 0 when the item has
 // no ray (padding), or 2 when the ray is resolved without a traversal (a miss known from a bounding
-// test; the job has nothing to store, and the counting build counts it as a ray of zero nodes);
+// test; the job has nothing to store, and the counting build counts it among the resolved rays);
 // bool results mean 1 / 0.  view(sv, item) names the scene to traverse (requests of one launch may
 // use different resident scenes), and write(sv, i, r, hit, item) stores the result.  JobBase
 // supplies the single-scene defaults.
@@ -87,7 +87,7 @@ __global__ void __launch_bounds__(CRT_TRACE_BLOCK, 8) k_trace(SceneView sv, Job 
     if (n_dev) n_items = *n_dev;   // item count produced by an earlier kernel on the stream
     const int lane = threadIdx.x & 31;
     TravStats st{0u, 0u};
-    uint32_t nrays = 0;
+    uint32_t nrays = 0, nres = 0;
     const uint32_t warps_total = gridDim.x * (blockDim.x >> 5);
     while (true) {
         uint32_t base = 0, take = 1;
@@ -111,20 +111,25 @@ __global__ void __launch_bounds__(CRT_TRACE_BLOCK, 8) k_trace(SceneView sv, Job 
                 const THit h = traverse<ANY, COUNT>(job.view(sv, it), r, sstack + threadIdx.x, CRT_TRACE_BLOCK, st, err);
                 job.write(sv, i, r, h, it);
             }
-            if (COUNT && kind != 0) ++nrays;
+            if (COUNT) {
+                nrays += kind == 1;
+                nres += kind == 2;
+            }
         }
     }
     if (COUNT) {
-        unsigned long long a = nrays, b = st.nodes, c = st.tris;
+        unsigned long long a = nrays, b = st.nodes, c = st.tris, d = nres;
         for (int o = 16; o; o >>= 1) {
             a += __shfl_xor_sync(0xffffffffu, a, o);
             b += __shfl_xor_sync(0xffffffffu, b, o);
             c += __shfl_xor_sync(0xffffffffu, c, o);
+            d += __shfl_xor_sync(0xffffffffu, d, o);
         }
         if (lane == 0) {
             atomicAdd(counters + 0, a);
             atomicAdd(counters + 1, b);
             atomicAdd(counters + 2, c);
+            if (d) atomicAdd(counters + 3, d);
         }
     }
 }

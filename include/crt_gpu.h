@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define CRT_ABI_VERSION 1
+#define CRT_ABI_VERSION 2
 
 enum {
     CRT_OK = 0,
@@ -182,6 +182,8 @@ typedef struct {
     uint64_t nodes;           /* 8-wide nodes fetched */
     uint64_t tris;            /* triangles tested */
     uint64_t launches;        /* kernels launched by the library on this context (always counted) */
+    uint64_t resolved;        /* rays answered without a traversal (counting mode): SRP sun rays that
+                                 miss the scene box, shadow rays stopped by the surface they leave */
 } crt_counters;
 
 /* ---------------------------------------------------------------- context */
@@ -317,7 +319,8 @@ typedef struct {
 } crt_server_result;
 typedef struct {
     uint64_t submitted, completed, batches, failed;   /* batches: waves run */
-    uint64_t rays;                        /* rays traced by completed batches (count_rays only) */
+    uint64_t rays;                        /* rays of completed batches, traversed or resolved without a
+                                             traversal (count_rays only) */
     double busy_s;                        /* summed lane time */
 } crt_server_stats;
 

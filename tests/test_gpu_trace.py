@@ -88,7 +88,7 @@ def camera_parity(ctx_scene, o, cam, ref=None):
 
 
 def test_abi_version_and_context(ctx):
-    assert lib.load().crt_abi_version() == 1
+    assert lib.load().crt_abi_version() == 2
 
 
 @pytest.mark.parametrize("name", ["cornell", "asteroid"])
