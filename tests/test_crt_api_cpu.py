@@ -100,3 +100,28 @@ def test_rotations_module():
     np.testing.assert_allclose(R @ R.T, np.eye(3), atol=1e-14)
     with pytest.raises(Exception):
         euler_to_rotmat("124", [0, 0, 0])
+
+
+def test_srp_request_packing():
+    """An SRP query of a mixed batch / server request fills crt_server_request as the C side reads it
+    (kind SRP, the scene handle, the descriptor, n_att quaternions and the two output buffers)."""
+    import ctypes
+    from crt_gb300 import lib
+
+    class FakeScene:
+        h = ctypes.c_void_p(0x1234)
+
+    q = dict(kind="srp", scene=FakeScene(), sun_dir=[0.0, 2.0, 0.0], quaternions=np.eye(4)[:3], grid=640,
+             num_bounces=1, flux=1000.0, center_of_mass=(0.1, 0.2, 0.3))
+    sr, keep = lib.ServerRequest(), []
+    force, torque = lib.fill_srp_request(q, sr, None, keep)
+    assert sr.base.kind == lib.REQUEST_SRP and sr.base.scene == 0x1234
+    assert sr.n_att == 3 and force.shape == (3, 3) and torque.shape == (3, 3)
+    assert sr.force == force.ctypes.data and sr.torque == torque.ctypes.data
+    d = sr.srp.contents
+    assert list(d.sun_dir_inertial) == [0.0, 2.0, 0.0] and d.grid == 640 and d.num_bounces == 1
+    assert d.flux == 1000.0 and abs(d.c - 299792458.0) < 1 and list(d.center_of_mass) == [0.1, 0.2, 0.3]
+    quats = np.ctypeslib.as_array(ctypes.cast(sr.quaternions, ctypes.POINTER(ctypes.c_double)), shape=(3, 4))
+    np.testing.assert_array_equal(quats, np.eye(4)[:3])
+    # the request struct the C ABI reads: base request, then the SRP fields
+    assert ctypes.sizeof(lib.ServerRequest) == ctypes.sizeof(lib.Request) + 5 * 8
