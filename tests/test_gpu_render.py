@@ -181,3 +181,23 @@ def test_terminator_shadow_rays_resolved_in_shade(ctx):
     shadow = rays - 128 * 128
     assert lit <= shadow < hits, (lit, shadow, hits)
     assert shadow < 0.9 * hits
+
+
+def test_smooth_shaded_two_bounce_render_vs_oracle(ctx):
+    """Smooth-shaded asteroid, 2 bounces, the oracle's random streams: bounce directions sampled about
+    the interpolated normal can point into the flat surface they leave (the reference then meets its
+    own triangle again); per-pixel radiance still agrees on nearly all pixels and the image mean
+    within 1 %."""
+    ents = [scenes.EntitySpec("a", scenes.asteroid(100_000, seed=3), (0.3, 0.3, 0.3), smooth=True)]
+    sc, o = ctx.scene(ents), oracle.Scene(ents)
+    view = scenes.unit_vector(21)
+    sun = view + 0.5 * scenes.unit_vector(22)   # lit from near the camera: most of the view is sunlit
+    sun /= np.linalg.norm(sun)
+    lights = [dict(type="point", intensity=1.0e18, position=1.0e9 * sun)]
+    cam = scenes.fov_camera(scenes.TAN5 * 2.4, (48, 48), 5000.0 * view, (0.0, 0.0, 0.0))
+    _, rad = sc.render(cam, lights, 4, 4, 0.0, 2, seed=11)
+    orad, _, _ = o.render(cam, lights, 4, 4, 0.0, 2, seed=11)
+    assert (orad[..., 0] > 0).mean() > 0.5
+    close = np.isclose(rad[..., :3], orad[..., :3], rtol=2e-3, atol=1e-3).all(-1)
+    assert close.mean() > 0.95, close.mean()
+    assert abs(rad[..., :3].mean() / orad[..., :3].mean() - 1) < 0.01
