@@ -289,3 +289,32 @@ def test_counting_mode(ctx, ast100k):
     assert c["rays"] == 128 * 128
     assert c["nodes"] >= c["rays"] and c["tris"] > 0
     assert c["launches"] >= 1
+
+
+def test_z_positive_camera_and_lidar_match_oracle(ctx):
+    """Cameras and LiDARs with z_positive (boresight +z in their frame, simple_camera.hpp:61-81,
+    simple_lidar.hpp:42-64): passes and per-pose LiDAR equal the oracle's; a z_positive beam grid
+    with the frame turned about y equals the default grid mirrored in x."""
+    d = load_golden("cornell")
+    ents = entities_from(d)
+    sc, o = ctx.scene(ents), oracle.Scene(ents)
+    F = np.diag([-1.0, 1.0, -1.0])   # half turn about y: the +z boresight looks where -z did
+    cam = camera_from(d, "rcam")
+    camz = dict(cam, z_positive=True, rotation=F @ np.asarray(cam["rotation"]), resolution=[40, 32])
+    gx, gi, gn = sc.passes(camz)
+    ox, oi, on, _ = o.passes(camz)
+    assert (oi > 0).mean() > 0.9
+    assert (gi == oi).mean() > 0.99
+    ok = (gi == oi) & (oi > 0)
+    np.testing.assert_allclose(gx[ok], ox[ok], rtol=DIST_REL, atol=1e-9)
+    pos = np.array([[0.5, 0.5, 2.4], [0.3, 0.6, 2.0], [0.7, 0.2, 1.5]])
+    rot = np.stack([F, F, F]).reshape(3, 9)
+    rng, prim = sc.lidar_batch(pos, rot, z_positive=True)
+    rng_o, prim_o = o.lidar_batch(pos, rot, z_positive=True)
+    np.testing.assert_array_equal(prim, prim_o)
+    np.testing.assert_allclose(rng, rng_o, rtol=DIST_REL)
+    g_z, p_z = sc.lidar_grid([0.5, 0.5, 2.4], F, 11, 9, 0.3, 0.2, z_positive=True)
+    g_0, p_0 = sc.lidar_grid([0.5, 0.5, 2.4], np.eye(3), 11, 9, 0.3, 0.2)
+    assert (p_z[:, ::-1] == p_0).mean() > 0.95
+    same = p_z[:, ::-1] == p_0
+    np.testing.assert_allclose(g_z[:, ::-1][same], g_0[same], rtol=1e-9)
