@@ -662,6 +662,7 @@ constexpr int SAH_T = 4;
 constexpr int SAH_W = 13;                               // count, box lo/hi, centroid lo/hi (fkeys)
 constexpr int SAH_TASK_WORDS = 3 * SAH_BINS * SAH_W;
 constexpr int SAH_BLOCK_ITEMS = 2048;
+constexpr int SAH_SMALL = 2048;                         // tasks of at most this many triangles: k_sah_bin_small
 
 struct SahTask {
     int first, count;
@@ -714,8 +715,40 @@ __device__ __forceinline__ void sah_add(uint32_t* b, const float4& lo, const flo
     atomicMax(&b[10], fkey(c.x)); atomicMax(&b[11], fkey(c.y)); atomicMax(&b[12], fkey(c.z));
 }
 
+// One warp per task of at most SAH_SMALL triangles: the warp bins its task's positions (a contiguous
+// range) into warp-private shared memory, where only its own lanes contend, and stores the task's
+// bins, which no other kernel writes (k_sah_bin skips these tasks).  Counts, minima and maxima do not
+// depend on the order of the additions, so the bins equal those of k_sah_bin.
+__global__ void __launch_bounds__(256) k_sah_bin_small(const uint32_t* __restrict__ perm,
+                                                       const SahTask* __restrict__ tasks, int n_tasks,
+                                                       const float4* __restrict__ tbox, const float4* __restrict__ cen,
+                                                       uint32_t* __restrict__ bins) {
+    __shared__ uint32_t sb[8][SAH_TASK_WORDS];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int t = blockIdx.x * 8 + warp;
+    if (t >= n_tasks) return;            // warp-uniform; the kernel has no block-wide barrier
+    const SahTask T = tasks[t];
+    if (T.count > SAH_SMALL) return;     // warp-uniform: binned by k_sah_bin
+    uint32_t* b = sb[warp];
+    for (int w = lane; w < SAH_TASK_WORDS; w += 32) {
+        const int k = w % SAH_W;
+        b[w] = k == 0 ? 0u : (((k - 1) % 6) < 3 ? 0xFFFFFFFFu : 0u);
+    }
+    __syncwarp();
+    for (int i = T.first + lane; i < T.first + T.count; i += 32) {
+        const uint32_t p = perm[i];
+        const float4 lo = tbox[2ull * p], hi = tbox[2ull * p + 1], c = cen[p];
+        const float cv[3] = {c.x, c.y, c.z};
+        for (int a = 0; a < 3; ++a) sah_add(b + (a * SAH_BINS + sah_bin(cv[a], T.clo[a], T.chi[a])) * SAH_W, lo, hi, c);
+    }
+    __syncwarp();
+    uint32_t* g = bins + (size_t)t * SAH_TASK_WORDS;
+    for (int w = lane; w < SAH_TASK_WORDS; w += 32) g[w] = b[w];
+}
+
 // One block per SAH_BLOCK_ITEMS positions; a block whose positions all belong to one task (tasks
-// are contiguous ranges) bins into shared memory first.
+// are contiguous ranges) bins into shared memory first.  Positions of tasks of at most SAH_SMALL
+// triangles are left to k_sah_bin_small.
 __global__ void __launch_bounds__(256) k_sah_bin(const uint32_t* __restrict__ perm, const int* __restrict__ task_of,
                                                  const SahTask* __restrict__ tasks, const float4* __restrict__ tbox,
                                                  const float4* __restrict__ cen, int n, uint32_t* __restrict__ bins) {
@@ -724,6 +757,7 @@ __global__ void __launch_bounds__(256) k_sah_bin(const uint32_t* __restrict__ pe
     if (b0 >= n) return;
     const int t0 = task_of[b0], t1 = task_of[b1 - 1];
     const bool priv = t0 >= 0 && t0 == t1;
+    if (priv && tasks[t0].count <= SAH_SMALL) return;   // block-uniform, before any barrier
     if (priv) {
         for (int w = threadIdx.x; w < SAH_TASK_WORDS; w += blockDim.x) {
             const int k = w % SAH_W;
@@ -735,6 +769,7 @@ __global__ void __launch_bounds__(256) k_sah_bin(const uint32_t* __restrict__ pe
         const int t = task_of[i];
         if (t < 0) continue;
         const SahTask& T = tasks[t];
+        if (T.count <= SAH_SMALL) continue;
         const uint32_t p = perm[i];
         const float4 lo = tbox[2ull * p], hi = tbox[2ull * p + 1], c = cen[p];
         const float cv[3] = {c.x, c.y, c.z};
@@ -1094,6 +1129,8 @@ int sah_topology(crt_context* ctx, int n, const float4* tbox, const float4* cen,
         k_sah_bin<<<(n + SAH_BLOCK_ITEMS - 1) / SAH_BLOCK_ITEMS, 256, 0, st>>>(perm[cur], task_of[cur], tasks[cur],
                                                                               tbox, cen, n, bins);
         check_launch(ctx, "k_sah_bin");
+        k_sah_bin_small<<<(n_tasks + 7) / 8, 256, 0, st>>>(perm[cur], tasks[cur], n_tasks, tbox, cen, bins);
+        check_launch(ctx, "k_sah_bin_small");
         k_sah_split<<<(n_tasks + 127) / 128, 128, 0, st>>>(tasks[cur], n_tasks, bins, splits);
         check_launch(ctx, "k_sah_split");
         k_sah_flags<<<(n + 255) / 256, 256, 0, st>>>(perm[cur], task_of[cur], tasks[cur], splits, cen, n, flags);
