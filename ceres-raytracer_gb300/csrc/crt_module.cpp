@@ -478,10 +478,10 @@ struct BodyFixedGroup : Pose {
     crt_scene* sc() const { return scene->s; }
 };
 
-// The dynamic path rebuilds the BVH on every call.  The binned-SAH topology costs about 7 ns per
-// triangle more to build than the radix tree (2M triangles: 19 vs 4.5 ms) and saves about 10 % of
-// the traversal, ~0.02 ns of ~0.2 ns per ray, so a call uses it only when it traces more than about
-// 400 rays per triangle; `rays` is the call's estimate.
+// The dynamic path rebuilds the BVH on every call.  The binned-SAH topology costs about 5.4 ns per
+// triangle more to build than the radix tree (2M triangles: 15.2 vs 4.5 ms) and saves about 10 % of
+// the traversal, ~0.018 ns of ~0.18 ns per ray, so a call uses it only when it traces more than
+// about 300 rays per triangle; `rays` is the call's estimate.
 std::unique_ptr<SceneHandle> dynamic_scene(const py::list& entities, bool assign_ids, double rays) {
     std::vector<crt_entity_desc> descs;
     uint32_t id = 1;
@@ -492,7 +492,7 @@ std::unique_ptr<SceneHandle> dynamic_scene(const py::list& entities, bool assign
         descs.push_back(entity_desc(e, *e.mesh, e.id));
         n_tris += (double)e.mesh->n;
     }
-    return build_scene(descs, rays > 400.0 * n_tris ? 1 : 0);
+    return build_scene(descs, rays > 300.0 * n_tris ? 1 : 0);
 }
 
 double pixels(const SimpleCamera& c) { return (double)std::max(c.width(), 0) * (double)std::max(c.height(), 0); }
