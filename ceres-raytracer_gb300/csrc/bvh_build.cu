@@ -27,7 +27,6 @@
 namespace {
 
 constexpr int BLOCK = 256;
-constexpr uint32_t NO_CHILD = 0xFFFFFFFFu;
 
 struct EntXform {
     double scale;
@@ -599,9 +598,9 @@ __global__ void k_collapse(CollapseArgs A, const int2* __restrict__ frontier, ui
             continue;
         }
         for (int a = 0; a < 3; ++a) {
-            const double q = ldexp(1.0, ex[a]);
-            double l = floor(((double)clo[k][a] - (double)p[a]) / q);
-            double h = ceil(((double)chi[k][a] - (double)p[a]) / q);
+            const double iq = ldexp(1.0, -ex[a]);   // 1 / 2^ex, exact: the products equal the quotients
+            double l = floor(((double)clo[k][a] - (double)p[a]) * iq);
+            double h = ceil(((double)chi[k][a] - (double)p[a]) * iq);
             l -= 1.0;
             h += 1.0;
             if (l < 0 || h > 255) atomicOr(A.err, (uint32_t)DEVERR_QUANT_RANGE);
