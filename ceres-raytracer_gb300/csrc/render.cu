@@ -623,10 +623,10 @@ __global__ void __launch_bounds__(256) k_shade(Batch B, int bounce, const uint32
 __device__ __forceinline__ float4 add_light(const Batch& B, uint32_t p, uint32_t n_lights, int bounce, float4 r) {
     float3 lr = f3(0.f, 0.f, 0.f);
     for (uint32_t l = 0; l < n_lights; ++l) {
-        if (!B.occ[(size_t)p * B.L + l]) {
-            const float4 cb = B.contrib[(size_t)p * B.L + l];
-            lr = f3(__fadd_rn(lr.x, cb.x), __fadd_rn(lr.y, cb.y), __fadd_rn(lr.z, cb.z));
-        }
+        // both loads issued together (the contribution slot exists whether or not it was written)
+        const uint8_t oc = B.occ[(size_t)p * B.L + l];
+        const float4 cb = B.contrib[(size_t)p * B.L + l];
+        if (!oc) lr = f3(__fadd_rn(lr.x, cb.x), __fadd_rn(lr.y, cb.y), __fadd_rn(lr.z, cb.z));
     }
     if (bounce >= 1) {   // unidirectional.hpp:74-78
         lr.x = fminf(fmaxf(lr.x, 0.f), 1.f);
@@ -655,7 +655,7 @@ __global__ void k_accum(Batch B, int bounce, const uint32_t* __restrict__ q_in) 
 // ---------------------------------------------------------------- pixel update (do_render.hpp:84-114)
 // ACC0: the wave's only bounce is bounce 0 and its light is added here instead of by k_accum
 template <bool ACC0>
-__global__ void k_update(Batch B) {
+__global__ void __launch_bounds__(256, 5) k_update(Batch B) {
     const WaveDesc& w = *B.cur;
     for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < w.n_update; u += gridDim.x * blockDim.x) {
         uint32_t lo = 0, hi = w.n_slices;
@@ -680,9 +680,12 @@ __global__ void k_update(Batch B) {
             const size_t p = (size_t)S.path_base + (size_t)k * S.npix + a;
             float4 L;
             if (ACC0) {
-                L = make_float4(0.f, 0.f, 0.f, 0.f);
-                if (R.c.num_bounces > 0 && __float_as_uint(B.hit[p].w) != CRT_MISS)
-                    L = add_light(B, (uint32_t)p, R.n_lights, 0, L);
+                // the lights' flags and contributions are read with the hit flag, not after it (a missed
+                // path's slots hold stale values, which are not used)
+                const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+                const bool hit = __float_as_uint(B.hit[p].w) != CRT_MISS;
+                const float4 Lh = add_light(B, (uint32_t)p, R.n_lights, 0, zero);
+                L = R.c.num_bounces > 0 && hit ? Lh : zero;
             } else {
                 L = B.rad[p];
             }
