@@ -14,6 +14,7 @@
 #include <deque>
 #include <thread>
 #include <unordered_map>
+#include <unordered_set>
 
 namespace {
 
@@ -55,6 +56,7 @@ struct crt_server {
     std::condition_variable cv_work, cv_done;
     std::deque<Pending*> queue;
     std::unordered_map<uint64_t, crt_server_result> done;
+    std::unordered_set<uint64_t> outstanding;   // issued and not yet collected by crt_server_wait
     uint64_t next_ticket = 1;
     bool stop = false;
     crt_server_stats stats;
@@ -254,6 +256,7 @@ int crt_server_submit(crt_server* S, const crt_server_request* r, uint64_t* tick
         p->ticket = S->next_ticket++;
         p->submit_s = now_s();
         *ticket = p->ticket;
+        S->outstanding.insert(p->ticket);
         S->queue.push_back(p);
         S->stats.submitted++;
     }
@@ -264,11 +267,18 @@ int crt_server_submit(crt_server* S, const crt_server_request* r, uint64_t* tick
 int crt_server_wait(crt_server* S, uint64_t ticket, double timeout_s, crt_server_result* out) {
     if (!S || !out) return CRT_ERR_INVALID;
     std::unique_lock<std::mutex> lk(S->mu);
-    auto ready = [&] { return S->done.count(ticket) != 0; };
+    if (!S->outstanding.count(ticket)) return CRT_ERR_INVALID;   // never issued, or already collected
+    // ready also when another thread collected the ticket meanwhile (it notifies cv_done)
+    auto ready = [&] { return S->done.count(ticket) != 0 || !S->outstanding.count(ticket); };
     if (timeout_s < 0) S->cv_done.wait(lk, ready);
     else if (!S->cv_done.wait_for(lk, std::chrono::duration<double>(timeout_s), ready)) return CRT_ERR_TIMEOUT;
-    *out = S->done[ticket];
-    S->done.erase(ticket);
+    auto it = S->done.find(ticket);
+    if (it == S->done.end()) return CRT_ERR_INVALID;
+    *out = it->second;
+    S->done.erase(it);
+    S->outstanding.erase(ticket);
+    lk.unlock();
+    S->cv_done.notify_all();
     return CRT_OK;
 }
 

@@ -335,7 +335,8 @@ int crt_server_destroy(crt_server* server);
 int crt_server_submit(crt_server* server, const crt_server_request* request, uint64_t* ticket);
 /* Message of the calling thread's last failed crt_server_submit. */
 const char* crt_server_last_error(void);
-/* Waits up to timeout_s (negative: forever) for a ticket; CRT_ERR_TIMEOUT when it has not finished. */
+/* Waits up to timeout_s (negative: forever) for a ticket; CRT_ERR_TIMEOUT when it has not finished.
+ * A ticket's result is collected once: CRT_ERR_INVALID for a ticket never issued or already collected. */
 int crt_server_wait(crt_server* server, uint64_t ticket, double timeout_s, crt_server_result* out);
 int crt_server_get_stats(crt_server* server, crt_server_stats* out);
 

@@ -5,7 +5,8 @@
   its waves and finish before it;
 * admission by memory budget: with a budget smaller than any request each request runs alone;
 * malformed requests are refused at submission and the server keeps serving;
-* waits are bounded (CRT_ERR_TIMEOUT), no GPU-side waiting is involved.
+* waits are bounded (CRT_ERR_TIMEOUT), no GPU-side waiting is involved; a ticket never issued or
+  already collected is refused (CRT_ERR_INVALID).
 """
 import threading
 import time
@@ -203,8 +204,23 @@ def test_bad_srp_attitude_fails_alone(server):
 
 
 def test_wait_is_bounded(server):
-    srv, *_ = server
+    srv, d, cornell, _ = server
+    # a ticket never issued is refused at once, even by an unbounded wait
     t = time.perf_counter()
     with pytest.raises(lib.CrtError) as e:
-        srv.wait(10 ** 9, timeout=0.05)
-    assert e.value.status == -4 and time.perf_counter() - t < 5.0
+        srv.wait(10 ** 9, timeout=-1.0)
+    assert e.value.status == -1 and time.perf_counter() - t < 5.0
+    # a wait shorter than the request ends with CRT_ERR_TIMEOUT (1024^2 x 16 spp x 3 bounces: 16.8 M
+    # paths, milliseconds of GPU work after admission); the result is then collected exactly once
+    cam = camera_from(d, "rcam")
+    q = dict(kind="render", scene=cornell, camera=dict(cam, resolution=[1024, 1024]), lights=lights_from(d["lights"]),
+             min_samples=16, max_samples=16, noise_threshold=0.0, num_bounces=3, seed=5, request=5, radiance=True)
+    tk = srv.submit(q)
+    with pytest.raises(lib.CrtError) as e:
+        srv.wait(tk, timeout=0.0)
+    assert e.value.status == -4
+    res, out = srv.wait(tk, timeout=120.0)
+    assert res["status"] == 0 and np.isfinite(out[1]).all()
+    with pytest.raises(lib.CrtError) as e:
+        srv.wait(tk, timeout=0.0)
+    assert e.value.status == -1
