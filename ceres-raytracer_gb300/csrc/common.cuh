@@ -74,7 +74,7 @@ struct crt_context {
     cudaStream_t stream = nullptr;
     std::string last_error;
     bool counting = false;
-    unsigned long long* d_counters = nullptr;   // rays, nodes, tris
+    unsigned long long* d_counters = nullptr;   // rays, nodes, tris, resolved
     uint32_t* d_error = nullptr;                // device error word
     uint64_t launches = 0;
     void* scratch[SCR_COUNT] = {};
@@ -90,9 +90,6 @@ struct crt_context {
     int use_graphs = 1;              // replay batched waves as CUDA graphs
     int build_sah = 1;               // scene builds: binned-SAH topology (1) or Karras radix tree (0)
     float collapse_tri_cost = 0.15f; // scene builds: triangle-test cost of the 8-wide collapse (node = 1)
-    // graph cache of the batched wavefront (one executable per wave shape)
-    void* graph_exec = nullptr;
-    uint64_t graph_key = 0;
 };
 
 // Grow-only device scratch buffer for one purpose.  Synchronises the stream before reallocating.

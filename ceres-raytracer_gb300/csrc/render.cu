@@ -1192,28 +1192,32 @@ void run_batch(crt_context* ctx, const crt_request* reqs, size_t n, crt_batch_st
     size_t waves_run = 0;
     const bool graph_ok = ctx->use_graphs && !ctx->counting && plan.size() > 1 && n_srp == 0;
     if (graph_ok) {
-        // capture one wave, replay it for every wave of the plan
-        cudaGraph_t g = nullptr;
-        cudaGraphExec_t ge = nullptr;
+        // capture one wave, replay it for every wave of the plan; the graph and its executable are
+        // destroyed on every exit (replays already enqueued still run)
+        struct GraphHold {
+            cudaGraph_t g = nullptr;
+            cudaGraphExec_t ge = nullptr;
+            ~GraphHold() {
+                if (ge) cudaGraphExecDestroy(ge);
+                if (g) cudaGraphDestroy(g);
+            }
+        } gh;
         CRT_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
         const uint64_t before = ctx->launches;
         try {
             launch_wave();
         } catch (...) {
-            cudaStreamEndCapture(st, &g);
-            if (g) cudaGraphDestroy(g);
+            cudaStreamEndCapture(st, &gh.g);
             throw;
         }
-        CRT_CUDA(cudaStreamEndCapture(st, &g));
+        CRT_CUDA(cudaStreamEndCapture(st, &gh.g));
         const uint64_t per_wave = ctx->launches - before;
-        CRT_CUDA(cudaGraphInstantiate(&ge, g, 0));
-        cudaGraphDestroy(g);
+        CRT_CUDA(cudaGraphInstantiate(&gh.ge, gh.g, 0));
         ctx->launches = before;
         for (size_t w = 0; w < plan.size(); ++w) {
-            CRT_CUDA(cudaGraphLaunch(ge, st));
+            CRT_CUDA(cudaGraphLaunch(gh.ge, st));
             ctx->launches += per_wave;
         }
-        cudaGraphExecDestroy(ge);
         waves_run = plan.size();
     } else if (n_srp) {
         // waves with SRP items: the SRP stages of the wave's range follow its primary trace
