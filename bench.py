@@ -280,6 +280,13 @@ def cpu_measure(ents, cfg, budget_s):
                                         f"of {len(lid_rays)} LiDAR beams); BVH built once (untimed)")
 
 
+def step_workload(args):
+    """Name of the asteroid step at the given sizes (both arms report the same name)."""
+    faces = "2M" if args.faces == 2_000_000 else str(args.faces)
+    return (f"asteroid-{faces}: render {args.res}^2 1 spp (primary + sun shadow) + LiDAR {args.lidar}^2 "
+            "(range + triangle id)")
+
+
 # ------------------------------------------------------------------ reference arm
 def reference_arm(args):
     rank, world, _ = dist_info()
@@ -298,7 +305,8 @@ def reference_arm(args):
     line = {"impl": "reference", "metric": METRIC, "value": round(mr, 3), "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "asteroid-2M render 2048^2 1spp + sun shadow, LiDAR 1024^2", "triangles": args.faces},
+            "config": {"workload": step_workload(args), "path": "CPU oracle port, all host threads, bounded sample",
+                       "triangles": args.faces},
             "cpu_baseline": {"value": round(mr, 3), "unit": UNIT, "cores": det["cores"], "kind": "port",
                              "sample": det["sample"]},
             "e2e": {"value": round(mr, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -450,8 +458,7 @@ def gpu_arm(args):
         line = {"metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-                "config": {"workload": "asteroid-2M: render 2048^2 1 spp (primary + sun shadow) + LiDAR 1024^2 "
-                                       "(range + triangle id), per-call GPU path, resident BVH",
+                "config": {"workload": step_workload(args), "path": "per-call GPU, resident BVH",
                            "triangles": st["n_tris"], "wide_nodes": st["n_nodes"], "bvh_depth": st["depth"],
                            "bvh_build_ms": round(st["build_ms"], 2), "rays_per_step": rays_step,
                            "l2": "256 MiB buffer written between steps (outside the timed events)",
