@@ -125,3 +125,39 @@ def test_srp_request_packing():
     np.testing.assert_array_equal(quats, np.eye(4)[:3])
     # the request struct the C ABI reads: base request, then the SRP fields
     assert ctypes.sizeof(lib.ServerRequest) == ctypes.sizeof(lib.Request) + 5 * 8
+
+
+def test_spice_pose_helpers_call_spice_as_the_reference(monkeypatch):
+    """spice_position / spice_rotation / spice_pose pass (name, et, ref, abcorr, origin) to spkpos and
+    (ref, frame, et) to pxform (crt/rigid_body.py:191, 206, 229-230 of the reference); spiceypy itself
+    is replaced by a recording fake (it is not installed)."""
+    import sys
+    import types
+    R = scenes.quaternion_to_matrix(scenes.random_quaternions(1, 11)[0])
+    calls = []
+    fake = types.ModuleType("spiceypy")
+
+    def spkpos(targ, et, ref, abcorr, obs):
+        calls.append(("spkpos", targ, et, ref, abcorr, obs))
+        return np.array([1.0, -2.0, 3.5]), 0.25
+
+    def pxform(frm, to, et):
+        calls.append(("pxform", frm, to, et))
+        return R
+
+    fake.spkpos, fake.pxform = spkpos, pxform
+    monkeypatch.setitem(sys.modules, "spiceypy", fake)
+    from crt.rigid_body import RigidBody
+    b = RigidBody(name="EROS", frame="IAU_EROS", origin="SUN", ref="ECLIPJ2000", abcorr="LT+S")
+    b._cpp = FakeCpp()
+    b.spice_pose(12.5)
+    assert calls == [("spkpos", "EROS", 12.5, "ECLIPJ2000", "LT+S", "SUN"),
+                     ("pxform", "ECLIPJ2000", "IAU_EROS", 12.5)]
+    np.testing.assert_array_equal(b.position, [1.0, -2.0, 3.5])
+    np.testing.assert_array_equal(b.rotation, R)
+    assert b._cpp.calls[-1][0] == "set_pose"
+    calls.clear()
+    b.spice_position(1.0)
+    b.spice_rotation(2.0)
+    assert calls == [("spkpos", "EROS", 1.0, "ECLIPJ2000", "LT+S", "SUN"), ("pxform", "ECLIPJ2000", "IAU_EROS", 2.0)]
+    assert [c[0] for c in b._cpp.calls[-2:]] == ["set_position", "set_rotation"]
