@@ -161,3 +161,38 @@ def test_spice_pose_helpers_call_spice_as_the_reference(monkeypatch):
     b.spice_rotation(2.0)
     assert calls == [("spkpos", "EROS", 1.0, "ECLIPJ2000", "LT+S", "SUN"), ("pxform", "ECLIPJ2000", "IAU_EROS", 2.0)]
     assert [c[0] for c in b._cpp.calls[-2:]] == ["set_position", "set_rotation"]
+
+
+def test_lidar_batch_spice_pose(monkeypatch):
+    """batch_spice_pose: one vectorised spkpos over the epochs and one pxform per epoch
+    (crt/lidars.py:32-44 of the reference), then the batch pose arrays the extension receives."""
+    import sys
+    import types
+    from crt.lidars import SimpleLidar
+    ets = np.array([0.0, 60.0, 120.0])
+    pos = np.array([[1.0, 2.0, 3.0], [4.0, 5.0, 6.0], [7.0, 8.0, 9.5]])
+    rots = [scenes.quaternion_to_matrix(q) for q in scenes.random_quaternions(3, 12)]
+    calls = []
+    fake = types.ModuleType("spiceypy")
+
+    def spkpos(targ, et, ref, abcorr, obs):
+        calls.append(("spkpos", targ, tuple(np.atleast_1d(et)), ref, abcorr, obs))
+        return pos, np.zeros(3)
+
+    def pxform(frm, to, et):
+        calls.append(("pxform", frm, to, float(et)))
+        return rots[int(et // 60)]
+
+    fake.spkpos, fake.pxform = spkpos, pxform
+    monkeypatch.setitem(sys.modules, "spiceypy", fake)
+    lid = SimpleLidar(name="SC", frame="SC_LIDAR", origin="EROS", ref="J2000", abcorr="NONE")
+    lid._cpp = FakeCpp()
+    lid.batch_spice_pose(ets)
+    assert calls[0] == ("spkpos", "SC", (0.0, 60.0, 120.0), "J2000", "NONE", "EROS")
+    assert calls[1:] == [("pxform", "J2000", "SC_LIDAR", e) for e in (0.0, 60.0, 120.0)]
+    np.testing.assert_array_equal(lid.batch_positions, pos)
+    name, args, _ = lid._cpp.calls[-1]
+    assert name == "batch_set_pose" and args[2] == 3 and args[1].shape == (3, 3, 100000)
+    for k in range(3):
+        np.testing.assert_array_equal(args[1][:, :, k], rots[k])
+    assert not args[1][:, :, 3:].any()
