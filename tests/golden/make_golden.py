@@ -17,6 +17,11 @@ scene inputs together with the reference outputs:
   asteroid.npz  8000-triangle asteroid (smooth, rotated, scaled, translated) plus a flat box:
                 BodyFixedGroup passes at 64x64, per-ray closest hits (primitive, t, u, v) and
                 any-hit flags for seeded rays, and batch_simulate_lidar ranges for 512 poses.
+  edges.npz     Cornell box: closest / any hits of edge-case rays (signed zeros, vertices and
+                edges, rays in a triangle's plane, tiny and huge directions, far origins,
+                inclusive and empty t ranges).
+
+`python tests/golden/make_golden.py edges` writes only the named fixtures.
 
 Nothing at test time reads the reference: the tests only read these .npz files.
 """
@@ -265,16 +270,97 @@ def make_asteroid(R, D, tmp):
     return out
 
 
+def edge_rays(ents):
+    """Rays at the corners of the traversal and triangle-test rules (Cornell box, FP64):
+    axis-aligned rays with +0.0 / -0.0 in their zero components; rays aimed exactly at triangle
+    vertices and edge midpoints (non-unit directions); rays leaving a surface point along, into and
+    out of its plane; direction components far below and far above 1; origins 1e6 away."""
+    rays = []
+
+    def add(o, d, tmin=0.0, tmax=np.finfo(np.float64).max):
+        rays.append([o[0], o[1], o[2], d[0], d[1], d[2], tmin, tmax])
+
+    for o in ((0.3, 0.7, 0.8), (0.05, 0.95, 0.9), (0.7, 0.45, 0.2)):
+        for k in range(3):
+            for sgn in (1.0, -1.0):
+                for z0 in (0.0, -0.0):
+                    for z1 in (0.0, -0.0):
+                        d = [0.0, 0.0, 0.0]
+                        d[k] = sgn
+                        d[(k + 1) % 3], d[(k + 2) % 3] = z0, z1
+                        add(o, d)
+    targets = []
+    for e in ents:
+        v = np.asarray(e.mesh.vertices, dtype=np.float64)
+        for f in np.asarray(e.mesh.faces):
+            for i in range(3):
+                a, b = v[f[i]], v[f[(i + 1) % 3]]
+                targets.append(a)
+                targets.append(0.5 * (a + b))
+    targets = np.unique(np.round(np.array(targets), 12), axis=0)
+    for o in (np.array([0.5, 0.5, 0.9]), np.array([0.5, 0.5, 2.4])):
+        for t in targets:
+            if np.abs(t - o).max() > 0:
+                add(o, t - o)
+    rng = np.random.Generator(np.random.PCG64(77))
+    for _ in range(8):
+        x, z = rng.uniform(0.02, 0.4, size=2)
+        o = (x, 0.0, z)                          # on the floor (y = 0), away from the boxes
+        for d in ((0.0, 1.0, 0.0), (0.0, -1.0, 0.0), (1.0, 0.0, 0.0), (-0.6, 0.0, 0.8), (0.3, 1e-18, 0.4)):
+            add(o, d)
+        o = (x + 0.3, z + 0.3, 0.0)              # on the back wall (z = 0)
+        for d in ((0.0, 0.0, 1.0), (0.0, 0.0, -1.0), (0.0, 1.0, 0.0), (0.7, -0.7, 0.0)):
+            add(o, d)
+    for o in ((0.5, 0.5, 0.5), (0.2, 0.3, 0.6)):
+        for d in ((1e-20, 1.0, -1e-20), (1e-300, -1e-300, -1.0), (3e-17, 2e-16, 1.0), (1e-6, 2e-6, -3e-6),
+                  (1e6, -2e6, 3e6), (1e-150, 1e-150, -1e-150), (-1e-170, 2e-170, 0.0)):
+            add(o, d)
+    for _ in range(24):
+        dirv = rng.normal(size=3)
+        o = 1e6 * dirv / np.linalg.norm(dirv)
+        add(o, rng.uniform(0.1, 0.9, size=3) - o)
+    return np.array(rays, dtype=np.float64)
+
+
+def make_edges(R, D, tmp):
+    ents, _, _ = scenes.cornell()
+    paths = write_objs(ents, tmp)
+    out = entity_arrays(ents)
+    h = driver_scene(D, ents, paths)
+    base = edge_rays(ents)
+    # inclusive t bounds: for rays that hit, tmax = t and tmin = t (both still hit), tmax one ulp
+    # below t, and tmin above tmax (never hits)
+    prim, t, _, _ = driver_closest(D, h, base)
+    hit = np.nonzero(prim >= 0)[0][::5]
+    extra = []
+    for i in hit:
+        r = base[i].copy()
+        r[7] = t[i]
+        extra.append(r.copy())
+        r[6], r[7] = t[i], np.finfo(np.float64).max
+        extra.append(r.copy())
+        r[6], r[7] = 0.0, np.nextafter(t[i], 0.0)
+        extra.append(r.copy())
+        r[6], r[7] = 0.5 * t[i] + 1e-9, 0.5 * t[i]
+        extra.append(r.copy())
+    rays = np.concatenate([base, np.array(extra)]) if extra else base
+    out["rays"] = rays
+    out["closest_prim"], out["closest_t"], out["closest_u"], out["closest_v"] = driver_closest(D, h, rays)
+    out["any_occluded"] = driver_any(D, h, rays)
+    return out
+
+
 def main():
+    """Writes every fixture, or only those named on the command line (cornell, asteroid, edges)."""
+    which = sys.argv[1:] or ["cornell", "asteroid", "edges"]
+    makers = {"cornell": make_cornell, "asteroid": make_asteroid, "edges": make_edges}
     R = load_ref_module()
     D = load_driver()
     with tempfile.TemporaryDirectory() as tmp:
-        c = make_cornell(R, D, tmp)
-        np.savez_compressed(os.path.join(HERE, "cornell.npz"), **c)
-        a = make_asteroid(R, D, tmp)
-        np.savez_compressed(os.path.join(HERE, "asteroid.npz"), **a)
-    for f in ("cornell.npz", "asteroid.npz"):
-        print(f, os.path.getsize(os.path.join(HERE, f)))
+        for name in which:
+            np.savez_compressed(os.path.join(HERE, name + ".npz"), **makers[name](R, D, tmp))
+    for name in which:
+        print(name + ".npz", os.path.getsize(os.path.join(HERE, name + ".npz")))
 
 
 if __name__ == "__main__":

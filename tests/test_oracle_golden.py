@@ -128,3 +128,36 @@ def test_philox_known_answer():
     np.testing.assert_array_equal(
         oracle.philox(0x243f6a88, 0x85a308d3, 0x13198a2e, 0x03707344, 0xa4093822, 0x299f31d0),
         np.array([0xd16cfe09, 0x94fdcceb, 0x5001e420, 0x24126ea1], dtype=np.uint32))
+
+
+@pytest.fixture(scope="module")
+def edges():
+    d = load_golden("edges")
+    return d, oracle.Scene(entities_from(d))
+
+
+def test_edge_case_rays(edges):
+    """Edge-case rays on the Cornell box (axis-aligned with signed zeros, aimed at vertices and edge
+    midpoints, in a triangle's plane, tiny / huge direction components, origins 1e6 away, t ranges
+    closed at the hit distance or empty): closest hits bit for bit outside exact ties on shared
+    edges and vertices, where both sides report the same distance; any-hit flags identical."""
+    d, s = edges
+    rays = d["rays"]
+    prim, t, u, v = s.trace_closest(rays)
+    ref_p, ref_t = d["closest_prim"], d["closest_t"]
+    mism = prim != ref_p
+    assert mism.mean() < 0.05
+    assert excused_id_mismatch(s.tris(), rays, prim, t, ref_p, ref_t)[mism].all()
+    assert ((prim >= 0) == (ref_p >= 0)).all()
+    both = prim >= 0
+    np.testing.assert_allclose(t[both & mism], ref_t[both & mism], rtol=1e-12)
+    same = ~mism & both
+    np.testing.assert_array_equal(t[same], ref_t[same])
+    np.testing.assert_array_equal(u[same], d["closest_u"][same])
+    np.testing.assert_array_equal(v[same], d["closest_v"][same])
+    assert (s.trace_any(rays) == d["any_occluded"]).all()
+    # the fixture exercises what it claims: hits and misses, closed and empty t ranges
+    assert 0.5 < both.mean() < 0.95
+    closed = (rays[:, 7] == ref_t) & (rays[:, 6] <= rays[:, 7])
+    assert closed.sum() >= 50 and (ref_p[closed] >= 0).all()
+    assert (ref_p[rays[:, 6] > rays[:, 7]] < 0).all()
