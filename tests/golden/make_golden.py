@@ -19,7 +19,8 @@ scene inputs together with the reference outputs:
                 any-hit flags for seeded rays, and batch_simulate_lidar ranges for 512 poses.
   edges.npz     Cornell box: closest / any hits of edge-case rays (signed zeros, vertices and
                 edges, rays in a triangle's plane, tiny and huge directions, far origins,
-                inclusive and empty t ranges).
+                inclusive and empty t ranges), and BodyFixedGroup passes through two non-square
+                cameras (one z_positive).
 
 `python tests/golden/make_golden.py edges` writes only the named fixtures.
 
@@ -347,6 +348,20 @@ def make_edges(R, D, tmp):
     out["rays"] = rays
     out["closest_prim"], out["closest_t"], out["closest_u"], out["closest_v"] = driver_closest(D, h, rays)
     out["any_occluded"] = driver_any(D, h, rays)
+    # BodyFixedGroup passes through non-square cameras: z_positive boresight (+z of the camera frame,
+    # turned into the box by diag(1, -1, -1)) with non-square pixels, and a tilted -z camera
+    g = body_fixed_group(R, ents, paths)
+    cams = {"zcam": dict(focal_length=0.02, resolution=[40.0, 24.0], sensor_size=[0.03, 0.02], z_positive=True,
+                         position=np.array([0.5, 0.5, 2.4]), rotation=np.diag([1.0, -1.0, -1.0])),
+            "wcam": dict(focal_length=0.03, resolution=[36.0, 20.0], sensor_size=[0.036, 0.024], z_positive=False,
+                         position=np.array([0.9, 0.8, 2.0]),
+                         rotation=scenes.look_at(np.array([0.9, 0.8, 2.0]), (0.5, 0.4, 0.3)))}
+    for name, cam in cams.items():
+        out.update(camera_arrays(cam, name))
+        c = ref_camera(R, cam)
+        out[name + "_xyz"] = g.intersection_pass(c)
+        out[name + "_ids"] = g.instance_pass(c)
+        out[name + "_normals"] = g.normal_pass(c)
     return out
 
 

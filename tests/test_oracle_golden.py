@@ -161,3 +161,18 @@ def test_edge_case_rays(edges):
     closed = (rays[:, 7] == ref_t) & (rays[:, 6] <= rays[:, 7])
     assert closed.sum() >= 50 and (ref_p[closed] >= 0).all()
     assert (ref_p[rays[:, 6] > rays[:, 7]] < 0).all()
+
+
+@pytest.mark.parametrize("name", ["zcam", "wcam"])
+def test_non_square_camera_passes(edges, name):
+    """Intersection / instance / normal passes through non-square cameras (W != H, non-square
+    pixels; one with the z_positive boresight) equal the reference's BodyFixedGroup passes."""
+    d, s = edges
+    cam = camera_from(d, name)
+    xyz, ids, nrm, _ = s.passes(cam)
+    W, H = int(cam["resolution"][0]), int(cam["resolution"][1])
+    assert ids.shape == (H, W) and W != H
+    np.testing.assert_array_equal(ids, d[name + "_ids"])
+    np.testing.assert_allclose(xyz, d[name + "_xyz"], rtol=0, atol=1e-12)
+    np.testing.assert_allclose(nrm, d[name + "_normals"], rtol=0, atol=1e-12)
+    assert 0.2 < (ids > 0).mean() < 1.0
