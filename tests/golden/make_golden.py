@@ -19,8 +19,9 @@ scene inputs together with the reference outputs:
                 any-hit flags for seeded rays, and batch_simulate_lidar ranges for 512 poses.
   edges.npz     Cornell box: closest / any hits of edge-case rays (signed zeros, vertices and
                 edges, rays in a triangle's plane, tiny and huge directions, far origins,
-                inclusive and empty t ranges), and BodyFixedGroup passes through two non-square
-                cameras (one z_positive).
+                inclusive and empty t ranges), BodyFixedGroup passes through two non-square
+                cameras (one z_positive), and a deterministic point-light render of a
+                smooth-shaded asteroid beside a flat box.
 
 `python tests/golden/make_golden.py edges` writes only the named fixtures.
 
@@ -362,6 +363,33 @@ def make_edges(R, D, tmp):
         out[name + "_xyz"] = g.intersection_pass(c)
         out[name + "_ids"] = g.instance_pass(c)
         out[name + "_normals"] = g.normal_pass(c)
+    # deterministic render of a smooth-shaded body (1 spp at integer pixel coordinates, 1 bounce,
+    # point light: no random draws): pins the interpolated shading normal and the unclamped
+    # Lambert term on a rotated, scaled and translated entity, through a non-square camera
+    c, s_ = 0.6, 0.8
+    rot = np.array([[1.0, 0.0, 0.0], [0.0, c, -s_], [0.0, s_, c]]) @ np.array([[c, 0.0, s_], [0.0, 1.0, 0.0],
+                                                                               [-s_, 0.0, c]])
+    sents = [scenes.EntitySpec("smooth", scenes.asteroid(3000, seed=9), (0.3, 0.25, 0.2), smooth=True, scale=0.9,
+                               position=np.array([40.0, -30.0, 20.0]), rotation=rot),
+             scenes.EntitySpec("flat", scenes.box_mesh((0.0, 0.0, 0.0), (400.0, 300.0, 200.0), 1.0, 0.0), (0.5, 0.5, 0.5),
+                               position=np.array([1300.0, 0.0, 0.0]))]
+    spaths = write_objs(sents, tmp)
+    out.update(entity_arrays(sents, "s"))
+    scam = scenes.fov_camera(0.25, (48, 30), (4000.0, 2500.0, 2000.0), (300.0, 0.0, 0.0))
+    out.update(camera_arrays(scam, "scam"))
+    sl = [dict(type="point", intensity=4.0e7, position=np.array([3000.0, 5000.0, 4000.0]))]
+    Ls = light_array(sl)
+    hs = driver_scene(D, sents, spaths)
+    W, H = int(scam["resolution"][0]), int(scam["resolution"][1])
+    rad = np.empty((H, W, 3), np.float32)
+    res_a = np.array(scam["resolution"], dtype=np.float64)
+    sen_a = np.array(scam["sensor_size"], dtype=np.float64)
+    pos_a = np.asarray(scam["position"], dtype=np.float64)
+    rot_a = np.ascontiguousarray(scam["rotation"], dtype=np.float64)
+    D.ref_render(hs, float(scam["focal_length"]), res_a.ctypes.data, sen_a.ctypes.data, int(scam["z_positive"]),
+                 pos_a.ctypes.data, rot_a.ctypes.data, 1, Ls.ctypes.data, 1, 1, 0.0, 1, rad.ctypes.data, None)
+    out["s_lights"] = Ls
+    out["s_radiance"] = rad
     return out
 
 

@@ -176,3 +176,17 @@ def test_non_square_camera_passes(edges, name):
     np.testing.assert_allclose(xyz, d[name + "_xyz"], rtol=0, atol=1e-12)
     np.testing.assert_allclose(nrm, d[name + "_normals"], rtol=0, atol=1e-12)
     assert 0.2 < (ids > 0).mean() < 1.0
+
+
+def test_smooth_point_light_render_deterministic(edges):
+    """1 spp at integer pixel coordinates, 1 bounce, point light on a smooth-shaded, rotated,
+    scaled and translated asteroid beside a flat box, through a non-square camera: no random
+    draws, so the oracle's radiance equals the reference's (interpolated shading normals and the
+    unclamped Lambert term, negative where the shading normal turns from the light)."""
+    d, _ = edges
+    s = oracle.Scene(entities_from(d, "s"))
+    cam = camera_from(d, "scam")
+    rad, _, taken = s.render(cam, lights_from(d["s_lights"]), 1, 1, 0.0, 1)
+    ref = d["s_radiance"]
+    np.testing.assert_allclose(rad[..., :3], ref, rtol=1e-6, atol=1e-7)
+    assert (taken == 1).all() and (ref > 0).any(-1).sum() > 300 and (ref < 0).any()
