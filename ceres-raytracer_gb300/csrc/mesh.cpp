@@ -10,6 +10,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -31,6 +32,10 @@ void remove_eol(char* p) {
     long i = (long)std::strlen(p) - 1;
     while (i > 0 && std::isspace((unsigned char)p[i])) p[i--] = '\0';
 }
+
+struct FileCloser {
+    void operator()(FILE* f) const { std::fclose(f); }
+};
 
 // obj.hpp:31-55 read_index
 bool read_index(char** ptr, long* out) {
@@ -59,21 +64,21 @@ extern "C" {
 int crt_mesh_load_obj(const char* path, crt_mesh** out) {
     if (!path || !out) return CRT_ERR_INVALID;
     *out = nullptr;
-    FILE* f = std::fopen(path, "r");
+    // the file is closed on every return, also when an allocation fails mid-parse
+    std::unique_ptr<FILE, FileCloser> file(std::fopen(path, "r"));
+    FILE* f = file.get();
     if (!f) return CRT_ERR_IO;
     crt_mesh* m = new (std::nothrow) crt_mesh();
-    if (!m) {
-        std::fclose(f);
-        return CRT_ERR_OOM;
-    }
+    if (!m) return CRT_ERR_OOM;
     std::vector<float> vx;                  // vertices, 3 per vertex (float32 as parsed)
     std::vector<double> acc;                // accumulated normals, 3 per vertex
     std::vector<long> tri_idx;              // 3 per triangle
     char line[1024];
     try {
         while (std::fgets(line, sizeof(line), f)) {
-            // a line longer than the buffer continues in the next read, as istream::getline would
-            // stop: skip the remainder of over-long lines
+            // over-long line: its first 1023 characters are parsed and the rest is skipped.  (The
+            // reference's istream::getline sets failbit there and its loop ends, silently dropping
+            // the rest of the file; this loader reads on.)
             size_t len = std::strlen(line);
             if (len == sizeof(line) - 1 && line[len - 1] != '\n') {
                 int c;
@@ -101,8 +106,7 @@ int crt_mesh_load_obj(const char* path, crt_mesh** out) {
                 for (size_t i = 0; read_index(&q, &index); ++i) {
                     const long nv = (long)(vx.size() / 3);
                     long j = index < 0 ? nv + index : index - 1;
-                    if (j < 0 || j >= nv) {
-                        std::fclose(f);
+                    if (j < 0 || j >= nv) {   // index 0, past the last vertex, or before the first
                         delete m;
                         return CRT_ERR_IO;
                     }
@@ -126,7 +130,7 @@ int crt_mesh_load_obj(const char* path, crt_mesh** out) {
                 }
             }
         }
-        std::fclose(f);
+        file.reset();
         const size_t nt = tri_idx.size() / 3;
         m->xyz.resize(nt * 9);
         m->normals.resize(nt * 9);

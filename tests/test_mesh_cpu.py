@@ -70,3 +70,30 @@ def test_obj_missing_file_and_no_faces(tmp_path):
     p.write_text("v 0 0 0\nv 1 0 0\n# no faces\n")
     rc, xyz, _ = load(p)
     assert rc == 0 and xyz.shape == (0, 9)
+
+
+def test_obj_index_out_of_range(tmp_path):
+    """A face index of 0, past the last vertex read so far, or a negative index reaching before the
+    first vertex is refused (CRT_ERR_IO, the file is malformed) and no mesh is returned; the same
+    file without that face loads."""
+    head = "v 0 0 0\nv 1 0 0\nv 0 1 0\n"
+    for bad in ("f 0 1 2", "f 1 2 4", "f -4 -2 -1", "f 1 2 3\nf 1 2 9"):
+        p = tmp_path / "bad.obj"
+        p.write_text(head + bad + "\n")
+        rc, xyz, _ = load(p)
+        assert rc == -5 and xyz is None, bad
+    p = tmp_path / "ok.obj"
+    p.write_text(head + "f -3 -2 -1\n")
+    rc, xyz, _ = load(p)
+    assert rc == 0 and xyz.shape == (1, 9)
+    np.testing.assert_array_equal(xyz[0], [0, 0, 0, 1, 0, 0, 0, 1, 0])
+
+
+def test_obj_long_lines_and_crlf(tmp_path):
+    """A line longer than the 1024-byte read buffer is cut there and parsing continues with the next
+    line (a deliberate difference: the reference's getline fails on it and stops reading the file,
+    which would drop the face below), and CR LF line ends parse as LF."""
+    p = tmp_path / "m.obj"
+    p.write_text("v 0 0 0\r\nv 1 0 0\r\nv 0 1 0\r\n# " + "x" * 3000 + "\r\nf 1 2 3\r\n", newline="")
+    rc, xyz, _ = load(p)
+    assert rc == 0 and xyz.shape == (1, 9)
