@@ -306,7 +306,7 @@ struct SceneHandle {
     }
 };
 
-// sah: -1 the context's setting, 0 radix tree, 1 binned SAH (for this build only)
+// sah: -1 the context's setting, 0 radix tree, 1 binned SAH (for this scene's build only)
 std::unique_ptr<SceneHandle> build_scene(const std::vector<crt_entity_desc>& descs, int sah = -1) {
     auto h = std::make_unique<SceneHandle>();
     py::gil_scoped_release nogil;

@@ -1,7 +1,7 @@
 /* CPU oracle for the CRT ray-query path.  TEST INFRASTRUCTURE ONLY.
  *
  * A plain-C, FP64 restatement of the reference (ceres-navigation/ceres-raytracer v0.6a4)
- * algorithms on the ray-query path.  It is the checker for the CUDA library: only the test
+ * algorithms on the ray-query path.  The CUDA library is tested against it: only the test
  * suite, the smoke check and the CPU-baseline leg of the benchmark load it.  Nothing in the
  * product links or calls it.
  *

@@ -1,6 +1,6 @@
 """Generate the golden fixtures in tests/golden/ from the reference implementation itself.
 
-Run in a container that has the reference sources (default /root/reference) after
+Run where the reference sources are available (default /root/reference) after
 `python oracle/build_ref.py`:
 
     python tests/golden/make_golden.py
