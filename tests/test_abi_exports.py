@@ -72,7 +72,6 @@ def test_struct_layouts_match_header(tmp_path):
     compiler gives the structs of include/crt_gpu.h (a mismatch would corrupt every request)."""
     import shutil
     import subprocess
-    import numpy as np  # noqa: F401
     cc = shutil.which("gcc") or shutil.which("cc")
     if cc is None:
         pytest.skip("no C compiler")
