@@ -196,3 +196,38 @@ def test_lidar_batch_spice_pose(monkeypatch):
     for k in range(3):
         np.testing.assert_array_equal(args[1][:, :, k], rots[k])
     assert not args[1][:, :, 3:].any()
+
+
+def test_dynamic_passes_return_images(monkeypatch):
+    """crt.rendering's passes hand the entities' C++ objects to _crt and, with return_image, add the
+    reference's images (crt/rendering.py:54-144): 255 |n| for normals, the distance to the origin
+    shifted to 0 and scaled to 255 for intersections, one colour per instance id."""
+    import types
+    import crt.rendering as rendering
+    rng = np.random.Generator(np.random.PCG64(13))
+    pts = rng.normal(size=(6, 5, 3))
+    nrm = rng.normal(size=(6, 5, 3))
+    ids = rng.integers(0, 4, size=(6, 5)).astype(np.uint32)
+    seen = []
+
+    def rec(out):
+        def f(cam, ents):
+            seen.append((cam, list(ents)))
+            return out
+        return f
+
+    fake = types.SimpleNamespace(normal_pass=rec(nrm), intersection_pass=rec(pts), instance_pass=rec(ids))
+    monkeypatch.setattr(rendering, "_crt", fake)
+    cam = types.SimpleNamespace(_cpp="camera")
+    ents = [types.SimpleNamespace(_cpp="e0"), types.SimpleNamespace(_cpp="e1")]
+    n, img = rendering.normal_pass(cam, ents, return_image=True)
+    assert n is nrm and np.array_equal(img, 255 * np.abs(nrm))
+    p, img = rendering.intersection_pass(cam, ents, return_image=True)
+    dist = np.sqrt(pts[:, :, 0] ** 2 + pts[:, :, 1] ** 2 + pts[:, :, 2] ** 2)
+    np.testing.assert_allclose(img, 255 * (dist - dist.min()) / (dist - dist.min()).max(), rtol=1e-15)
+    i, img = rendering.instance_pass(cam, ents, return_image=True)
+    assert img.shape == (6, 5, 3)
+    for k in np.unique(ids):
+        assert len(np.unique(img[ids == k], axis=0)) == 1
+    assert all(s == ("camera", ["e0", "e1"]) for s in seen) and len(seen) == 3
+    assert rendering.normal_pass(cam, ents) is nrm
