@@ -20,8 +20,8 @@ scene inputs together with the reference outputs:
   edges.npz     Cornell box: closest / any hits of edge-case rays (signed zeros, vertices and
                 edges, rays in a triangle's plane, tiny and huge directions, far origins,
                 inclusive and empty t ranges), BodyFixedGroup passes through two non-square
-                cameras (one z_positive), and a deterministic point-light render of a
-                smooth-shaded asteroid beside a flat box.
+                cameras (one z_positive), batch LiDAR with the z_positive boresight, and a
+                deterministic point-light render of a smooth-shaded asteroid beside a flat box.
 
 `python tests/golden/make_golden.py edges` writes only the named fixtures.
 
@@ -363,6 +363,21 @@ def make_edges(R, D, tmp):
         out[name + "_xyz"] = g.intersection_pass(c)
         out[name + "_ids"] = g.instance_pass(c)
         out[name + "_normals"] = g.normal_pass(c)
+    # batch LiDAR with the z_positive boresight (+z of the sensor frame, simple_lidar.hpp:42-64)
+    rng = np.random.Generator(np.random.PCG64(78))
+    npose = 64
+    lp = np.where(np.arange(npose)[:, None] % 2 == 0, rng.uniform(0.1, 0.9, size=(npose, 3)),
+                  rng.uniform(-2.0, 3.0, size=(npose, 3)))
+    rots = np.zeros((3, 3, 100000))
+    for k in range(npose):
+        aim = rng.uniform(0.2, 0.8, size=3)
+        # look_at points -z at the target; flip to put +z there
+        rots[:, :, k] = np.diag([1.0, -1.0, -1.0]) @ scenes.look_at(lp[k], aim, up=(0.0, 0.3, 1.0))
+    lid = R.SimpleLidar(True)
+    lid.batch_set_pose(np.ascontiguousarray(lp), rots, npose)
+    out["zlidar_pos"] = lp
+    out["zlidar_rot"] = np.ascontiguousarray(np.moveaxis(rots[:, :, :npose], 2, 0))
+    out["zlidar_range"] = g.batch_simulate_lidar(lid, 1.0)[0]
     # deterministic render of a smooth-shaded body (1 spp at integer pixel coordinates, 1 bounce,
     # point light: no random draws): pins the interpolated shading normal and the unclamped
     # Lambert term on a rotated, scaled and translated entity, through a non-square camera

@@ -190,3 +190,14 @@ def test_smooth_point_light_render_deterministic(edges):
     ref = d["s_radiance"]
     np.testing.assert_allclose(rad[..., :3], ref, rtol=1e-6, atol=1e-7)
     assert (taken == 1).all() and (ref > 0).any(-1).sum() > 300 and (ref < 0).any()
+
+
+def test_z_positive_lidar_batch(edges):
+    """Batch LiDAR with the z_positive boresight (64 poses inside and around the Cornell box) equals
+    the reference's batch_simulate_lidar; the -z boresight would give other ranges."""
+    d, s = edges
+    pos, rot = d["zlidar_pos"], d["zlidar_rot"].reshape(-1, 9)
+    rng, prim = s.lidar_batch(pos, rot, z_positive=True)
+    np.testing.assert_array_equal(rng, d["zlidar_range"])
+    assert ((rng == 0) == (prim < 0)).all() and (rng > 0).mean() > 0.8
+    assert (s.lidar_batch(pos, rot, z_positive=False)[0] != rng).mean() > 0.5
