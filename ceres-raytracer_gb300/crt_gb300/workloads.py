@@ -38,6 +38,47 @@ def asteroid_config(res=2048, lidar_n=1024, seed=0):
     return dict(camera=camera, lights=lights, lidar=lidar, spp=1, bounces=1)
 
 
+def lidar_grid_rays(lid):
+    """FP64 beam rays [nx * ny, 8] (origin, direction, tmin 0, tmax max) of a LiDAR beam grid in the
+    order crt_lidar_grid reports them (row-major [ny][nx]): beam (i, j) along
+    R^T normalize(tan_x[i], tan_y[j], -1) (+1 with z_positive), tan of angles uniform over each half
+    angle."""
+    nx, ny = int(lid["nx"]), int(lid["ny"])
+    tx = np.tan(-lid["half_x"] + (np.arange(nx) + 0.5) * 2 * lid["half_x"] / nx)
+    ty = np.tan(-lid["half_y"] + (np.arange(ny) + 0.5) * 2 * lid["half_y"] / ny)
+    zs = 1.0 if lid.get("z_positive", False) else -1.0
+    s = np.stack(np.broadcast_arrays(tx[None, :], ty[:, None], zs * np.ones((ny, nx))), -1).reshape(-1, 3)
+    s /= np.linalg.norm(s, axis=1)[:, None]
+    rays = np.zeros((nx * ny, 8))
+    rays[:, 0:3] = np.asarray(lid["position"], dtype=np.float64)
+    rays[:, 3:6] = s @ np.asarray(lid["rotation"], dtype=np.float64)
+    rays[:, 7] = np.finfo(np.float64).max
+    return rays
+
+
+def camera_rays(cam):
+    """FP64 camera rays [W * H, 8] at integer pixel coordinates, row-major, as SimpleCamera::pixel_to_ray
+    (cameras/simple_camera.hpp:61-81): direction R^T normalize((u - W/2) / sx, (H/2 - v) / sy, -+f)
+    with sx = W / sensor_w, sy = H / sensor_h; origin the camera position."""
+    W, H = int(cam["resolution"][0]), int(cam["resolution"][1])
+    sx = cam["resolution"][0] / cam["sensor_size"][0]
+    sy = cam["resolution"][1] / cam["sensor_size"][1]
+    f = cam["focal_length"] if cam.get("z_positive", False) else -cam["focal_length"]
+    u = np.arange(W, dtype=np.float64)
+    v = np.arange(H, dtype=np.float64)
+    d = np.empty((H, W, 3))
+    d[..., 0] = ((u - cam["resolution"][0] / 2.0) / sx)[None, :]
+    d[..., 1] = ((cam["resolution"][1] / 2.0 - v) / sy)[:, None]
+    d[..., 2] = f
+    d = d.reshape(-1, 3)
+    d /= np.linalg.norm(d, axis=1)[:, None]
+    rays = np.zeros((W * H, 8))
+    rays[:, 0:3] = np.asarray(cam["position"], dtype=np.float64)
+    rays[:, 3:6] = d @ np.asarray(cam["rotation"], dtype=np.float64).reshape(3, 3)
+    rays[:, 7] = np.finfo(np.float64).max
+    return rays
+
+
 def batched_config(seed=1, n_render=32, n_lidar=32):
     rng = np.random.Generator(np.random.PCG64(seed))
     sun = scenes.unit_vector(3000 + seed)

@@ -13,13 +13,11 @@
 // box centre, 2 R_b + 1 upstream, one ray per cell centre, power flux * cell area.
 //
 // crt_srp runs as a wavefront on the shared persistent trace kernel (per-segment trace launches
-// into per-ray hits, then k_srp_shade; see the section below).  crt_srp_static, which may not
-// allocate, keeps the fused kernel k_srp: each persistent warp takes 16 tiles (8 x 4 rays) of one
-// attitude per grab, lanes accumulate force and torque in FP64, the warp reduces them with
-// shuffles and lane 0 writes the grab's partial sums to a slot indexed by the grab.
-// In both, per-attitude totals are summed by k_srp_reduce in a fixed order (bitwise reproducible);
-// facet powers are summed per facet within a warp (FP32, at most 32 terms) and added with FP64
-// atomics (reproducible up to the order of additions); warps whose rays all missed skip that step.
+// into per-ray hits, then k_srp_shade; see the section below); crt_srp_static runs the same stages
+// with its scratch in a static device array.  Per-attitude totals are summed from per-block partial
+// sums in a fixed order (bitwise reproducible); facet powers are summed per facet within a warp (FP32,
+// at most 32 terms) and added with FP64 atomics (reproducible up to the order of additions); warps
+// whose rays all missed skip that step.
 #include "common.cuh"
 #include "srp.cuh"
 #include "trace.cuh"
@@ -29,161 +27,61 @@
 
 namespace {
 
-constexpr uint32_t CHUNK = 16;   // tiles per work grab (at most)
+// Per-attitude totals from the partial sums of its blocks, in a fixed order: thread t of a 256-thread
+// block adds blocks t, t + 256, t + 512, ... in increasing order, then a shared-memory tree sums the
+// 256 thread totals.  k_srp_reduce does both for whole attitudes; k_srp_fold runs the first step over
+// the blocks of one wave (a part of one attitude) into a running per-thread total and k_srp_tree the
+// second, so an attitude summed wave by wave gets the same additions in the same order.
+constexpr uint32_t SRP_REDUCE_THREADS = 256;
 
-struct SrpArgs {
-    const SrpAtt* att;
-    uint32_t G;
-    uint32_t tiles;          // tiles per attitude
-    uint32_t grabs_per_att;
-    uint32_t chunk;          // tiles per grab
-    uint32_t n_att;
-    float inv_c;
-    float cm[3];
-    uint32_t nb;
-    double* partial;         // n_att * grabs_per_att * 6
-    double* facet;           // n_att * n_tris or null
-    uint32_t n_tris;
-};
-
-template <bool COUNT>
-__global__ void __launch_bounds__(CRT_TRACE_BLOCK) k_srp(SceneView sv, SrpArgs A, uint32_t* __restrict__ queue,
-                                                         uint32_t* __restrict__ err,
-                                                         unsigned long long* __restrict__ counters) {
-    extern __shared__ uint2 sstack[];
-    const int lane = threadIdx.x & 31;
-    const uint32_t tiles_x = (A.G + 7) >> 3;
-    const uint32_t total = A.n_att * A.grabs_per_att;
-    TravStats st{0u, 0u};
-    uint32_t nrays = 0;
-    while (true) {
-        uint32_t g = 0;
-        if (lane == 0) g = atomicAdd(queue, 1u);
-        g = __shfl_sync(0xffffffffu, g, 0);
-        if (g >= total) break;
-        const uint32_t a = g / A.grabs_per_att;
-        const uint32_t t0 = (g % A.grabs_per_att) * A.chunk;
-        const uint32_t t1 = min(t0 + A.chunk, A.tiles);
-        const SrpAtt P = A.att[a];
-        double acc[6] = {0, 0, 0, 0, 0, 0};
-        for (uint32_t tile = t0; tile < t1; ++tile) {
-            const uint32_t px = (tile % tiles_x) * 8u + (lane & 7), py = (tile / tiles_x) * 4u + (lane >> 3);
-            bool alive = px < A.G && py < A.G;
-            TRay r;
-            r.o = f3(P.org[0] + px * P.du[0] + py * P.dv[0], P.org[1] + px * P.du[1] + py * P.dv[1],
-                     P.org[2] + px * P.du[2] + py * P.dv[2]);
-            r.d = f3(P.dir[0], P.dir[1], P.dir[2]);
-            r.tmin = 0.f;
-            r.tmax = 3.402823466e38f;
-            float E = P.E0;
-            for (uint32_t seg = 0; seg <= A.nb; ++seg) {
-                THit h;
-                h.slot = CRT_MISS;
-                if (alive) {
-                    h = traverse<false, COUNT>(sv, r, sstack + threadIdx.x, CRT_TRACE_BLOCK, st, err);
-                    if (COUNT) ++nrays;
-                    if (h.slot == CRT_MISS) alive = false;
-                }
-                __syncwarp();
-                const bool hit = h.slot != CRT_MISS;
-                float absorbed = 0.f;
-                uint32_t key = 0xFFFFFFFFu;
-                float3 n = f3(0.f, 0.f, 0.f), x = f3(0.f, 0.f, 0.f);
-                float rs = 0.f;
-                if (hit) {
-                    const SurfacePoint sp = surface_point(sv, h);
-                    const EntityDev& Ent = sv.entities[sp.entity];
-                    rs = Ent.rho_s;
-                    const float rd = Ent.rho_d;
-                    n = sp.flat_n * -1.0f;                       // outward for counter-clockwise meshes
-                    if (dot3(r.d, n) > 0.f) n = n * -1.0f;       // two-sided: face the incoming ray
-                    const float cs = -dot3(r.d, n);
-                    const float k1 = E * A.inv_c * (1.0f - rs);
-                    const float k2 = E * A.inv_c * (2.0f * rs * cs + (2.0f / 3.0f) * rd);
-                    const float3 dF = r.d * k1 - n * k2;
-                    x = sp.x;
-                    const float3 dT = cross3(x - f3(A.cm[0], A.cm[1], A.cm[2]), dF);
-                    acc[0] += dF.x; acc[1] += dF.y; acc[2] += dF.z;
-                    acc[3] += dT.x; acc[4] += dT.y; acc[5] += dT.z;
-                    absorbed = (1.0f - rs - rd) * E;
-                    key = __ldg(sv.leaf_prim + h.slot);
-                }
-                if (A.facet && __any_sync(0xffffffffu, hit)) {
-                    // warp-aggregated facet power: lanes hitting the same facet add once.  The group
-                    // sum (at most 32 terms) is FP32, the accumulation across groups FP64 atomics.
-                    const uint32_t peers = __match_any_sync(0xffffffffu, key);
-                    float sum = absorbed;
-                    if (__any_sync(0xffffffffu, hit && peers != (1u << lane))) {
-                        sum = 0.f;
-#pragma unroll 8
-                        for (int j = 0; j < 32; ++j) {
-                            const float v = __shfl_sync(0xffffffffu, absorbed, j);
-                            if ((peers >> j) & 1u) sum += v;
-                        }
-                    }
-                    if (hit && lane == __ffs(peers) - 1) atomicAdd(&A.facet[(size_t)a * A.n_tris + key], (double)sum);
-                }
-                if (hit) {
-                    if (rs > 0.f && seg < A.nb) {
-                        const float3 dn = r.d - n * (2.0f * dot3(r.d, n));
-                        const float m = fmaxf(fabsf(x.x), fmaxf(fabsf(x.y), fabsf(x.z)));
-                        int e;
-                        frexpf(m, &e);
-                        const float off = fmaxf(1e-5f, ldexpf(1.0f, e - 24 + 3));
-                        r.o = x + n * off;
-                        r.d = dn;
-                        r.tmin = 0.f;
-                        r.tmax = 3.402823466e38f;
-                        r.skip = h.slot;
-                        E *= rs;
-                    } else {
-                        alive = false;
-                    }
-                }
-                if (!__any_sync(0xffffffffu, alive)) break;
-            }
-        }
-        for (int k = 0; k < 6; ++k)
-            for (int o = 16; o; o >>= 1) acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], o);
-        if (lane == 0)
-            for (int k = 0; k < 6; ++k) A.partial[6ull * g + k] = acc[k];
-    }
-    if (COUNT) {
-        unsigned long long a = nrays, b = st.nodes, c = st.tris;
-        for (int o = 16; o; o >>= 1) {
-            a += __shfl_xor_sync(0xffffffffu, a, o);
-            b += __shfl_xor_sync(0xffffffffu, b, o);
-            c += __shfl_xor_sync(0xffffffffu, c, o);
-        }
-        if (lane == 0) {
-            atomicAdd(counters + 0, a);
-            atomicAdd(counters + 1, b);
-            atomicAdd(counters + 2, c);
-        }
-    }
-}
-
-// one block per attitude, fixed-order tree sum of its partials
-__global__ void k_srp_reduce(const double* __restrict__ partial, uint32_t grabs_per_att, double* __restrict__ force,
-                             double* __restrict__ torque) {
-    __shared__ double sh[256][6];
-    const uint32_t a = blockIdx.x;
-    double acc[6] = {0, 0, 0, 0, 0, 0};
-    for (uint32_t g = threadIdx.x; g < grabs_per_att; g += blockDim.x)
-        for (int k = 0; k < 6; ++k) acc[k] += partial[6ull * ((size_t)a * grabs_per_att + g) + k];
+__device__ __forceinline__ void srp_tree_store(double (*sh)[6], const double acc[6], double* __restrict__ force,
+                                               double* __restrict__ torque) {
     for (int k = 0; k < 6; ++k) sh[threadIdx.x][k] = acc[k];
     __syncthreads();
-    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    for (int s = SRP_REDUCE_THREADS / 2; s > 0; s >>= 1) {
         if ((int)threadIdx.x < s)
             for (int k = 0; k < 6; ++k) sh[threadIdx.x][k] += sh[threadIdx.x + s][k];
         __syncthreads();
     }
     if (threadIdx.x == 0) {
         for (int k = 0; k < 3; ++k) {
-            force[3ull * a + k] = sh[0][k];
-            torque[3ull * a + k] = sh[0][3 + k];
+            force[k] = sh[0][k];
+            torque[k] = sh[0][3 + k];
         }
     }
+}
+
+// one block per attitude
+__global__ void __launch_bounds__(SRP_REDUCE_THREADS) k_srp_reduce(const double* __restrict__ partial,
+                                                                  uint32_t blocks_per_att, double* __restrict__ force,
+                                                                  double* __restrict__ torque) {
+    __shared__ double sh[SRP_REDUCE_THREADS][6];
+    const uint32_t a = blockIdx.x;
+    double acc[6] = {0, 0, 0, 0, 0, 0};
+    for (uint32_t g = threadIdx.x; g < blocks_per_att; g += SRP_REDUCE_THREADS)
+        for (int k = 0; k < 6; ++k) acc[k] += partial[6ull * ((size_t)a * blocks_per_att + g) + k];
+    srp_tree_store(sh, acc, force + 3ull * a, torque + 3ull * a);
+}
+
+// blocks [block0, block0 + nblk) of one attitude, whose partials start at `partial`, into the
+// running thread totals `run` (SRP_REDUCE_THREADS x 6, zeroed before the attitude's first wave)
+__global__ void __launch_bounds__(SRP_REDUCE_THREADS) k_srp_fold(const double* __restrict__ partial, uint64_t block0,
+                                                                uint32_t nblk, double* __restrict__ run) {
+    double acc[6];
+    for (int k = 0; k < 6; ++k) acc[k] = run[6 * threadIdx.x + k];
+    uint64_t g = block0 + ((threadIdx.x + SRP_REDUCE_THREADS - block0 % SRP_REDUCE_THREADS) % SRP_REDUCE_THREADS);
+    for (; g < block0 + nblk; g += SRP_REDUCE_THREADS)
+        for (int k = 0; k < 6; ++k) acc[k] += partial[6ull * (g - block0) + k];
+    for (int k = 0; k < 6; ++k) run[6 * threadIdx.x + k] = acc[k];
+}
+
+__global__ void __launch_bounds__(SRP_REDUCE_THREADS) k_srp_tree(const double* __restrict__ run,
+                                                                double* __restrict__ force,
+                                                                double* __restrict__ torque) {
+    __shared__ double sh[SRP_REDUCE_THREADS][6];
+    double acc[6];
+    for (int k = 0; k < 6; ++k) acc[k] = run[6 * threadIdx.x + k];
+    srp_tree_store(sh, acc, force, torque);
 }
 
 // ---------------------------------------------------------------- wavefront SRP (crt_srp)
@@ -243,7 +141,8 @@ struct SrpShadeArgs {
     uint32_t seg, nb;
     float inv_c;
     float cm[3];
-    double* partial;          // 6 per block of SRP_BLOCK_ITEMS items (global block index)
+    double* partial;          // 6 per block of SRP_BLOCK_ITEMS items (the request's block index - block0)
+    uint64_t block0;
     double* facet;            // n_att * n_tris or null
     uint32_t n_tris;
     uint32_t* q_out;          // continuing items of the next segment
@@ -344,7 +243,7 @@ __global__ void __launch_bounds__(SRP_SHADE_THREADS) k_srp_shade(SceneView sv, S
                 atomicAdd(&A.facet[(size_t)a * A.n_tris + key], (double)sum);
         }
     }
-    const size_t slot = (size_t)(W.i0 / SRP_BLOCK_ITEMS + blockIdx.x) * 6;
+    const size_t slot = (size_t)(W.i0 / SRP_BLOCK_ITEMS + blockIdx.x - A.block0) * 6;
     if (!__syncthreads_or(any_hit)) {
         if (FIRST && threadIdx.x < 6) A.partial[slot + threadIdx.x] = 0.0;
         return;
@@ -363,8 +262,7 @@ __global__ void __launch_bounds__(SRP_SHADE_THREADS) k_srp_shade(SceneView sv, S
 
 }  // namespace
 
-void srp_plan(crt_scene* s, const crt_srp_desc* desc, const double* quats, size_t n_att, SrpPlan& P) {
-    CRT_CHECK(n_att == 0 || quats, CRT_ERR_INVALID, "null buffer");
+void srp_frame(crt_scene* s, const crt_srp_desc* desc, SrpPlan& P, SrpFrame& F) {
     CRT_CHECK(desc->grid > 0 && desc->grid <= 32768, CRT_ERR_INVALID, "grid must be in [1, 32768]");
     CRT_CHECK(desc->c > 0 && std::isfinite(desc->flux), CRT_ERR_INVALID, "bad flux or speed of light");
     CRT_CHECK(desc->num_bounces <= 16, CRT_ERR_INVALID, "at most 16 specular bounces");
@@ -372,61 +270,26 @@ void srp_plan(crt_scene* s, const crt_srp_desc* desc, const double* quats, size_
                                 desc->sun_dir_inertial[1] * desc->sun_dir_inertial[1] +
                                 desc->sun_dir_inertial[2] * desc->sun_dir_inertial[2]);
     CRT_CHECK(sl > 0 && std::isfinite(sl), CRT_ERR_INVALID, "sun direction must be a non-zero vector");
-    const double si[3] = {desc->sun_dir_inertial[0] / sl, desc->sun_dir_inertial[1] / sl,
-                          desc->sun_dir_inertial[2] / sl};
+    for (int k = 0; k < 3; ++k) F.si[k] = desc->sun_dir_inertial[k] / sl;
     // body-frame box of the scene
-    double lo[3], hi[3], ctr[3];
+    double lo[3], hi[3];
     for (int k = 0; k < 3; ++k) {
         lo[k] = s->bounds[k];
         hi[k] = s->bounds[3 + k];
-        ctr[k] = 0.5 * (lo[k] + hi[k]);
+        F.ctr[k] = 0.5 * (lo[k] + hi[k]);
     }
-    const double Rb = 0.5 * std::sqrt((hi[0] - lo[0]) * (hi[0] - lo[0]) + (hi[1] - lo[1]) * (hi[1] - lo[1]) +
-                                      (hi[2] - lo[2]) * (hi[2] - lo[2]));
+    F.Rb = 0.5 * std::sqrt((hi[0] - lo[0]) * (hi[0] - lo[0]) + (hi[1] - lo[1]) * (hi[1] - lo[1]) +
+                           (hi[2] - lo[2]) * (hi[2] - lo[2]));
     const uint32_t G = desc->grid;
-    const double h = 2.0 * Rb / G;
-    std::vector<double> hq(4 * n_att);
-    if (n_att && is_device_ptr(quats)) {
-        CRT_CUDA(cudaMemcpy(hq.data(), quats, 32 * n_att, cudaMemcpyDeviceToHost));
-    } else {
-        std::copy(quats, quats + 4 * n_att, hq.begin());
-    }
-    P.att.resize(n_att);
-    for (size_t a = 0; a < n_att; ++a) {
-        double w = hq[4 * a], x = hq[4 * a + 1], y = hq[4 * a + 2], z = hq[4 * a + 3];
-        const double qn = std::sqrt(w * w + x * x + y * y + z * z);
-        CRT_CHECK(qn > 0 && std::isfinite(qn), CRT_ERR_INVALID, "attitude quaternion must be non-zero");
-        w /= qn; x /= qn; y /= qn; z /= qn;
-        // R(q) maps body vectors into the inertial frame; s_b = R^T s_i
-        const double R[9] = {1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y),
-                             2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x),
-                             2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)};
-        double sb[3];
-        for (int k = 0; k < 3; ++k) sb[k] = R[k] * si[0] + R[3 + k] * si[1] + R[6 + k] * si[2];
-        // grid basis perpendicular to s_b (same construction as the oracle)
-        double ax[3] = {1, 0, 0};
-        if (std::fabs(sb[0]) >= 0.9) { ax[0] = 0; ax[1] = 1; }
-        double e1[3] = {sb[1] * ax[2] - sb[2] * ax[1], sb[2] * ax[0] - sb[0] * ax[2], sb[0] * ax[1] - sb[1] * ax[0]};
-        const double l1 = std::sqrt(e1[0] * e1[0] + e1[1] * e1[1] + e1[2] * e1[2]);
-        for (int k = 0; k < 3; ++k) e1[k] /= l1;
-        const double e2[3] = {sb[1] * e1[2] - sb[2] * e1[1], sb[2] * e1[0] - sb[0] * e1[2], sb[0] * e1[1] - sb[1] * e1[0]};
-        for (int k = 0; k < 3; ++k) {
-            const double o0 = ctr[k] + sb[k] * (2.0 * Rb + 1.0) + e1[k] * (-Rb + 0.5 * h) + e2[k] * (-Rb + 0.5 * h);
-            P.att[a].org[k] = (float)o0;
-            P.att[a].du[k] = (float)(e1[k] * h);
-            P.att[a].dv[k] = (float)(e2[k] * h);
-            P.att[a].dir[k] = (float)(-sb[k]);
-        }
-        P.att[a].E0 = (float)(desc->flux * h * h);
-        P.att[a].pad = 0.f;
-    }
+    F.h = 2.0 * F.Rb / G;
+    F.E0 = desc->flux * F.h * F.h;
     P.G = G;
     P.tiles_x = (G + 7) / 8;
     P.tiles = P.tiles_x * ((G + 3) / 4);
     P.ipa = ((uint64_t)P.tiles * 32 + SRP_BLOCK_ITEMS - 1) / SRP_BLOCK_ITEMS * SRP_BLOCK_ITEMS;
-    P.total = P.ipa * n_att;
     P.blocks_per_att = P.ipa / SRP_BLOCK_ITEMS;
-    CRT_CHECK(P.blocks_per_att * n_att < (1ull << 31), CRT_ERR_INVALID, "too many rays in one call");
+    P.natt = 0;
+    P.total = 0;
     // specular continuations only when some entity reflects specularly
     bool specular = false;
     for (const EntityDev& E : s->host_entities) specular |= E.rho_s > 0.f;
@@ -440,6 +303,58 @@ void srp_plan(crt_scene* s, const crt_srp_desc* desc, const double* quats, size_
         P.box_lo[k] = (float)(lo[k] - m - 1e-6 * std::fabs(lo[k]));
         P.box_hi[k] = (float)(hi[k] + m + 1e-6 * std::fabs(hi[k]));
     }
+}
+
+void srp_set_attitudes(SrpPlan& P, size_t n_att) {
+    CRT_CHECK(P.blocks_per_att * n_att < (1ull << 31), CRT_ERR_INVALID, "too many rays in one call");
+    P.natt = n_att;
+    P.total = P.ipa * n_att;
+}
+
+void srp_attitude(const SrpFrame& F, const double q[4], SrpAtt& out) {
+    double w = q[0], x = q[1], y = q[2], z = q[3];
+    const double qn = std::sqrt(w * w + x * x + y * y + z * z);
+    CRT_CHECK(qn > 0 && std::isfinite(qn), CRT_ERR_INVALID, "attitude quaternion must be non-zero");
+    w /= qn; x /= qn; y /= qn; z /= qn;
+    // R(q) maps body vectors into the inertial frame; s_b = R^T s_i
+    const double R[9] = {1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y),
+                         2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x),
+                         2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)};
+    const double* si = F.si;
+    double sb[3];
+    for (int k = 0; k < 3; ++k) sb[k] = R[k] * si[0] + R[3 + k] * si[1] + R[6 + k] * si[2];
+    // grid basis perpendicular to s_b (same construction as the oracle)
+    double ax[3] = {1, 0, 0};
+    if (std::fabs(sb[0]) >= 0.9) { ax[0] = 0; ax[1] = 1; }
+    double e1[3] = {sb[1] * ax[2] - sb[2] * ax[1], sb[2] * ax[0] - sb[0] * ax[2], sb[0] * ax[1] - sb[1] * ax[0]};
+    const double l1 = std::sqrt(e1[0] * e1[0] + e1[1] * e1[1] + e1[2] * e1[2]);
+    for (int k = 0; k < 3; ++k) e1[k] /= l1;
+    const double e2[3] = {sb[1] * e1[2] - sb[2] * e1[1], sb[2] * e1[0] - sb[0] * e1[2], sb[0] * e1[1] - sb[1] * e1[0]};
+    const double Rb = F.Rb, h = F.h;
+    for (int k = 0; k < 3; ++k) {
+        const double o0 = F.ctr[k] + sb[k] * (2.0 * Rb + 1.0) + e1[k] * (-Rb + 0.5 * h) + e2[k] * (-Rb + 0.5 * h);
+        out.org[k] = (float)o0;
+        out.du[k] = (float)(e1[k] * h);
+        out.dv[k] = (float)(e2[k] * h);
+        out.dir[k] = (float)(-sb[k]);
+    }
+    out.E0 = (float)F.E0;
+    out.pad = 0.f;
+}
+
+void srp_plan(crt_scene* s, const crt_srp_desc* desc, const double* quats, size_t n_att, SrpPlan& P) {
+    CRT_CHECK(n_att == 0 || quats, CRT_ERR_INVALID, "null buffer");
+    SrpFrame F;
+    srp_frame(s, desc, P, F);
+    std::vector<double> hq(4 * n_att);
+    if (n_att && is_device_ptr(quats)) {
+        CRT_CUDA(cudaMemcpy(hq.data(), quats, 32 * n_att, cudaMemcpyDeviceToHost));
+    } else {
+        std::copy(quats, quats + 4 * n_att, hq.begin());
+    }
+    P.att.resize(n_att);
+    for (size_t a = 0; a < n_att; ++a) srp_attitude(F, hq.data() + 4 * a, P.att[a]);
+    srp_set_attitudes(P, n_att);
 }
 
 uint64_t srp_wave_items(const SrpPlan& P, uint64_t cap, uint64_t i0) {
@@ -472,7 +387,8 @@ SrpWave srp_wave(const SrpPlan& P, const SrpAtt* d_att, char* state, uint64_t ca
 }
 
 void srp_wave_stages(crt_context* ctx, const SceneView& sv, const SrpWave& W, uint32_t n, const SrpPlan& P,
-                     double* partial, double* facet, uint32_t n_tris, uint32_t* bq, uint32_t* bcount) {
+                     double* partial, double* facet, uint32_t n_tris, uint32_t* bq, uint32_t* bcount,
+                     uint64_t partial_block0, uint32_t* trace_queue) {
     cudaStream_t st = ctx->stream;
     SrpShadeArgs A;
     A.n_items = n;
@@ -480,6 +396,7 @@ void srp_wave_stages(crt_context* ctx, const SceneView& sv, const SrpWave& W, ui
     A.inv_c = P.inv_c;
     for (int k = 0; k < 3; ++k) A.cm[k] = P.cm[k];
     A.partial = partial;
+    A.block0 = partial_block0;
     A.facet = facet;
     A.n_tris = n_tris;
     A.q_out = bq;
@@ -495,7 +412,7 @@ void srp_wave_stages(crt_context* ctx, const SceneView& sv, const SrpWave& W, ui
             SrpBounceJob J;
             J.W = W;
             J.q = bq;
-            launch_trace<false>(ctx, sv, J, n, bcount + ((seg - 1) & 1));
+            launch_trace<false>(ctx, sv, J, n, bcount + ((seg - 1) & 1), trace_queue);
             k_srp_shade<false><<<nblk, SRP_SHADE_THREADS, 0, st>>>(sv, W, A);
         }
         check_launch(ctx, "k_srp_shade");
@@ -504,7 +421,8 @@ void srp_wave_stages(crt_context* ctx, const SceneView& sv, const SrpWave& W, ui
 
 void srp_reduce(crt_context* ctx, const double* partial, const SrpPlan& P, double* force, double* torque) {
     if (!P.n_att()) return;
-    k_srp_reduce<<<(uint32_t)P.n_att(), 256, 0, ctx->stream>>>(partial, (uint32_t)P.blocks_per_att, force, torque);
+    k_srp_reduce<<<(uint32_t)P.n_att(), SRP_REDUCE_THREADS, 0, ctx->stream>>>(partial, (uint32_t)P.blocks_per_att,
+                                                                             force, torque);
     check_launch(ctx, "k_srp_reduce");
 }
 
@@ -561,28 +479,42 @@ extern "C" int crt_srp(crt_scene* s, const crt_srp_desc* desc, const double* qua
 }
 
 // ---------------------------------------------------------------- allocation-free variant
-// crt_srp_static: the same force / torque computation with every piece of scratch (work counter,
-// attitude table, per-chunk FP64 partial sums, staging of host outputs) in the file-scope device
-// array below, so a call performs no device allocation.  It serves callers that must not allocate
-// device memory after start-up: flight-dynamics or attitude-control loops with a fixed memory
-// budget, and code that runs while another component owns the CUDA allocator.  Every GPU that loads
-// the library holds this array until the process exits.
-#define CRT_SRP_STATIC_BYTES (16u << 20)          // 16 MiB per device
+// crt_srp_static: the same force and torque as crt_srp, from the same wavefront stages, with every
+// piece of scratch in the file-scope device array below, so that a call allocates no memory.  It
+// serves callers that must not allocate device memory once they run: flight-dynamics or attitude
+// loops that evaluate radiation pressure every integration step under a fixed memory budget, and
+// components embedded in a host application that owns the CUDA allocator.  Every GPU that loads the
+// library holds this array until the process exits.
+//
+// Layout: work counters, the attitude table and the staging of host outputs, then the state of one
+// wave of at most SS_WAVE items (per-item hits and continuation rays, hit mask, continuation queue)
+// and the partial sums of that wave's blocks.  Waves hold whole attitudes when an attitude has at
+// most SS_WAVE items (their totals are reduced right after the wave); a larger attitude runs as
+// several waves whose block sums are folded into running per-thread totals (k_srp_fold) and summed
+// by k_srp_tree after its last wave.  Either way every addition happens in the order crt_srp uses,
+// so the results are bitwise equal to crt_srp's.
+#define CRT_SRP_STATIC_BYTES (64u << 20)          // 64 MiB per device
 #define CRT_SRP_STATIC_MAX_ATT 4096u              // attitudes per call
 static __device__ __align__(256) unsigned char g_srp_static_scratch[CRT_SRP_STATIC_BYTES];
 
 namespace {
 
-constexpr size_t SS_COUNTER = 0;                                  // work counter (zeroed per launch)
+constexpr uint64_t SS_WAVE = 1u << 20;                            // items per wave
+constexpr size_t ss_align(size_t x) { return (x + 255) & ~size_t(255); }
+constexpr size_t SS_QUEUE = 0;                                    // trace work counter
+constexpr size_t SS_BCOUNT = 128;                                 // 2 continuation-queue counters
 constexpr size_t SS_ATT = 256;                                    // SrpAtt table
-constexpr size_t SS_OUT = SS_ATT + sizeof(SrpAtt) * CRT_SRP_STATIC_MAX_ATT;    // force | torque staging
-constexpr size_t SS_PART = (SS_OUT + 48ull * CRT_SRP_STATIC_MAX_ATT + 255) & ~size_t(255);
-constexpr size_t SS_PART_BYTES = CRT_SRP_STATIC_BYTES - SS_PART;
+constexpr size_t SS_OUT = ss_align(SS_ATT + sizeof(SrpAtt) * CRT_SRP_STATIC_MAX_ATT);   // force | torque staging
+constexpr size_t SS_RUN = ss_align(SS_OUT + 48ull * CRT_SRP_STATIC_MAX_ATT);          // running totals 256 x 6
+constexpr size_t SS_PART = ss_align(SS_RUN + 6ull * 8 * SRP_REDUCE_THREADS);          // one wave's block sums
+constexpr size_t SS_BQ = ss_align(SS_PART + 48ull * (SS_WAVE / SRP_BLOCK_ITEMS));      // continuation queue
+constexpr size_t SS_STATE = ss_align(SS_BQ + 4ull * SS_WAVE + 256);                   // wave state
+static_assert(SS_WAVE % SRP_BLOCK_ITEMS == 0, "waves hold whole reduction blocks");
 
 std::mutex g_static_mu;
 void* g_static_ptr[256] = {};
 
-// Device address of the scratch array on the current device; resolved once per device.
+// Device address of the scratch array on `device` (which must be current); resolved once per device.
 void* static_scratch(int device) {
     CRT_CHECK(device >= 0 && device < 256, CRT_ERR_INVALID, "device index out of range");
     std::lock_guard<std::mutex> lk(g_static_mu);
@@ -594,6 +526,13 @@ void* static_scratch(int device) {
     return g_static_ptr[device];
 }
 
+// One output: written on the device directly, or staged in the scratch and copied to host memory.
+struct StaticOut {
+    double* user;
+    double* dev;
+    bool host;
+};
+
 }  // namespace
 
 extern "C" int crt_srp_static(crt_scene* s, const crt_srp_desc* desc, const double* quats, size_t n_att,
@@ -604,111 +543,74 @@ extern "C" int crt_srp_static(crt_scene* s, const crt_srp_desc* desc, const doub
         CRT_CHECK(n_att == 0 || (quats && force && torque), CRT_ERR_INVALID, "null buffer");
         CRT_CHECK(n_att <= CRT_SRP_STATIC_MAX_ATT, CRT_ERR_INVALID,
                   "crt_srp_static: at most 4096 attitudes per call (static scratch limit)");
-        CRT_CHECK(desc->grid > 0 && desc->grid <= 32768, CRT_ERR_INVALID, "grid must be in [1, 32768]");
-        CRT_CHECK(desc->c > 0 && std::isfinite(desc->flux), CRT_ERR_INVALID, "bad flux or speed of light");
-        CRT_CHECK(desc->num_bounces <= 16, CRT_ERR_INVALID, "at most 16 specular bounces");
-        CRT_CHECK(!is_device_ptr(quats), CRT_ERR_INVALID, "crt_srp_static reads the quaternions from host memory");
-        const uint32_t G = desc->grid;
-        const uint32_t tiles = ((G + 7) / 8) * ((G + 3) / 4);
-        const uint32_t gpa = (tiles + CHUNK - 1) / CHUNK;
-        CRT_CHECK((size_t)gpa * 48 <= SS_PART_BYTES, CRT_ERR_INVALID,
-                  "crt_srp_static: grid too large for the 16 MiB static scratch (one attitude's partial sums "
-                  "must fit; grid <= 11585)");
+        SrpPlan P;   // its attitude table stays empty: the attitudes go to the static array
+        SrpFrame F;
+        srp_frame(s, desc, P, F);
+        static_assert(srp_state_bytes(SS_WAVE, 1) <= CRT_SRP_STATIC_BYTES - SS_STATE, "static scratch too small");
         if (!n_att) return;
         CRT_CUDA(cudaSetDevice(ctx->device));
         char* base = (char*)static_scratch(ctx->device);
-        uint32_t* queue = (uint32_t*)(base + SS_COUNTER);
+        uint32_t* queue = (uint32_t*)(base + SS_QUEUE);
+        uint32_t* bcount = (uint32_t*)(base + SS_BCOUNT);
         SrpAtt* d_att = (SrpAtt*)(base + SS_ATT);
-        double* d_out = (double*)(base + SS_OUT);
+        double* run = (double*)(base + SS_RUN);
         double* d_partial = (double*)(base + SS_PART);
+        uint32_t* bq = (uint32_t*)(base + SS_BQ);
+        char* state = base + SS_STATE;
         cudaStream_t st = ctx->stream;
 
-        const double sl = std::sqrt(desc->sun_dir_inertial[0] * desc->sun_dir_inertial[0] +
-                                    desc->sun_dir_inertial[1] * desc->sun_dir_inertial[1] +
-                                    desc->sun_dir_inertial[2] * desc->sun_dir_inertial[2]);
-        CRT_CHECK(sl > 0 && std::isfinite(sl), CRT_ERR_INVALID, "sun direction must be a non-zero vector");
-        const double si[3] = {desc->sun_dir_inertial[0] / sl, desc->sun_dir_inertial[1] / sl,
-                              desc->sun_dir_inertial[2] / sl};
-        double ctr[3], ext2 = 0;
-        for (int k = 0; k < 3; ++k) {
-            ctr[k] = 0.5 * ((double)s->bounds[k] + (double)s->bounds[3 + k]);
-            const double e = (double)s->bounds[3 + k] - (double)s->bounds[k];
-            ext2 += e * e;
-        }
-        const double Rb = 0.5 * std::sqrt(ext2);
-        const double h = 2.0 * Rb / G;
-        // attitude table: computed on the host in chunks held on the stack, copied into the scratch
-        SrpAtt chunk[64];
+        // attitude table: computed on the host in chunks held on the stack, copied into the scratch;
+        // quaternions in device memory are read back chunk by chunk
+        const bool dev_q = is_device_ptr(quats);
         for (size_t a0 = 0; a0 < n_att; a0 += 64) {
             const size_t na = std::min<size_t>(64, n_att - a0);
-            for (size_t j = 0; j < na; ++j) {
-                const double* q = quats + 4 * (a0 + j);
-                double w = q[0], x = q[1], y = q[2], z = q[3];
-                const double qn = std::sqrt(w * w + x * x + y * y + z * z);
-                CRT_CHECK(qn > 0 && std::isfinite(qn), CRT_ERR_INVALID, "attitude quaternion must be non-zero");
-                w /= qn; x /= qn; y /= qn; z /= qn;
-                const double R[9] = {1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y),
-                                     2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x),
-                                     2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)};
-                double sb[3];
-                for (int k = 0; k < 3; ++k) sb[k] = R[k] * si[0] + R[3 + k] * si[1] + R[6 + k] * si[2];
-                double ax[3] = {1, 0, 0};
-                if (std::fabs(sb[0]) >= 0.9) { ax[0] = 0; ax[1] = 1; }
-                double e1[3] = {sb[1] * ax[2] - sb[2] * ax[1], sb[2] * ax[0] - sb[0] * ax[2],
-                                sb[0] * ax[1] - sb[1] * ax[0]};
-                const double l1 = std::sqrt(e1[0] * e1[0] + e1[1] * e1[1] + e1[2] * e1[2]);
-                for (int k = 0; k < 3; ++k) e1[k] /= l1;
-                const double e2[3] = {sb[1] * e1[2] - sb[2] * e1[1], sb[2] * e1[0] - sb[0] * e1[2],
-                                      sb[0] * e1[1] - sb[1] * e1[0]};
-                for (int k = 0; k < 3; ++k) {
-                    const double o0 = ctr[k] + sb[k] * (2.0 * Rb + 1.0) + e1[k] * (-Rb + 0.5 * h) + e2[k] * (-Rb + 0.5 * h);
-                    chunk[j].org[k] = (float)o0;
-                    chunk[j].du[k] = (float)(e1[k] * h);
-                    chunk[j].dv[k] = (float)(e2[k] * h);
-                    chunk[j].dir[k] = (float)(-sb[k]);
-                }
-                chunk[j].E0 = (float)(desc->flux * h * h);
-                chunk[j].pad = 0.f;
-            }
+            double qh[4 * 64];
+            SrpAtt chunk[64];
+            if (dev_q) CRT_CUDA(cudaMemcpy(qh, quats + 4 * a0, 32 * na, cudaMemcpyDeviceToHost));
+            else std::copy(quats + 4 * a0, quats + 4 * (a0 + na), qh);
+            for (size_t j = 0; j < na; ++j) srp_attitude(F, qh + 4 * j, chunk[j]);
             CRT_CUDA(cudaMemcpyAsync(d_att + a0, chunk, sizeof(SrpAtt) * na, cudaMemcpyHostToDevice, st));
             CRT_CUDA(cudaStreamSynchronize(st));   // the stack chunk is reused for the next attitudes
         }
-        const bool host_out = !is_device_ptr(force) || !is_device_ptr(torque);
-        double* f_out = host_out ? d_out : force;
-        double* t_out = host_out ? d_out + 3 * CRT_SRP_STATIC_MAX_ATT : torque;
-        const size_t att_per_launch = std::max<size_t>(1, std::min<size_t>(n_att, SS_PART_BYTES / (48ull * gpa)));
-        const size_t smem = (size_t)CRT_STACK_SMEM * CRT_TRACE_BLOCK * sizeof(uint2);
-        const int grid = occupancy_grid(ctx, ctx->counting ? (const void*)k_srp<true> : (const void*)k_srp<false>,
-                                        CRT_TRACE_BLOCK, smem);
+        StaticOut out[2] = {{force, nullptr, !is_device_ptr(force)}, {torque, nullptr, !is_device_ptr(torque)}};
+        for (int k = 0; k < 2; ++k)
+            out[k].dev = out[k].host ? (double*)(base + SS_OUT) + 3 * CRT_SRP_STATIC_MAX_ATT * k : out[k].user;
+
         const SceneView sv = scene_view(s);
-        for (size_t a0 = 0; a0 < n_att; a0 += att_per_launch) {
-            const size_t na = std::min(att_per_launch, n_att - a0);
-            SrpArgs A;
-            A.att = d_att + a0;
-            A.G = G;
-            A.tiles = tiles;
-            A.grabs_per_att = gpa;
-            A.chunk = CHUNK;
-            A.n_att = (uint32_t)na;
-            A.inv_c = (float)(1.0 / desc->c);
-            for (int k = 0; k < 3; ++k) A.cm[k] = (float)desc->center_of_mass[k];
-            A.nb = desc->num_bounces;
-            A.partial = d_partial;
-            A.facet = nullptr;
-            A.n_tris = (uint32_t)s->n_tris;
-            CRT_CUDA(cudaMemsetAsync(queue, 0, sizeof(uint32_t), st));   // the counter must start at zero
-            if (ctx->counting)
-                k_srp<true><<<grid, CRT_TRACE_BLOCK, smem, st>>>(sv, A, queue, ctx->d_error, ctx->d_counters);
-            else
-                k_srp<false><<<grid, CRT_TRACE_BLOCK, smem, st>>>(sv, A, queue, ctx->d_error, ctx->d_counters);
-            check_launch(ctx, "k_srp");
-            k_srp_reduce<<<(uint32_t)na, 256, 0, st>>>(d_partial, gpa, f_out + 3 * a0, t_out + 3 * a0);
-            check_launch(ctx, "k_srp_reduce");
+        // whole attitudes per wave when they fit, else one attitude over several waves
+        const size_t att_per_wave = P.ipa <= SS_WAVE ? (size_t)(SS_WAVE / P.ipa) : 1;
+        for (size_t a0 = 0; a0 < n_att; a0 += att_per_wave) {
+            const size_t na = std::min(att_per_wave, n_att - a0);
+            SrpPlan G = P;   // the group of attitudes [a0, a0 + na) as a request of its own
+            srp_set_attitudes(G, na);
+            const bool split = G.total > SS_WAVE;
+            if (split) CRT_CUDA(cudaMemsetAsync(run, 0, 6 * 8 * SRP_REDUCE_THREADS, st));
+            for (uint64_t i0 = 0; i0 < G.total;) {
+                const uint32_t n = (uint32_t)srp_wave_items(G, SS_WAVE, i0);
+                const SrpWave W = srp_wave(G, d_att + a0, state, SS_WAVE, i0, n);
+                SrpPrimaryJob J;
+                J.W = W;
+                CRT_CUDA(cudaMemsetAsync(W.hitmask, 0, srp_mask_bytes(n), st));
+                launch_trace<false>(ctx, sv, J, n, nullptr, queue);
+                // block sums of this wave only: slot = (block of the attitude group) - (wave's first block)
+                const uint64_t block0 = i0 / SRP_BLOCK_ITEMS;
+                srp_wave_stages(ctx, sv, W, n, G, d_partial, nullptr, (uint32_t)s->n_tris, bq, bcount, block0, queue);
+                if (split) {
+                    k_srp_fold<<<1, SRP_REDUCE_THREADS, 0, st>>>(d_partial, block0, n / SRP_BLOCK_ITEMS, run);
+                    check_launch(ctx, "k_srp_fold");
+                }
+                i0 += n;
+            }
+            if (split) {
+                k_srp_tree<<<1, SRP_REDUCE_THREADS, 0, st>>>(run, out[0].dev + 3 * a0, out[1].dev + 3 * a0);
+                check_launch(ctx, "k_srp_tree");
+            } else {
+                srp_reduce(ctx, d_partial, G, out[0].dev + 3 * a0, out[1].dev + 3 * a0);
+            }
         }
-        if (host_out) {
-            CRT_CUDA(cudaMemcpyAsync(force, f_out, n_att * 24, cudaMemcpyDeviceToHost, st));
-            CRT_CUDA(cudaMemcpyAsync(torque, t_out, n_att * 24, cudaMemcpyDeviceToHost, st));
-            check_device_error(ctx, "crt_srp_static");
-        }
+        for (int k = 0; k < 2; ++k)
+            if (out[k].host)
+                CRT_CUDA(cudaMemcpyAsync(out[k].user, out[k].dev, n_att * 24, cudaMemcpyDeviceToHost, st));
+        check_device_error(ctx, "crt_srp_static");
     });
 }

@@ -91,13 +91,24 @@ struct SrpPlan {
     uint64_t blocks_per_att = 0;
     float inv_c = 0.f, cm[3] = {0.f, 0.f, 0.f};
     float box_lo[3] = {0.f, 0.f, 0.f}, box_hi[3] = {0.f, 0.f, 0.f};   // scene box + 1e-4 extent + 1e-5
-    size_t n_att() const { return att.size(); }
+    size_t natt = 0;                  // attitudes (att holds their table unless the caller keeps it)
+    size_t n_att() const { return natt; }
+};
+
+// The attitude-independent frame of a request: unit sun direction (inertial), grid centre and
+// half size, cell size and ray power.  srp_attitude turns one quaternion into its grid of rays.
+struct SrpFrame {
+    double si[3];
+    double ctr[3];
+    double Rb, h, E0;
 };
 
 // Per-wave SRP state for waves of at most `cap` items: hits (16 B per item), continuation state when
 // there are specular segments (33 B per item), then the primary segment's hit mask (1 bit per item).
-inline size_t srp_mask_offset(uint64_t cap, uint32_t nb) { return ((size_t)cap * (nb ? 49 : 16) + 255) & ~size_t(255); }
-inline size_t srp_state_bytes(uint64_t cap, uint32_t nb) {
+constexpr size_t srp_mask_offset(uint64_t cap, uint32_t nb) {
+    return ((size_t)cap * (nb ? 49 : 16) + 255) & ~size_t(255);
+}
+constexpr size_t srp_state_bytes(uint64_t cap, uint32_t nb) {
     return srp_mask_offset(cap, nb) + ((((size_t)cap + 31) / 32 * 4 + 255) & ~size_t(255)) + 256;
 }
 inline size_t srp_mask_bytes(uint64_t n) { return ((size_t)n + 31) / 32 * 4; }
@@ -112,6 +123,14 @@ __device__ __forceinline__ void srp_store_primary(const SrpWave& W, uint32_t i, 
 // Validates an SRP request and builds its plan; quaternions may be host or device memory.  Throws
 // CrtError.
 void srp_plan(crt_scene* s, const crt_srp_desc* desc, const double* quats, size_t n_att, SrpPlan& P);
+// The parts of srp_plan that need no attitude: validates desc and fills every field of P but the
+// attitude table and count (natt = total = 0), and the frame F.  Allocates nothing.  Throws CrtError.
+void srp_frame(crt_scene* s, const crt_srp_desc* desc, SrpPlan& P, SrpFrame& F);
+// Sets P's attitude count (natt, total); throws when the call holds too many rays.
+void srp_set_attitudes(SrpPlan& P, size_t n_att);
+// Ray grid of one attitude (unit quaternion w, x, y, z rotating body vectors into the inertial
+// frame; normalised here).  Throws CrtError for a zero or non-finite quaternion.
+void srp_attitude(const SrpFrame& F, const double q[4], SrpAtt& out);
 // Wave descriptor over `state` (room for `cap` items) for items [i0, i0 + n) of the request
 // (d_att: its attitude table on the device)
 SrpWave srp_wave(const SrpPlan& P, const SrpAtt* d_att, char* state, uint64_t cap, uint64_t i0, uint64_t n);
@@ -119,8 +138,12 @@ SrpWave srp_wave(const SrpPlan& P, const SrpAtt* d_att, char* state, uint64_t ca
 // else the rest of the current attitude
 uint64_t srp_wave_items(const SrpPlan& P, uint64_t cap, uint64_t i0);
 // After the primary segment's hits are in W.hit: its shade, then the specular segments (trace of
-// the compacted continuation queue + shade).  bq: room for n entries; bcount: 2 counters.
+// the compacted continuation queue + shade).  bq: room for n entries; bcount: 2 counters.  Block b
+// of the wave sums into partial slot W.i0 / SRP_BLOCK_ITEMS + b - partial_block0 (0: the request's
+// whole partial array; the wave's first block: an array holding this wave's blocks only).
+// trace_queue: work counter of the continuation traces (null: the context's scratch counter).
 void srp_wave_stages(crt_context* ctx, const SceneView& sv, const SrpWave& W, uint32_t n, const SrpPlan& P,
-                     double* partial, double* facet, uint32_t n_tris, uint32_t* bq, uint32_t* bcount);
+                     double* partial, double* facet, uint32_t n_tris, uint32_t* bq, uint32_t* bcount,
+                     uint64_t partial_block0 = 0, uint32_t* trace_queue = nullptr);
 // Per-attitude force and torque from the request's partial sums (device outputs)
 void srp_reduce(crt_context* ctx, const double* partial, const SrpPlan& P, double* force, double* torque);

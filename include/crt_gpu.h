@@ -258,15 +258,18 @@ int crt_batch(crt_context* ctx, const crt_request* requests, size_t n, crt_batch
 int crt_srp(crt_scene* scene, const crt_srp_desc* desc, const double* quaternions, size_t n_att, double* force,
             double* torque, double* facet_power);
 /* Allocation-free variant of crt_srp (no counterpart in the reference): the same force and torque,
- * with all scratch (work counter, attitude table, per-chunk FP64 partial sums, staging of host
- * outputs) in one 16 MiB file-scope device array instead of device allocations, for callers that
- * must not allocate device memory once running (fixed-budget flight-dynamics or attitude loops,
- * components that do not own the CUDA allocator).  Limits: n_att <= 4096 per call and
- * grid <= 11585 (one attitude's partial sums must fit); quaternions are read from host memory;
- * force / torque may be host or device memory; no per-facet output.  The first call on a device
+ * bit for bit, from the same wavefront stages, with all scratch (work counters, attitude table, one
+ * wave's ray state and block sums, staging of host outputs) in one 64 MiB file-scope device array
+ * instead of device allocations.  It is for callers that must not allocate device memory once they
+ * run: flight-dynamics or attitude loops that evaluate radiation pressure every integration step
+ * under a fixed memory budget, and components embedded in an application that owns the CUDA
+ * allocator.  Limits: n_att <= 4096 per call (larger counts are refused with CRT_ERR_INVALID and a
+ * message naming the static scratch); grid <= 32768 as for crt_srp; no per-facet output.
+ * Quaternions, force and torque may each be host or device memory.  The first call on a device
  * resolves the array's device address (cudaGetSymbolAddress) and should come before any stream
- * capture.  All calls share the array: calls that overlap on the GPU (other streams or contexts)
- * race.  Every GPU that loads the library keeps the 16 MiB until the process exits. */
+ * capture.  Every call shares the array and keeps the previous call's contents: calls that overlap
+ * on the GPU (other streams or contexts of the same device) race.  Every GPU that loads the library
+ * keeps the 64 MiB until the process exits. */
 int crt_srp_static(crt_scene* scene, const crt_srp_desc* desc, const double* quaternions, size_t n_att,
                    double* force, double* torque);
 

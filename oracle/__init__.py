@@ -70,7 +70,7 @@ def lib():
         L.oracle_camera_rays.argtypes = [vp, u32, u32, vp]
         L.oracle_passes.argtypes = [vp, vp, u32, u32, vp, vp, vp, vp, i32]
         L.oracle_lidar_batch.argtypes = [vp, vp, vp, sz, i32, vp, vp, i32]
-        L.oracle_render.argtypes = [vp, vp, vp, u32, vp, u32, u32, vp, vp, vp, i32]
+        L.oracle_render.argtypes = [vp, vp, vp, u32, vp, u32, u32, vp, vp, vp, vp, i32]
         L.oracle_srp.argtypes = [vp, vp, u32, u32, vp, vp, vp, i32]
         L.oracle_philox.argtypes = [u32, u32, u32, u32, u32, u32, vp]
         _lib = L
@@ -176,7 +176,9 @@ class Scene:
         return rng, prim
 
     def render(self, cam, lights, min_samples=1, max_samples=1, noise_threshold=1.0, num_bounces=1, seed=0,
-               request=0, row0=0, row1=None):
+               request=0, row0=0, row1=None, with_m2=False):
+        """(radiance [h, w, 4] f32, rgba8 [h, w, 4], samples taken [h, w]) and, with_m2, the Welford
+        M2 [h, w, 3] (FP64) of each pixel's path samples: the sample variance is M2 / (n - 1)."""
         c = make_camera(cam)
         L = make_lights(lights)
         p = RenderParams(int(min_samples), int(max_samples), float(noise_threshold), int(num_bounces), int(seed),
@@ -187,10 +189,12 @@ class Scene:
         rad = np.empty((n, 4), np.float32)
         u8 = np.empty((n, 4), np.uint8)
         taken = np.empty(n, np.uint32)
+        m2 = np.empty((n, 3)) if with_m2 else None
         lib().oracle_render(self.h, ctypes.byref(c), L, len(lights), ctypes.byref(p), row0, row1, _ptr(rad), _ptr(u8),
-                            _ptr(taken), self.nthreads)
+                            _ptr(taken), _ptr(m2), self.nthreads)
         shp = (row1 - row0, W)
-        return rad.reshape(shp + (4,)), u8.reshape(shp + (4,)), taken.reshape(shp)
+        out = rad.reshape(shp + (4,)), u8.reshape(shp + (4,)), taken.reshape(shp)
+        return out + (m2.reshape(shp + (3,)),) if with_m2 else out
 
     def srp(self, params, row0=0, row1=None, facet_power=None):
         row1 = params.grid if row1 is None else row1

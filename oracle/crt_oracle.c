@@ -667,7 +667,7 @@ static col_t trace_path(const oracle_scene* s, const oracle_light* L, uint32_t n
 /* do_render (do_render.hpp:65-134): jittered samples, running mean, adaptive stop, u8 quantise */
 void oracle_render(const oracle_scene* s, const oracle_camera* cam, const oracle_light* lights, uint32_t n_lights,
                    const oracle_render_params* p, uint32_t row0, uint32_t row1, float* radiance, uint8_t* rgba8,
-                   uint32_t* samples_taken, int nthreads) {
+                   uint32_t* samples_taken, double* m2, int nthreads) {
     set_threads(nthreads);
     uint32_t W = width_of(cam);
     long long total = (long long)(row1 - row0) * W;
@@ -676,6 +676,7 @@ void oracle_render(const oracle_scene* s, const oracle_camera* cam, const oracle
         uint32_t j = row0 + (uint32_t)(k / W), i = (uint32_t)(k % W);
         uint32_t pixel = j * W + i;
         col_t pix = {0, 0, 0};
+        double wm[3] = {0, 0, 0}, wm2[3] = {0, 0, 0};   /* Welford mean / M2 of the samples (test statistics) */
         int sample;
         int taken = 0;
         for (sample = 1; sample < p->max_samples + 1; ++sample) {
@@ -688,6 +689,12 @@ void oracle_render(const oracle_scene* s, const oracle_camera* cam, const oracle
             }
             col_t L = trace_path(s, lights, n_lights, p, ray, pixel, (uint32_t)(sample - 1));
             taken = sample;
+            const double lv[3] = {L.r, L.g, L.b};
+            for (int c = 0; c < 3; ++c) {
+                double dl = lv[c] - wm[c];
+                wm[c] += dl / sample;
+                wm2[c] += dl * (lv[c] - wm[c]);
+            }
             float inv = 1.0f / sample;
             col_t d = {(L.r - pix.r) * inv, (L.g - pix.g) * inv, (L.b - pix.b) * inv};
             pix.r += d.r; pix.g += d.g; pix.b += d.b;
@@ -706,6 +713,7 @@ void oracle_render(const oracle_scene* s, const oracle_camera* cam, const oracle
             }
         }
         if (samples_taken) samples_taken[k] = (uint32_t)taken;
+        if (m2) for (int c = 0; c < 3; ++c) m2[3 * k + c] = wm2[c];
     }
 }
 

@@ -95,10 +95,11 @@ void oracle_passes(const oracle_scene* s, const oracle_camera* cam, uint32_t row
 void oracle_lidar_batch(const oracle_scene* s, const double* positions, const double* rotations, size_t n,
                         int z_positive, double* range, int64_t* prim, int nthreads);
 
-/* unidirectional path tracer over rows [row0, row1): radiance n*4 floats, rgba8 n*4 bytes */
+/* unidirectional path tracer over rows [row0, row1): radiance n*4 floats, rgba8 n*4 bytes; m2 (may be
+ * NULL) n*3 Welford sums of squared deviations of each pixel's path samples (FP64), for statistics */
 void oracle_render(const oracle_scene* s, const oracle_camera* cam, const oracle_light* lights, uint32_t n_lights,
                    const oracle_render_params* p, uint32_t row0, uint32_t row1, float* radiance,
-                   uint8_t* rgba8, uint32_t* samples_taken, int nthreads);
+                   uint8_t* rgba8, uint32_t* samples_taken, double* m2, int nthreads);
 
 /* radiation pressure for one attitude (sun direction already in the body frame) over grid rows
  * [row0, row1): force[3], torque[3] (N, N m), facet_power[n_tris] (W, accumulated, caller zeroes) */

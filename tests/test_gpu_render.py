@@ -1,19 +1,24 @@
 """GPU wavefront path tracer vs the reference fixtures and the FP64 oracle, through the C ABI.
 
-* 1 spp at pixel corners, 1 bounce, point light: no random draws; radiance equals the reference's
-  within FP32 rounding except where a shading term crosses zero or a shadow edge moves.
-* Same seed as the oracle: both draw the same Philox streams, so per-pixel radiance agrees closely
-  (paths diverge only where FP32 and FP64 take different branches).
+* Deterministic renders (1 spp at pixel centres, 1 bounce, point lights: no random draws): radiance
+  equals the oracle's (which reproduces the reference's, tests/test_oracle_golden.py) within FP32
+  rounding on every pixel except those whose primary or shadow ray passes within the edge distance
+  of a triangle edge, or whose shadow ray re-enters its own surface within the shade stage's
+  decision margin of that triangle's edge (helpers.check_direct_render).
+* Same seed as the oracle: both draw the same Philox streams; per pixel within 4 sigma of the
+  Monte-Carlo error (sigma from the oracle's per-pixel sample variance), at most 1e-3 of the pixel
+  values beyond, image mean within 0.5 % (helpers.check_mc_radiance).
 * Area light, 512 spp, 3 bounces vs the reference's own path tracer (different random streams):
-  per pixel within 4 sigma, image mean within 0.5 % (pixels next to the light plane excluded, see
-  test_oracle_golden.test_area_light_render_statistics).
+  per pixel within 4 sigma with at most 1e-3 of the values beyond, image mean within 0.5 % (pixels
+  next to the light plane excluded, see test_oracle_golden.test_area_light_render_statistics).
 """
 import numpy as np
 import pytest
 
 import oracle
-from crt_gb300 import lib, scenes
-from helpers import camera_from, entities_from, lights_from, load_golden, radiance_stats_ok
+from crt_gb300 import lib, scenes, workloads
+from helpers import (TriIndex, camera_from, check_direct_render, check_mc_radiance, entities_from, lights_from,
+                     load_golden, radiance_stats_ok, to_f32_rays)
 
 pytestmark = pytest.mark.gpu
 
@@ -32,15 +37,43 @@ def cornell(ctx):
     return d, ents, ctx.scene(ents), oracle.Scene(ents)
 
 
+def direct_parity(sc, o, cam, lights, rad, orad, what):
+    """check_direct_render for a 1-spp, 1-bounce point-light render of scene sc (GPU) / o (oracle)."""
+    index = TriIndex(o.tris())
+    rays = workloads.camera_rays(cam)
+    ox, _, _, oprim = o.passes(cam)
+    gx = sc.passes(cam)[0]
+    h = sc.trace_closest(rays32(to_f32_rays(rays)))
+    gprim = np.where(h["prim"] == lib.CRT_MISS, -1, h["prim"].astype(np.int64))
+
+    def trace_o(r):
+        p, t, _, _ = o.trace_closest(r)
+        return p, t
+
+    def trace_g(r):
+        hh = sc.trace_closest(rays32(to_f32_rays(r)))
+        return np.where(hh["prim"] == lib.CRT_MISS, -1, hh["prim"].astype(np.int64)), hh["t"].astype(np.float64)
+    return check_direct_render(index, rays, rad, orad, ox, oprim, gx, gprim, lights, trace_o, trace_g, what=what)
+
+
+def rays32(rays64):
+    r = np.empty(rays64.shape[0], lib.RAY_DTYPE)
+    r["o"] = rays64[:, 0:3]
+    r["d"] = rays64[:, 3:6]
+    r["tmin"] = rays64[:, 6]
+    r["tmax"] = np.minimum(rays64[:, 7], np.finfo(np.float32).max)
+    return r
+
+
 def test_point_light_deterministic(cornell):
     d, ents, sc, o = cornell
     cam = camera_from(d, "rcam")
     lights = lights_from(d["point_lights"])
     rgba, rad = sc.render(cam, lights, 1, 1, 0.0, 1)
     ref = d["point_radiance"]
-    close = np.isclose(rad[..., :3], ref, rtol=1e-4, atol=1e-5).all(-1)
-    assert close.mean() > 0.99, close.mean()
-    # a pixel whose shadow ray grazes an edge may flip between lit and shadowed: image mean 0.5 %
+    orad, _, _ = o.render(cam, lights, 1, 1, 0.0, 1)
+    np.testing.assert_allclose(orad[..., :3], ref, rtol=1e-6, atol=1e-6)
+    direct_parity(sc, o, cam, lights, rad, orad, "Cornell point-light render")
     assert abs(rad[..., :3].mean() / ref.mean() - 1) < 5e-3
     assert (rad[..., 3] == 1).all()
     # quantisation: clamp(v * 256, 0, 255) truncated to uint8 (do_render.hpp:118-134)
@@ -52,10 +85,8 @@ def test_same_seed_matches_oracle(cornell):
     cam = dict(camera_from(d, "rcam"), resolution=[32, 32])
     lights = lights_from(d["lights"])
     _, rad = sc.render(cam, lights, 8, 8, 0.0, 3, seed=5)
-    orad, _, _ = o.render(cam, lights, 8, 8, 0.0, 3, seed=5)
-    rel = np.abs(rad[..., :3] - orad[..., :3]) / np.maximum(np.abs(orad[..., :3]), 1e-3)
-    assert (rel < 1e-3).mean() > 0.9, (rel < 1e-3).mean()
-    assert abs(rad[..., :3].mean() / orad[..., :3].mean() - 1) < 0.01
+    orad, _, _, m2 = o.render(cam, lights, 8, 8, 0.0, 3, seed=5, with_m2=True)
+    check_mc_radiance(rad, orad, m2, 8, what="same seed, 8 spp")
 
 
 def test_area_light_statistics_vs_reference(cornell):
@@ -67,7 +98,7 @@ def test_area_light_statistics_vs_reference(cornell):
     mask = ~((ids == 1) & (xyz[..., 1] > 0.94)) & (ids != 6) & (ids > 0)
     ref, m2 = d["render_mean"], d["render_m2"]
     z = radiance_stats_ok(rad[..., :3], m2, spp, ref, m2, spp, mask=np.repeat(mask[..., None], 3, -1))
-    assert (z > 4).mean() < 0.01, (z > 4).mean()
+    assert (z > 4).mean() <= 1e-3, (z > 4).mean()
     ours, theirs = rad[..., :3][mask].mean(), ref[mask].mean()
     assert abs(ours / theirs - 1) < 0.005, (ours, theirs)
 
@@ -77,11 +108,9 @@ def test_adaptive_sampling_matches_oracle(cornell):
     cam = dict(camera_from(d, "rcam"), resolution=[24, 24])
     lights = lights_from(d["lights"])
     _, rad = sc.render(cam, lights, 2, 32, 2.0, 2, seed=9)
-    orad, _, taken = o.render(cam, lights, 2, 32, 2.0, 2, seed=9)
-    # the same random streams stop most pixels after the same sample
+    orad, _, taken, m2 = o.render(cam, lights, 2, 32, 2.0, 2, seed=9, with_m2=True)
     assert taken.min() >= 2 and taken.max() <= 32 and (taken < 32).any()
-    close = np.isclose(rad[..., :3], orad[..., :3], rtol=2e-3, atol=1e-3).all(-1)
-    assert close.mean() > 0.9, close.mean()
+    check_mc_radiance(rad, orad, m2, taken, what="adaptive sampling")
 
 
 @pytest.mark.parametrize("res,spp,thr", [((37, 23), (4, 4), 0.0), ((29, 19), (2, 16), 2.0), ((5, 3), (3, 3), 0.0)])
@@ -92,10 +121,9 @@ def test_odd_resolutions_match_oracle(cornell, res, spp, thr):
     cam = dict(camera_from(d, "rcam"), resolution=list(res))
     lights = lights_from(d["lights"])
     _, rad = sc.render(cam, lights, spp[0], spp[1], thr, 2, seed=7)
-    orad, _, _ = o.render(cam, lights, spp[0], spp[1], thr, 2, seed=7)
+    orad, _, taken, m2 = o.render(cam, lights, spp[0], spp[1], thr, 2, seed=7, with_m2=True)
     assert rad.shape == (res[1], res[0], 4) and (rad[..., 3] == 1).all()
-    close = np.isclose(rad[..., :3], orad[..., :3], rtol=2e-3, atol=1e-3).all(-1)
-    assert close.mean() > 0.9, close.mean()
+    check_mc_radiance(rad, orad, m2, taken, what=f"{res[0]}x{res[1]}")
 
 
 def test_multiple_lights_and_no_bounce(cornell):
@@ -103,8 +131,8 @@ def test_multiple_lights_and_no_bounce(cornell):
     cam = dict(camera_from(d, "rcam"), resolution=[16, 16])
     lights = lights_from(d["lights"]) + lights_from(d["point_lights"])
     _, rad = sc.render(cam, lights, 4, 4, 0.0, 2, seed=3)
-    orad, _, _ = o.render(cam, lights, 4, 4, 0.0, 2, seed=3)
-    assert abs(rad[..., :3].mean() / orad[..., :3].mean() - 1) < 0.01
+    orad, _, _, m2 = o.render(cam, lights, 4, 4, 0.0, 2, seed=3, with_m2=True)
+    check_mc_radiance(rad, orad, m2, 4, what="area + point lights")
     rgba, rad0 = sc.render(cam, lights, 1, 1, 0.0, 0)   # no bounce: black, alpha 1
     assert (rad0[..., :3] == 0).all() and (rgba[..., 3] == 255).all()
 
@@ -121,8 +149,8 @@ def test_asteroid_sun_render_vs_oracle(ctx):
     cam = scenes.fov_camera(scenes.TAN5 * 2.4, (128, 128), 5000.0 * view, (0.0, 0.0, 0.0))
     _, rad = sc.render(cam, lights, 1, 1, 1.0, 1)
     orad, _, _ = o.render(cam, lights, 1, 1, 1.0, 1)
-    close = np.isclose(rad[..., :3], orad[..., :3], rtol=1e-3, atol=1e-4).all(-1)
-    assert close.mean() > 0.98, close.mean()
+    st = direct_parity(sc, o, cam, lights, rad, orad, "100k asteroid sun render")
+    print("asteroid sun render", st)
     lit = orad[..., 0] > 0
     assert 0.2 < lit.mean() < 0.9
 
@@ -139,12 +167,13 @@ def test_open_quad_self_occlusion_matches_oracle(ctx):
     blocked = dict(type="point", intensity=3.0, position=[0.3, 2.0, 0.2])    # camera side: behind n's offset
     lit = dict(type="point", intensity=2.0, position=[-0.2, -2.0, 0.1])
     _, rad = sc.render(cam, [blocked], 1, 1, 0.0, 1)
-    assert (rad[..., :3] == 0).mean() > 0.995, (rad[..., :3] != 0).mean()
+    orad, _, _ = o.render(cam, [blocked], 1, 1, 0.0, 1)
+    assert (orad[..., :3] == 0).all()
+    direct_parity(sc, o, cam, [blocked], rad, orad, "open quad, light behind the offset side")
     _, rad2 = sc.render(cam, [blocked, lit], 1, 1, 0.0, 1)
     orad2, _, _ = o.render(cam, [blocked, lit], 1, 1, 0.0, 1)
     assert (orad2[..., 0] > 0).mean() > 0.3
-    close = np.isclose(rad2[..., :3], orad2[..., :3], rtol=1e-4, atol=1e-6).all(-1)
-    assert close.mean() > 0.995, close.mean()
+    direct_parity(sc, o, cam, [blocked, lit], rad2, orad2, "open quad, two lights")
     # counting build: the blocked light's shadow rays are not traced (at most an edge band is)
     ctx.set_counting(True)
     try:
@@ -186,8 +215,7 @@ def test_terminator_shadow_rays_resolved_in_shade(ctx):
 def test_smooth_shaded_two_bounce_render_vs_oracle(ctx):
     """Smooth-shaded asteroid, 2 bounces, the oracle's random streams: bounce directions sampled about
     the interpolated normal can point into the flat surface they leave (the reference then meets its
-    own triangle again); per-pixel radiance still agrees on nearly all pixels and the image mean
-    within 1 %."""
+    own triangle again); per-pixel radiance within 4 sigma, image mean within 0.5 %."""
     ents = [scenes.EntitySpec("a", scenes.asteroid(100_000, seed=3), (0.3, 0.3, 0.3), smooth=True)]
     sc, o = ctx.scene(ents), oracle.Scene(ents)
     view = scenes.unit_vector(21)
@@ -196,8 +224,6 @@ def test_smooth_shaded_two_bounce_render_vs_oracle(ctx):
     lights = [dict(type="point", intensity=1.0e18, position=1.0e9 * sun)]
     cam = scenes.fov_camera(scenes.TAN5 * 2.4, (48, 48), 5000.0 * view, (0.0, 0.0, 0.0))
     _, rad = sc.render(cam, lights, 4, 4, 0.0, 2, seed=11)
-    orad, _, _ = o.render(cam, lights, 4, 4, 0.0, 2, seed=11)
+    orad, _, _, m2 = o.render(cam, lights, 4, 4, 0.0, 2, seed=11, with_m2=True)
     assert (orad[..., 0] > 0).mean() > 0.5
-    close = np.isclose(rad[..., :3], orad[..., :3], rtol=2e-3, atol=1e-3).all(-1)
-    assert close.mean() > 0.95, close.mean()
-    assert abs(rad[..., :3].mean() / orad[..., :3].mean() - 1) < 0.01
+    check_mc_radiance(rad, orad, m2, 4, what="smooth-shaded 2-bounce asteroid")

@@ -82,8 +82,13 @@ def test_spacecraft_vs_oracle(ctx):
         assert np.linalg.norm(f[a] - of) <= 1e-4 * np.linalg.norm(of)
         assert np.linalg.norm(t[a] - ot) <= 1e-4 * max(np.linalg.norm(ot), 1e-3 * np.linalg.norm(of))
         assert abs(fp[a].sum() / ofp.sum() - 1) < 1e-4
-        hitf = ofp > 0
-        assert (np.abs(fp[a] - ofp)[hitf] <= 0.05 * ofp[hitf] + 1e-9).mean() > 0.95
+        # per facet: a ray through an edge shared by two facets may land on either; each such ray
+        # moves at most its power (flux x cell area) and that of its specular continuation
+        e_ray = 1361.0 * (2 * srp_params(stats, sb, 384, 2, cm).half_extent / 384) ** 2
+        excess = np.abs(fp[a] - ofp) - 1e-4 * ofp
+        print(f"attitude {a}: max facet diff / ray power {np.abs(fp[a] - ofp).max() / e_ray:.2f}, "
+              f"facets beyond 1e-4 {(excess > 0).sum()}")
+        assert (excess <= 2 * e_ray).all()
 
 
 def test_reduction_is_deterministic(ctx):
