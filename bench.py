@@ -51,8 +51,8 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-served", action="store_true")
-    ap.add_argument("--served-seconds", type=float, default=10.0,
-                    help="length of the Poisson request stream (the configuration states 60 s)")
+    ap.add_argument("--served-seconds", type=float, default=60.0,
+                    help="length of the Poisson request stream (the configuration's 60 s)")
     ap.add_argument("--served-rate", type=float, default=200.0)
     ap.add_argument("--served-lanes", type=int, default=4)
     ap.add_argument("--served-wave-paths", type=int, default=1 << 22)
@@ -61,7 +61,8 @@ def parse():
     ap.add_argument("--no-cornell", action="store_true")
     ap.add_argument("--srp-attitudes", type=int, default=256)
     ap.add_argument("--probe", type=int, default=0,
-                    help="profiling aid: only run the --probe-kind workload this many times")
+                    help="profiling aid (the commands of the ncu summaries under profiles/ run it): only run "
+                         "the --probe-kind workload this many times")
     ap.add_argument("--probe-kind", default="closest", choices=["closest", "batched", "srp"],
                     help="closest: crt_trace_closest on the 2048^2 primary rays; batched: one crt_batch of the "
                          "64-request mix; srp: 8 attitudes x 4096^2 rays x 2 bounces with per-facet flux")
@@ -69,8 +70,9 @@ def parse():
 
 
 def probe(args):
-    """Small profiling case: the 2M-triangle asteroid resident (about 330 MB with the rays, larger than
-    L2) and `--probe` launches of crt_trace_closest on the 2048^2 primary camera rays."""
+    """Profiling aid used by the commands of the ncu summaries under profiles/: the 2M-triangle asteroid
+    resident (about 330 MB with the rays, larger than L2) and `--probe` launches of crt_trace_closest on
+    the 2048^2 primary camera rays (or of the batched mix / SRP batch, --probe-kind)."""
     import torch
     from crt_gb300 import build, lib, workloads
     build.build()
@@ -216,33 +218,41 @@ def measured_peak():
     return 6800.0, "fallback"
 
 
-def profiled_traffic():
-    """dram bytes per launch of the primary trace kernel, from the committed ncu summary."""
-    path = os.path.join(REPO, "profiles", "trace_closest_asteroid2M.md")
+PROFILE = os.path.join("profiles", "trace_closest_asteroid2M.md")
+
+
+def profiled_counters():
+    """Per-launch counters of the primary trace kernel on the bench's rays from the committed ncu
+    summary (its `key = value` lines): dram_bytes, lts_bytes, warp_inst, issue_active_pct, rays.  ncu
+    cannot run inside the timed bench, so these are the capture's figures for the same kernel, BVH and
+    rays; bench.py divides them by the kernel time it measures."""
+    path = os.path.join(REPO, PROFILE)
+    out = {}
     if not os.path.exists(path):
-        return None
+        return out
     for line in open(path):
-        if "dram_bytes_per_launch_full" in line and "=" in line:
+        line = line.strip().strip("`")
+        if line.startswith("counter ") and "=" in line:
+            k, v = line[len("counter "):].split("=", 1)
             try:
-                return float(line.split("=")[1].replace("|", " ").split()[0])
+                out[k.strip()] = float(v.split()[0])
             except (IndexError, ValueError):
-                return None
-    return None
+                pass
+    return out
 
 
-def lidar_rays64(lid):
-    """FP64 beam rays of a LiDAR grid (same construction as crt_lidar_grid)."""
-    nx, ny = lid["nx"], lid["ny"]
-    tx = np.tan(-lid["half_x"] + (np.arange(nx) + 0.5) * 2 * lid["half_x"] / nx)
-    ty = np.tan(-lid["half_y"] + (np.arange(ny) + 0.5) * 2 * lid["half_y"] / ny)
-    s = np.stack(np.broadcast_arrays(tx[None, :], ty[:, None], -np.ones((ny, nx))), -1).reshape(-1, 3)
-    s /= np.linalg.norm(s, axis=1)[:, None]
-    d = s @ np.asarray(lid["rotation"])
-    rays = np.zeros((nx * ny, 8))
-    rays[:, 0:3] = lid["position"]
-    rays[:, 3:6] = d
-    rays[:, 7] = np.finfo(np.float64).max
-    return rays
+def read_peaks(ctx, dev):
+    """Streaming-read bandwidth measured here with the library's read kernel (crt_measure_read):
+    a 48 MiB buffer that stays in L2 after the first pass, and a 4 GiB buffer from HBM.  GB/s."""
+    import torch
+    small = torch.ones(48 << 20, dtype=torch.uint8, device=dev)
+    ms_l2 = ctx.measure_read(small, reps=200)
+    big = torch.ones(4 << 30, dtype=torch.uint8, device=dev)
+    ms_hbm = ctx.measure_read(big, reps=10)
+    out = {"l2_read_gbs": round(small.numel() / ms_l2 / 1e6, 1), "hbm_read_gbs": round(big.numel() / ms_hbm / 1e6, 1)}
+    del small, big
+    torch.cuda.empty_cache()
+    return out
 
 
 # ------------------------------------------------------------------ CPU (oracle port) timing
@@ -255,7 +265,8 @@ def cpu_measure(ents, cfg, budget_s):
     build_s = time.perf_counter() - t0
     cam, lights = cfg["camera"], cfg["lights"]
     W, H = int(cam["resolution"][0]), int(cam["resolution"][1])
-    lid_rays = lidar_rays64(cfg["lidar"])
+    from crt_gb300 import workloads
+    lid_rays = workloads.lidar_grid_rays(cfg["lidar"])
     # probe: 16 rows of the image + 1/64 of the beams, then scale the sample to ~budget_s
     rows = 16
     t = time.perf_counter()
@@ -394,6 +405,18 @@ def gpu_arm(args):
     if world > 1:
         torch.distributed.barrier()
     clk = clocks.stop()
+    # the K-step window is short (tens of ms); clocks over ~2 s of the same step, right after it
+    sustained = ClockSampler(local)
+    sustained.start()
+    t_s = time.perf_counter()
+    with torch.cuda.stream(stream):
+        while time.perf_counter() - t_s < 2.0:
+            for _ in range(20):
+                flush.zero_()
+                render()
+                scan()
+            torch.cuda.synchronize()
+    clk_sustained = sustained.stop()
     lat_render = [a.elapsed_time(b) for a, b, c in ev]
     lat_lidar = [b.elapsed_time(c) for a, b, c in ev]
     step_ms = [a.elapsed_time(c) for a, b, c in ev]
@@ -424,12 +447,29 @@ def gpu_arm(args):
     b_ray = NODE_BYTES * nodes_ray + TRI_BYTES * tris_ray + RAY_BYTES + HIT_BYTES
     achieved = b_ray * cnt["rays"] / t_kernel / 1e9
     peak, peak_kind = measured_peak()
-    traffic = profiled_traffic()
+    pk = read_peaks(ctx, dev)
+    prof = profiled_counters()
     roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-            "frac": round(achieved / peak, 4), "traffic": traffic, "peak_source": peak_kind,
+            "frac": round(achieved / peak, 4), "traffic": prof.get("dram_bytes"), "peak_source": peak_kind,
             "kernel": "k_trace<closest> on 2048^2 primary camera rays in 8x4 tiles (crt_trace_closest)",
             "bytes_per_ray": round(b_ray, 1), "nodes_per_ray": round(nodes_ray, 2), "tris_per_ray": round(tris_ray, 2),
-            "kernel_ms": round(t_kernel * 1e3, 3), "kernel_mrays_s": round(cnt["rays"] / t_kernel / 1e6, 1)}
+            "kernel_ms": round(t_kernel * 1e3, 3), "kernel_mrays_s": round(cnt["rays"] / t_kernel / 1e6, 1),
+            "frac_note": "algorithmic bytes (80 B per node and 48 B per triangle fetched, 48 B ray + hit) over "
+                         "the measured HBM copy bandwidth; most are served from L1 / L2, see dram_frac / l2_frac",
+            "read_peaks_gbs": pk}
+    if prof.get("dram_bytes") and prof.get("lts_bytes"):
+        # the ncu capture's bytes for one launch of this kernel on these rays, over the time measured here
+        dram_gbs = prof["dram_bytes"] / t_kernel / 1e9
+        l2_gbs = prof["lts_bytes"] / t_kernel / 1e9
+        roof.update(traffic_source="ncu capture of the same kernel, BVH and rays (" + PROFILE + ", counters "
+                                   "dram__bytes_read.sum + dram__bytes_write.sum, lts__t_bytes.sum) over the "
+                                   "kernel time measured in this run",
+                    dram_gbs=round(dram_gbs, 1), dram_frac=round(dram_gbs / pk["hbm_read_gbs"], 4),
+                    l2_gbs=round(l2_gbs, 1), l2_frac=round(l2_gbs / pk["l2_read_gbs"], 4))
+    if prof.get("warp_inst") and prof.get("rays"):
+        roof.update(warp_inst_per_32_rays=round(prof["warp_inst"] / (prof["rays"] / 32.0), 1),
+                    issue_active_pct=prof.get("issue_active_pct"),
+                    binding="SM instruction issue (ncu issue-active % above; DRAM and L2 fractions low)")
 
     # ---- batched vs per-call on the config-3 request set
     batched = None
@@ -469,7 +509,8 @@ def gpu_arm(args):
                                "lidar_p99": round(percentile(lat_lidar, 99), 3),
                                "step_p50": round(percentile(step_ms, 50), 3),
                                "step_max": round(max(step_ms), 3)},
-                "roofline": roof, "gpu_launches": int(launches), "clocks": clk, "e2e": e2e, "batched": batched,
+                "roofline": roof, "gpu_launches": int(launches), "clocks": clk,
+                "clocks_sustained": clk_sustained, "e2e": e2e, "batched": batched,
                 "served": served, "srp": srp, "cornell": cornell}
         if world == 1 and not args.no_cpu:
             mr, det = cpu_measure(ents, cfg, args.cpu_seconds)
@@ -751,9 +792,12 @@ def served_measure(args, device):
            "rays": rays, "offered_mrays_s": round(rays / args.served_seconds / 1e6, 1),
            "lanes": args.served_lanes, "lane_budget_mib": args.served_budget_mib,
            "wave_paths": args.served_wave_paths,
-           "open_loop": {"served": dict(summary(lat_s, span_s), waves=nb_s, clocks=clk_s),
+           "open_loop": {"kind": "latency: requests submitted at their Poisson arrival times, so mrays_s is "
+                                 "the offered load, not a throughput figure",
+                         "served": dict(summary(lat_s, span_s), waves=nb_s, clocks=clk_s),
                          "per_call": dict(summary(lat_p, span_p), clocks=clk_p)},
-           "closed_loop": {"served": dict(summary(clat_s, cspan_s), waves=cnb_s, clocks=cclk_s),
+           "closed_loop": {"kind": "throughput: every request submitted at once, makespan Mrays/s",
+                           "served": dict(summary(clat_s, cspan_s), waves=cnb_s, clocks=cclk_s),
                            "per_call": dict(summary(clat_p, cspan_p), clocks=cclk_p),
                            "speedup": round(cspan_p / cspan_s, 3)},
            "body_generation_s": round(t_gen, 1)}
@@ -848,6 +892,22 @@ def srp_measure(args, ctx, stream):
             b.record(stream)
             torch.cuda.synchronize()
             res[facet] = a.elapsed_time(b) / 1e3
+        # the allocation-free entry point on the first 16 attitudes, beside crt_srp on the same ones
+        ns = min(16, n)
+        qh = np.ascontiguousarray(cfg["quaternions"][:ns])
+        fs = torch.empty((ns, 3), dtype=torch.float64, device=q.device)
+        ts = torch.empty((ns, 3), dtype=torch.float64, device=q.device)
+        sc.srp_static_into(cfg["sun"], qh, cfg["grid"], fs, ts, num_bounces=cfg["num_bounces"])   # warm-up
+        st_ms = {}
+        for name, fn in (("crt_srp", lambda: sc.srp_into(cfg["sun"], qh, cfg["grid"], fs, ts,
+                                                         num_bounces=cfg["num_bounces"])),
+                         ("crt_srp_static", lambda: sc.srp_static_into(cfg["sun"], qh, cfg["grid"], fs, ts,
+                                                                       num_bounces=cfg["num_bounces"]))):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            fn()
+            torch.cuda.synchronize()
+            st_ms[name] = (time.perf_counter() - t0) * 1e3 / ns
     sc.close()
     return {"workload": "SRP batch: spacecraft %d triangles, %d attitudes x %d^2 sun rays, %d bounces"
                         % (n_tris, n, cfg["grid"], cfg["num_bounces"]),
@@ -856,7 +916,9 @@ def srp_measure(args, ctx, stream):
             "rays_note": "sun rays of the grids (traced, or resolved as misses by the scene-box test) + "
                          "specular continuations traced",
             "ms": round(res[True] * 1e3, 2), "ms_without_facet_power": round(res[False] * 1e3, 2),
-            "ms_per_attitude": round(res[True] * 1e3 / n, 3), "nodes_per_ray": round(cnt["nodes"] / cnt["rays"], 2)}
+            "ms_per_attitude": round(res[True] * 1e3 / n, 3), "nodes_per_ray": round(cnt["nodes"] / cnt["rays"], 2),
+            "static_vs_allocating": {"attitudes": ns, "host_quaternions_device_outputs": True,
+                                     "wall_ms_per_attitude": {k: round(v, 3) for k, v in st_ms.items()}}}
 
 
 def tile_order(W, H):
@@ -876,10 +938,10 @@ def tile_order(W, H):
 
 def scenes_camera_rays(cam):
     """FP32 camera rays in crt_ray layout (o.xyz, tmin, d.xyz, tmax) as an [n, 8] float32 array in the
-    render path's 8 x 4 tile order, for the roofline probe (the oracle's FP64 rays are laid out
-    o.xyz, d.xyz, tmin, tmax, one per pixel in row-major order)."""
-    import oracle
-    r64 = oracle.camera_rays(cam)[tile_order(int(cam["resolution"][0]), int(cam["resolution"][1]))]
+    render path's 8 x 4 tile order, for the roofline probe (workloads.camera_rays gives FP64 rays laid
+    out o.xyz, d.xyz, tmin, tmax, one per pixel in row-major order)."""
+    from crt_gb300 import workloads
+    r64 = workloads.camera_rays(cam)[tile_order(int(cam["resolution"][0]), int(cam["resolution"][1]))]
     r = np.empty((r64.shape[0], 8), dtype=np.float32)
     r[:, 0:3] = r64[:, 0:3]
     r[:, 3] = 0.0

@@ -119,6 +119,7 @@ SIGNATURES = {
     "crt_context_set_stream": ([vp, vp], i32),
     "crt_context_get_stream": ([vp], vp),
     "crt_context_synchronize": ([vp], i32),
+    "crt_measure_read": ([vp, vp, sz, u32, ctypes.POINTER(dbl)], i32),
     "crt_context_set_counting": ([vp, i32], i32),
     "crt_context_get_counters": ([vp, ctypes.POINTER(Counters)], i32),
     "crt_context_reset_counters": ([vp], i32),
@@ -264,6 +265,14 @@ class Context:
 
     def synchronize(self):
         self._check(self.L.crt_context_synchronize(self.h))
+
+    def measure_read(self, buf, reps=20):
+        """Mean device time (ms) of one streaming read of a device buffer (a torch tensor or a pointer
+        with .nbytes): crt_measure_read."""
+        ms = dbl()
+        nbytes = buf.numel() * buf.element_size() if hasattr(buf, "numel") else buf.nbytes
+        self._check(self.L.crt_measure_read(self.h, ptr(buf), nbytes, int(reps), ctypes.byref(ms)))
+        return ms.value
 
     def set_counting(self, on):
         self._check(self.L.crt_context_set_counting(self.h, int(bool(on))))
@@ -492,6 +501,18 @@ class Scene:
         n = int(quaternions.shape[0])
         self.ctx._check(self.ctx.L.crt_srp(self.h, ctypes.byref(d), ptr(quaternions), n, ptr(force), ptr(torque),
                                            ptr(facet_power)))
+
+    def srp_static_into(self, sun_dir, quaternions, grid, force, torque, num_bounces=2, flux=1361.0, c=299792458.0,
+                        center_of_mass=(0, 0, 0)):
+        """crt_srp_static (no device allocation; static scratch) with caller buffers, as srp_into."""
+        d = SrpDesc()
+        d.sun_dir_inertial[:] = [float(x) for x in sun_dir]
+        d.flux, d.c = float(flux), float(c)
+        d.center_of_mass[:] = [float(x) for x in center_of_mass]
+        d.grid, d.num_bounces = int(grid), int(num_bounces)
+        n = int(quaternions.shape[0])
+        self.ctx._check(self.ctx.L.crt_srp_static(self.h, ctypes.byref(d), ptr(quaternions), n, ptr(force),
+                                                  ptr(torque)))
 
 
 def make_rays(o, d, tmin=0.0, tmax=3.4e38):

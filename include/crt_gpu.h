@@ -273,6 +273,13 @@ int crt_srp(crt_scene* scene, const crt_srp_desc* desc, const double* quaternion
 int crt_srp_static(crt_scene* scene, const crt_srp_desc* desc, const double* quaternions, size_t n_att,
                    double* force, double* torque);
 
+/* Read bandwidth of the context's GPU (no counterpart in the reference; a measurement aid for the
+ * roofline of the traversal kernels): reads the `bytes` (>= 16) of the 16-byte aligned device buffer
+ * `buf` `reps` times with 16-byte loads that bypass L1 and returns the mean device time of one pass
+ * in ms (CUDA events on the context stream, after one untimed pass).  A buffer well inside the L2
+ * cache measures L2 read bandwidth, one much larger than L2 measures HBM read bandwidth. */
+int crt_measure_read(crt_context* ctx, const void* buf, size_t bytes, uint32_t reps, double* ms_per_pass);
+
 /* Page-locked host memory for outputs (no counterpart in the reference): device-to-host copies
  * into such buffers run at the full host link rate instead of through a pageable bounce buffer.
  * The pybind11 module hands its result arrays out of a pool of these. */
