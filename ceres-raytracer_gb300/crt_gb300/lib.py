@@ -72,7 +72,7 @@ class BatchStats(ctypes.Structure):
 
 class Tuning(ctypes.Structure):
     _fields_ = [("queue_chunk", u32), ("wave_paths", u32), ("use_graphs", i32), ("build_sah", i32),
-                ("collapse_tri_cost", ctypes.c_float)]
+                ("collapse_tri_cost", ctypes.c_float), ("treelet_passes", u32)]
 
 
 REQUEST_RENDER, REQUEST_LIDAR, REQUEST_SRP = 0, 1, 2
@@ -290,16 +290,18 @@ class Context:
     def scene(self, entities):
         return Scene(self, entities)
 
-    def set_tuning(self, queue_chunk=1, wave_paths=1 << 23, use_graphs=True, build_sah=True, collapse_tri_cost=0.15):
+    def set_tuning(self, queue_chunk=1, wave_paths=1 << 23, use_graphs=True, build_sah=True, collapse_tri_cost=0.15,
+                   treelet_passes=2):
         t = Tuning(int(queue_chunk), int(wave_paths), int(bool(use_graphs)), int(bool(build_sah)),
-                   float(collapse_tri_cost))
+                   float(collapse_tri_cost), int(treelet_passes))
         self._check(self.L.crt_context_set_tuning(self.h, ctypes.byref(t)))
 
     def get_tuning(self):
         t = Tuning()
         self._check(self.L.crt_context_get_tuning(self.h, ctypes.byref(t)))
         return dict(queue_chunk=t.queue_chunk, wave_paths=t.wave_paths, use_graphs=bool(t.use_graphs),
-                    build_sah=bool(t.build_sah), collapse_tri_cost=round(float(t.collapse_tri_cost), 4))
+                    build_sah=bool(t.build_sah), collapse_tri_cost=round(float(t.collapse_tri_cost), 4),
+                    treelet_passes=int(t.treelet_passes))
 
     def batch(self, requests, outputs=None):
         """Run render / LiDAR / SRP requests in one batch.  Each request is a dict:

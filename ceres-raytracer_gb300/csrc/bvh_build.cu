@@ -359,7 +359,7 @@ __device__ __forceinline__ void dp_child(const float* __restrict__ dp, int ref, 
 __global__ void k_refit(const uint32_t* __restrict__ sorted, const float4* __restrict__ tbox, int n,
                         const int2* __restrict__ child, const int* __restrict__ parent, float4* nbox,
                         uint32_t* __restrict__ flags, const int2* __restrict__ range, float* __restrict__ dp,
-                        float cost_tri) {
+                        float cost_tri, uint32_t* __restrict__ err) {
     int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n) return;
     const uint32_t p = sorted[j];
@@ -367,7 +367,11 @@ __global__ void k_refit(const uint32_t* __restrict__ sorted, const float4* __res
     nbox[2ull * (n - 1 + j)] = lo;
     nbox[2ull * (n - 1 + j) + 1] = hi;
     int node = parent[n - 1 + j];
-    while (node >= 0) {
+    for (int steps = 0; node >= 0; ++steps) {
+        if (steps >= 1024) {   // deeper than any tree built here, or damaged links: report, do not loop
+            atomicOr(err, (uint32_t)DEVERR_BUILD_OVERFLOW);
+            return;
+        }
         __threadfence();
         if (atomicAdd(&flags[node], 1u) == 0) return;   // first arrival: the sibling finishes the union
         const int2 c = child[node];
@@ -398,6 +402,284 @@ __global__ void k_refit(const uint32_t* __restrict__ sorted, const float4* __res
             __stcg(out, fminf(c_int, c_leaf));
         }
         node = parent[node];
+    }
+}
+
+// ---------------------------------------------------------------- treelet restructuring
+// Tree optimisation after the topology build, in place of the reference's parallel reinsertion
+// (ParallelReinsertionOptimizer::optimize, parallel_reinsertion_optimizer.hpp:140-211): treelet
+// restructuring after Karras and Aila, "Fast parallel construction of high-quality bounding volume
+// hierarchies" (HPG 2013).  A treelet is a node R with up to TL_LEAVES descendants as leaves, grown
+// from R's two children by repeatedly opening the leaf of largest surface area; its internal nodes
+// are rebuilt into the topology of least summed surface area (the surface-area cost with the leaf
+// subtrees fixed: their costs are the same in every topology), found by a dynamic program over the
+// 2^7 - 1 subsets of leaves, one warp per treelet.  Node indices, boxes of R and everything outside
+// the treelet stay; only child / parent links of its internal nodes and their boxes change.
+// Treelets of one launch must not share nodes: a launch takes the roots whose depth is = r (mod 7),
+// and a treelet from depth d holds internal nodes at depths d .. d + 5 and leaves at depths up to
+// d + 6, so two roots 7 or more levels apart, or in disjoint subtrees, touch disjoint nodes.  Depths
+// are recomputed before every launch.  Afterwards k_tl_count / k_tl_position / k_tl_relayout renumber
+// the leaves in depth-first order, so every subtree is again a contiguous range of sorted positions
+// (what the refit and the 8-wide collapse read).
+constexpr int TL_LEAVES = 7;
+constexpr int TL_WARPS = 4;
+
+__device__ __forceinline__ size_t tl_index(int n, int ref) { return ref >= 0 ? (size_t)ref : (size_t)(n - 1 + ~ref); }
+
+// depth of every internal node (root 0), by walking up the parent links
+__global__ void k_tl_depth(const int* __restrict__ parent, int n, uint8_t* __restrict__ depth) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n - 1) return;
+    int d = 0, node = i;
+    while (true) {
+        const int p = parent[node];
+        if (p < 0 || d >= 255) break;
+        node = p;
+        ++d;
+    }
+    depth[i] = (uint8_t)d;
+}
+
+__global__ void __launch_bounds__(32 * TL_WARPS) k_treelet(int2* __restrict__ child, int* __restrict__ parent,
+                                                          float4* __restrict__ nbox,
+                                                          const uint8_t* __restrict__ depth, int n, int cls,
+                                                          uint32_t* __restrict__ stats) {
+    __shared__ float s_area[TL_WARPS][128];
+    __shared__ float s_cost[TL_WARPS][128];
+    __shared__ uint8_t s_part[TL_WARPS][128];
+    __shared__ float s_box[TL_WARPS][TL_LEAVES][6];
+    __shared__ int s_leaf[TL_WARPS][TL_LEAVES];
+    __shared__ int s_int[TL_WARPS][TL_LEAVES - 1];
+    __shared__ int s_nl[TL_WARPS];
+    __shared__ float s_old[TL_WARPS];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int warps = gridDim.x * TL_WARPS;
+    uint32_t improved = 0;
+    for (int R = blockIdx.x * TL_WARPS + w; R < n - 1; R += warps) {
+        if (depth[R] == 255 || (int)depth[R] % 7 != cls) continue;   // warp-uniform; 255: deeper than tracked
+        if (lane == 0) {
+            // grow the treelet: open the leaf of largest area that is an internal node
+            int leaf[TL_LEAVES], nl = 2, ni = 1;
+            float area[TL_LEAVES];
+            const int2 c = child[R];
+            leaf[0] = c.x;
+            leaf[1] = c.y;
+            s_int[w][0] = R;
+            float old = box_area(nbox[2 * (size_t)R], nbox[2 * (size_t)R + 1]);
+            for (int k = 0; k < 2; ++k) area[k] = leaf[k] >= 0 ? box_area(nbox[2 * tl_index(n, leaf[k])], nbox[2 * tl_index(n, leaf[k]) + 1]) : -1.f;
+            while (nl < TL_LEAVES) {
+                int best = -1;
+                float ba = -1.f;
+                for (int k = 0; k < nl; ++k)
+                    if (leaf[k] >= 0 && area[k] > ba) { ba = area[k]; best = k; }
+                if (best < 0) break;
+                const int L = leaf[best];
+                s_int[w][ni++] = L;
+                old += ba;
+                const int2 cc = child[L];
+                leaf[best] = cc.x;
+                leaf[nl] = cc.y;
+                area[best] = cc.x >= 0 ? box_area(nbox[2 * tl_index(n, cc.x)], nbox[2 * tl_index(n, cc.x) + 1]) : -1.f;
+                area[nl] = cc.y >= 0 ? box_area(nbox[2 * tl_index(n, cc.y)], nbox[2 * tl_index(n, cc.y) + 1]) : -1.f;
+                ++nl;
+            }
+            for (int k = 0; k < nl; ++k) {
+                s_leaf[w][k] = leaf[k];
+                const size_t bi = tl_index(n, leaf[k]);
+                const float4 lo = nbox[2 * bi], hi = nbox[2 * bi + 1];
+                s_box[w][k][0] = lo.x; s_box[w][k][1] = lo.y; s_box[w][k][2] = lo.z;
+                s_box[w][k][3] = hi.x; s_box[w][k][4] = hi.y; s_box[w][k][5] = hi.z;
+            }
+            s_nl[w] = nl;
+            s_old[w] = old;
+        }
+        __syncwarp();
+        const int nl = s_nl[w];
+        if (nl < 3) {
+            __syncwarp();
+            continue;
+        }
+        const uint32_t full = (1u << nl) - 1u;
+        // surface area of the union of each subset's boxes
+        for (uint32_t S = lane + 1; S <= full; S += 32) {
+            float lo[3] = {3.0e38f, 3.0e38f, 3.0e38f}, hi[3] = {-3.0e38f, -3.0e38f, -3.0e38f};
+            for (int k = 0; k < nl; ++k)
+                if ((S >> k) & 1u)
+                    for (int a = 0; a < 3; ++a) {
+                        lo[a] = fminf(lo[a], s_box[w][k][a]);
+                        hi[a] = fmaxf(hi[a], s_box[w][k][3 + a]);
+                    }
+            const float dx = hi[0] - lo[0], dy = hi[1] - lo[1], dz = hi[2] - lo[2];
+            s_area[w][S] = dx * dy + dy * dz + dz * dx;
+            s_cost[w][S] = 0.f;
+        }
+        __syncwarp();
+        // cost of the best subtree over each subset, by subset size
+        for (int size = 2; size <= nl; ++size) {
+            for (uint32_t S = lane + 1; S <= full; S += 32) {
+                if (__popc(S) != size) continue;
+                const uint32_t low = S & (0u - S);
+                float best = 3.0e38f;
+                uint32_t bp = low;
+                for (uint32_t P = (S - 1) & S; P; P = (P - 1) & S) {
+                    if (!(P & low)) continue;
+                    const float c = s_cost[w][P] + s_cost[w][S ^ P];
+                    if (c < best) { best = c; bp = P; }
+                }
+                s_cost[w][S] = s_area[w][S] + best;
+                s_part[w][S] = (uint8_t)bp;
+            }
+            __syncwarp();
+        }
+        if (lane == 0 && s_cost[w][full] < s_old[w] * (1.0f - 1e-5f)) {
+            // rebuild: internal nodes reuse the treelet's indices (R stays the root)
+            uint32_t stk_s[TL_LEAVES], ord_s[TL_LEAVES];
+            int stk_n[TL_LEAVES], ord_n[TL_LEAVES];
+            int sp = 0, no = 0, next = 1;
+            stk_s[sp] = full;
+            stk_n[sp++] = R;
+            while (sp) {
+                --sp;
+                const uint32_t S = stk_s[sp];
+                const int node = stk_n[sp];
+                ord_s[no] = S;
+                ord_n[no++] = node;
+                const uint32_t P = s_part[w][S], Q = S ^ P;
+                int ch[2];
+                const uint32_t part[2] = {P, Q};
+                for (int k = 0; k < 2; ++k) {
+                    if (__popc(part[k]) == 1) {
+                        ch[k] = s_leaf[w][__ffs(part[k]) - 1];
+                    } else {
+                        ch[k] = s_int[w][next++];
+                        stk_s[sp] = part[k];
+                        stk_n[sp++] = ch[k];
+                    }
+                    parent[tl_index(n, ch[k])] = node;
+                }
+                child[node] = make_int2(ch[0], ch[1]);
+            }
+            // boxes of the rebuilt internal nodes (R's box is unchanged)
+            for (int k = 1; k < no; ++k) {
+                float lo[3] = {3.0e38f, 3.0e38f, 3.0e38f}, hi[3] = {-3.0e38f, -3.0e38f, -3.0e38f};
+                for (int j = 0; j < nl; ++j)
+                    if ((ord_s[k] >> j) & 1u)
+                        for (int a = 0; a < 3; ++a) {
+                            lo[a] = fminf(lo[a], s_box[w][j][a]);
+                            hi[a] = fmaxf(hi[a], s_box[w][j][3 + a]);
+                        }
+                nbox[2 * (size_t)ord_n[k]] = make_float4(lo[0], lo[1], lo[2], 0.f);
+                nbox[2 * (size_t)ord_n[k] + 1] = make_float4(hi[0], hi[1], hi[2], 0.f);
+            }
+            ++improved;
+        }
+        __syncwarp();
+    }
+    if (stats && lane == 0 && improved) atomicAdd(stats, improved);
+}
+
+// boxes only (the treelet pass reads node areas): second arrival at each node does the union
+// Every walk up the parent links below stops after TL_MAX_WALK steps with DEVERR_BUILD_OVERFLOW (a
+// binary tree this deep, or a damaged one, is reported instead of looping).
+constexpr int TL_MAX_WALK = 1024;
+
+__global__ void k_tl_boxes(const uint32_t* __restrict__ sorted, const float4* __restrict__ tbox, int n,
+                           const int2* __restrict__ child, const int* __restrict__ parent, float4* nbox,
+                           uint32_t* __restrict__ flags, uint32_t* __restrict__ err) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const uint32_t p = sorted[j];
+    nbox[2ull * (n - 1 + j)] = tbox[2ull * p];
+    nbox[2ull * (n - 1 + j) + 1] = tbox[2ull * p + 1];
+    int node = parent[n - 1 + j];
+    for (int steps = 0; node >= 0; ++steps) {
+        if (steps >= TL_MAX_WALK) {
+            atomicOr(err, (uint32_t)DEVERR_BUILD_OVERFLOW);
+            return;
+        }
+        __threadfence();
+        if (atomicAdd(&flags[node], 1u) == 0) return;
+        const int2 c = child[node];
+        const size_t a = tl_index(n, c.x), b = tl_index(n, c.y);
+        const float4 alo = __ldcg(&nbox[2 * a]), ahi = __ldcg(&nbox[2 * a + 1]);
+        const float4 blo = __ldcg(&nbox[2 * b]), bhi = __ldcg(&nbox[2 * b + 1]);
+        __stcg(&nbox[2ull * node], make_float4(fminf(alo.x, blo.x), fminf(alo.y, blo.y), fminf(alo.z, blo.z), 0.f));
+        __stcg(&nbox[2ull * node + 1], make_float4(fmaxf(ahi.x, bhi.x), fmaxf(ahi.y, bhi.y), fmaxf(ahi.z, bhi.z), 0.f));
+        node = parent[node];
+    }
+}
+
+// triangles under every internal node: second arrival at each node adds its children's counts
+__global__ void k_tl_count(int n, const int2* __restrict__ child, const int* __restrict__ parent,
+                           int* __restrict__ cnt, uint32_t* __restrict__ flags, uint32_t* __restrict__ err) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    int node = parent[n - 1 + j];
+    for (int steps = 0; node >= 0; ++steps) {
+        if (steps >= TL_MAX_WALK) {
+            atomicOr(err, (uint32_t)DEVERR_BUILD_OVERFLOW);
+            return;
+        }
+        __threadfence();
+        if (atomicAdd(&flags[node], 1u) == 0) return;
+        const int2 c = child[node];
+        const int a = c.x >= 0 ? __ldcg(&cnt[c.x]) : 1, b = c.y >= 0 ? __ldcg(&cnt[c.y]) : 1;
+        __stcg(&cnt[node], a + b);
+        node = parent[node];
+    }
+}
+
+// depth-first position of every node (internal: of its first leaf): the triangles of the left
+// siblings along the path to the root
+__global__ void k_tl_position(int n, const int2* __restrict__ child, const int* __restrict__ parent,
+                              const int* __restrict__ cnt, int* __restrict__ pos, uint32_t* __restrict__ err) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= 2 * n - 1) return;
+    int node = x, p = 0;
+    int ref = x < n - 1 ? x : ~(x - (n - 1));
+    for (int steps = 0;; ++steps) {
+        const int par = parent[node];
+        if (par < 0) break;
+        if (steps >= TL_MAX_WALK) {
+            atomicOr(err, (uint32_t)DEVERR_BUILD_OVERFLOW);
+            p = 0;
+            break;
+        }
+        const int2 c = child[par];
+        if (c.y == ref) p += c.x >= 0 ? cnt[c.x] : 1;
+        node = par;
+        ref = par;
+    }
+    pos[x] = p;
+}
+
+// renumber leaves by their depth-first position: sorted order, leaf references, leaf parents, ranges
+__global__ void k_tl_relayout(int n, const int* __restrict__ pos, const int* __restrict__ cnt,
+                              const uint32_t* __restrict__ sorted_in, uint32_t* __restrict__ sorted_out,
+                              int2* __restrict__ child, int2* __restrict__ range, const int* __restrict__ parent_in,
+                              int* __restrict__ leaf_parent_out, uint32_t* __restrict__ err) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {   // leaf at sorted position i moves to pos[n - 1 + i]
+        const int q = pos[n - 1 + i];
+        if (q < 0 || q >= n) {
+            atomicOr(err, (uint32_t)DEVERR_BUILD_OVERFLOW);
+        } else {
+            sorted_out[q] = sorted_in[i];
+            leaf_parent_out[q] = parent_in[n - 1 + i];
+        }
+    }
+    if (i < n - 1) {
+        int2 c = child[i];
+        const bool ok = (c.x >= 0 ? c.x < n - 1 : ~c.x < n) && (c.y >= 0 ? c.y < n - 1 : ~c.y < n) && cnt[i] >= 2 &&
+                        pos[i] >= 0 && pos[i] + cnt[i] <= n;
+        if (!ok) {
+            atomicOr(err, (uint32_t)DEVERR_BUILD_OVERFLOW);
+            return;
+        }
+        if (c.x < 0) c.x = ~pos[n - 1 + ~c.x];
+        if (c.y < 0) c.y = ~pos[n - 1 + ~c.y];
+        child[i] = c;
+        range[i] = make_int2(pos[i], pos[i] + cnt[i] - 1);
     }
 }
 
@@ -517,6 +799,10 @@ __global__ void k_collapse(CollapseArgs A, const int2* __restrict__ frontier, ui
         } else {
             cnt[k] = ref_count(A, refs[k]);
             first[k] = ref_first(A, refs[k]);
+            if (cnt[k] < 1 || first[k] < 0 || first[k] + cnt[k] > n) {   // damaged ranges: report, read nothing
+                atomicOr(A.err, (uint32_t)DEVERR_BUILD_OVERFLOW);
+                return;
+            }
             const size_t bi = box_index(n, refs[k]);
             const float4 a = A.nbox[2 * bi], b = A.nbox[2 * bi + 1];
             clo[k][0] = a.x; clo[k][1] = a.y; clo[k][2] = a.z;
@@ -1249,6 +1535,9 @@ void scene_build(crt_scene* s, const crt_entity_desc* ents, uint32_t n_ents) {
     uint32_t *hist = nullptr, *flags = nullptr, *keys = nullptr;
     int2 *child = nullptr, *range = nullptr, *front = nullptr, *front_b = nullptr;
     int* parent = nullptr;
+    uint8_t* tl_depth = nullptr;
+    int *tl_cnt = nullptr, *tl_pos = nullptr, *tl_par = nullptr;
+    uint32_t* tl_sorted = nullptr;
     const size_t nb_sort = (nn + SORT_TILE - 1) / SORT_TILE;
     auto carve = [&](char* base) {
         size_t off = 0;
@@ -1278,6 +1567,11 @@ void scene_build(crt_scene* s, const crt_entity_desc* ents, uint32_t n_ents) {
         keys = (uint32_t*)take(64 * 4);
         front = (int2*)take(nn * 8 + 8);
         front_b = (int2*)take(nn * 8 + 8);
+        tl_depth = (uint8_t*)take(nn);
+        tl_cnt = (int*)take(nn * 4);
+        tl_pos = (int*)take(nn * 8);          // 2n - 1 nodes
+        tl_par = (int*)take(nn * 4);
+        tl_sorted = (uint32_t*)take(nn * 4);
         return off;
     };
     const size_t total = carve(nullptr);
@@ -1317,8 +1611,33 @@ void scene_build(crt_scene* s, const crt_entity_desc* ents, uint32_t n_ents) {
             k_karras<<<cdiv(n - 1, BLOCK), BLOCK, 0, st>>>(ka, (int)n, child, range, parent);
             check_launch(ctx, "k_karras");
         }
+        if (sah && root_index >= 0 && ctx->treelet_passes > 0 && n >= 8) {
+            // treelet restructuring of the binary tree, then leaves renumbered depth-first
+            k_tl_boxes<<<cdiv(n, BLOCK), BLOCK, 0, st>>>(va, tbox, (int)n, child, parent, nbox, flags, ctx->d_error);
+            check_launch(ctx, "k_tl_boxes");
+            const uint32_t tl_grid = std::min<uint32_t>(cdiv(n - 1, TL_WARPS), (uint32_t)ctx->sm_count * 16);
+            for (uint32_t pass = 0; pass < ctx->treelet_passes; ++pass)
+                for (int cls = 0; cls < 7; ++cls) {
+                    k_tl_depth<<<cdiv(n - 1, BLOCK), BLOCK, 0, st>>>(parent, (int)n, tl_depth);
+                    check_launch(ctx, "k_tl_depth");
+                    k_treelet<<<tl_grid, 32 * TL_WARPS, 0, st>>>(child, parent, nbox, tl_depth, (int)n, cls, nullptr);
+                    check_launch(ctx, "k_treelet");
+                }
+            CRT_CUDA(cudaMemsetAsync(flags, 0, nn * 4, st));
+            k_tl_count<<<cdiv(n, BLOCK), BLOCK, 0, st>>>((int)n, child, parent, tl_cnt, flags, ctx->d_error);
+            check_launch(ctx, "k_tl_count");
+            k_tl_position<<<cdiv(2 * n - 1, BLOCK), BLOCK, 0, st>>>((int)n, child, parent, tl_cnt, tl_pos,
+                                                                   ctx->d_error);
+            check_launch(ctx, "k_tl_position");
+            k_tl_relayout<<<cdiv(n, BLOCK), BLOCK, 0, st>>>((int)n, tl_pos, tl_cnt, va, tl_sorted, child, range, parent,
+                                                           tl_par, ctx->d_error);
+            check_launch(ctx, "k_tl_relayout");
+            CRT_CUDA(cudaMemcpyAsync(va, tl_sorted, 4ull * n, cudaMemcpyDeviceToDevice, st));
+            CRT_CUDA(cudaMemcpyAsync(parent + (n - 1), tl_par, 4ull * n, cudaMemcpyDeviceToDevice, st));
+            CRT_CUDA(cudaMemsetAsync(flags, 0, nn * 4, st));
+        }
         k_refit<<<cdiv(n, BLOCK), BLOCK, 0, st>>>(va, tbox, (int)n, child, parent, nbox, flags, range, dpc,
-                                                  ctx->collapse_tri_cost);
+                                                  ctx->collapse_tri_cost, ctx->d_error);
         check_launch(ctx, "k_refit");
         idx_a = va;
     }

@@ -304,8 +304,9 @@ int crt_context_reset_counters(crt_context* ctx) {
 int crt_context_set_tuning(crt_context* ctx, const crt_tuning* t) {
     if (!ctx || !t) return CRT_ERR_INVALID;
     if (t->queue_chunk < 1 || t->queue_chunk > 8 || t->wave_paths < (1u << 16) ||
-        !(t->collapse_tri_cost >= 0.01f && t->collapse_tri_cost <= 10.0f)) {
-        ctx->last_error = "tuning out of range (queue_chunk 1..8, wave_paths >= 65536, collapse_tri_cost 0.01..10)";
+        !(t->collapse_tri_cost >= 0.01f && t->collapse_tri_cost <= 10.0f) || t->treelet_passes > 8) {
+        ctx->last_error = "tuning out of range (queue_chunk 1..8, wave_paths >= 65536, collapse_tri_cost 0.01..10, "
+                          "treelet_passes 0..8)";
         return CRT_ERR_INVALID;
     }
     ctx->queue_chunk = t->queue_chunk;
@@ -313,6 +314,7 @@ int crt_context_set_tuning(crt_context* ctx, const crt_tuning* t) {
     ctx->use_graphs = t->use_graphs ? 1 : 0;
     ctx->build_sah = t->build_sah ? 1 : 0;
     ctx->collapse_tri_cost = t->collapse_tri_cost;
+    ctx->treelet_passes = t->treelet_passes;
     return CRT_OK;
 }
 
@@ -323,6 +325,7 @@ int crt_context_get_tuning(const crt_context* ctx, crt_tuning* out) {
     out->use_graphs = ctx->use_graphs;
     out->build_sah = ctx->build_sah;
     out->collapse_tri_cost = ctx->collapse_tri_cost;
+    out->treelet_passes = ctx->treelet_passes;
     return CRT_OK;
 }
 

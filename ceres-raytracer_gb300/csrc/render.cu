@@ -97,8 +97,8 @@ struct WaveDesc {
     uint32_t n_lidar_items, n_lreq, n_paths, n_primary;
     uint32_t n_slices, n_update, n_srp_items, pad0;
     Slice slices[MAX_SLICES];
-    SceneView srp_sv;     // SRP items of the wave (crt_batch_mixed): one request's sun rays, after the
-    SrpWave srp;          // LiDAR beams and camera paths in the primary trace
+    SrpStage srp;         // SRP items of the wave (crt_batch_mixed, serving): one request's sun rays,
+                          // after the LiDAR beams and camera paths in the primary trace
 };
 
 struct Batch {
@@ -202,7 +202,7 @@ struct PrimaryJobT {
         uint32_t lidar;   // 0 camera path, 1 LiDAR beam, 2 SRP sun ray
     };
     __device__ SceneView view(const SceneView&, const Item& it) const {
-        if (SRP && it.lidar == 2) return B.cur->srp_sv;
+        if (SRP && it.lidar == 2) return B.cur->srp.sv;
         return it.lidar ? B.lr[it.req].sv : B.rr[it.req].sv;
     }
     __device__ void beam64(const LReq& L, uint32_t px, uint32_t py, double d[3]) const {
@@ -236,7 +236,7 @@ struct PrimaryJobT {
             const uint32_t k = i - w.n_lidar_items - w.n_paths;
             it.req = k;
             it.lidar = 2;
-            return srp_primary_ray(w.srp, k, r);
+            return srp_primary_ray(w.srp.W, k, r);
         }
         const uint32_t p = i - w.n_lidar_items;
         const Slice& S = w.slices[find_slice_by_path(w, p)];
@@ -262,7 +262,7 @@ struct PrimaryJobT {
     }
     __device__ void write(const SceneView&, uint32_t i, const TRay&, const THit& h, const Item& it) const {
         if (SRP && it.lidar == 2) {
-            srp_store_primary(B.cur->srp, it.req, h);
+            srp_store_primary(B.cur->srp.W, it.req, h);
             return;
         }
         if (it.lidar) {
@@ -789,17 +789,21 @@ inline uint32_t tiles_items(uint32_t W, uint32_t H) { return ((W + 7) / 8) * ((H
 // The stage sequence of one wave on the context stream.  Every launch reads the wave from B.cur
 // (filled by k_wave_begin from B.descs[*B.wave_idx]), so the sequence can be captured once and
 // replayed.  P: path capacity, NL: light stride, lidar_items: bound on the wave's LiDAR items.
-// srp_items: bound on the wave's SRP items (crt_batch_mixed); when non-zero the primary trace also
-// traces the wave's SRP sun rays and srp_stages (host launches of that wave's SRP shade and
-// specular segments) runs right after it, so such waves are launched one by one, not replayed.
+// srp_items: bound on the wave's SRP items (crt_batch_mixed, serving); when non-zero the primary
+// trace also traces the wave's SRP sun rays and srp_stages (launches of the SRP shade and specular
+// segments) runs right after it.  srp_mask (when given): the SRP hit mask, zeroed before the primary
+// trace.  With srp_stages reading the wave's range from the device descriptor (srp_wave_stages_dev)
+// the sequence is the same for every wave and can be captured and replayed.
 void launch_wave_kernels(crt_context* ctx, const Batch& B, size_t P, size_t NL, uint32_t lidar_items,
                          int max_bounces, uint32_t* qa, uint32_t* qb, uint32_t* tqueue, uint32_t srp_items = 0,
-                         const std::function<void()>* srp_stages = nullptr) {
+                         const std::function<void()>* srp_stages = nullptr, uint32_t* srp_mask = nullptr,
+                         size_t srp_mask_len = 0) {
     cudaStream_t st = ctx->stream;
     const uint32_t g_shade = grid_for(ctx, k_shade, P), g_accum = grid_for(ctx, k_accum, P);
     const uint32_t g_update = max_bounces <= 1 ? grid_for(ctx, k_update<true>, P) : grid_for(ctx, k_update<false>, P);
     k_wave_begin<<<1, 128, 0, st>>>(B);
     check_launch(ctx, "k_wave_begin");
+    if (srp_mask) CRT_CUDA(cudaMemsetAsync(srp_mask, 0, srp_mask_len, st));
     if (srp_items) {
         launch_trace<false>(ctx, SceneView{}, PrimaryJobT<true>{B},
                             (uint32_t)std::min<size_t>(P + lidar_items + srp_items, 0xFFFFFF00u), &B.cur->n_primary,
@@ -1135,8 +1139,9 @@ void run_batch(crt_context* ctx, const crt_request* reqs, size_t n, crt_batch_st
 
     for (size_t k = 0; k < sranges.size(); ++k) {
         const SrpRange& R = sranges[k];
-        plan[k].srp_sv = scene_view(srps[R.req]->base.scene);
-        plan[k].srp = srp_wave(splans[R.req], s_att[R.req], s_state, srp_max, R.i0, R.n);
+        crt_scene* sc = srps[R.req]->base.scene;
+        plan[k].srp = srp_stage(scene_view(sc), srp_wave(splans[R.req], s_att[R.req], s_state, srp_max, R.i0, R.n, (int)srp_nb),
+                                (uint32_t)R.n, splans[R.req], s_partial[R.req], (uint32_t)sc->n_tris);
     }
 
     // ---- uploads (pinned staging ring: no wait for the previous call's kernels)
@@ -1190,8 +1195,20 @@ void run_batch(crt_context* ctx, const crt_request* reqs, size_t n, crt_batch_st
     auto launch_wave = [&]() { launch_wave_kernels(ctx, B, P, NL, lidar_items, max_bounces, qa, qb, tqueue); };
 
     size_t waves_run = 0;
-    const bool graph_ok = ctx->use_graphs && !ctx->counting && plan.size() > 1 && n_srp == 0;
+    const bool graph_ok = ctx->use_graphs && !ctx->counting && plan.size() > 1;
+    const bool with_srp = n_srp && srp_max > 0;
     if (graph_ok) {
+        // waves carrying SRP items run their SRP stages from the wave descriptor (B.cur->srp), for
+        // every wave (no-ops in waves without SRP items): the sequence does not change between waves
+        std::function<void()> srp_stages;
+        uint32_t* srp_mask = nullptr;
+        if (with_srp) {
+            const SrpStage* d_stage = &B.cur->srp;
+            srp_stages = [&, d_stage]() {
+                srp_wave_stages_dev(ctx, d_stage, (uint32_t)srp_max, srp_nb, s_bq, s_bcount, tqueue);
+            };
+            srp_mask = (uint32_t*)(s_state + srp_mask_offset(srp_max, srp_nb));
+        }
         // capture one wave, replay it for every wave of the plan; the graph and its executable are
         // destroyed on every exit (replays already enqueued still run)
         struct GraphHold {
@@ -1205,7 +1222,11 @@ void run_batch(crt_context* ctx, const crt_request* reqs, size_t n, crt_batch_st
         CRT_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
         const uint64_t before = ctx->launches;
         try {
-            launch_wave();
+            if (with_srp)
+                launch_wave_kernels(ctx, B, P, NL, lidar_items, max_bounces, qa, qb, tqueue, (uint32_t)srp_max,
+                                    &srp_stages, srp_mask, srp_mask_bytes(srp_max));
+            else
+                launch_wave();
         } catch (...) {
             cudaStreamEndCapture(st, &gh.g);
             throw;
@@ -1219,16 +1240,17 @@ void run_batch(crt_context* ctx, const crt_request* reqs, size_t n, crt_batch_st
             ctx->launches += per_wave;
         }
         waves_run = plan.size();
-    } else if (n_srp) {
-        // waves with SRP items: the SRP stages of the wave's range follow its primary trace
+    } else if (with_srp) {
+        // waves with SRP items launched one by one: the SRP stages of the wave's range follow its
+        // primary trace
         for (size_t w = 0; w < plan.size(); ++w) {
             std::function<void()> stages;
             if (w < sranges.size()) {
                 const SrpRange& R = sranges[w];
                 crt_scene* sc = srps[R.req]->base.scene;
-                CRT_CUDA(cudaMemsetAsync(plan[w].srp.hitmask, 0, srp_mask_bytes(R.n), st));   // before the trace
+                CRT_CUDA(cudaMemsetAsync(plan[w].srp.W.hitmask, 0, srp_mask_bytes(R.n), st));   // before the trace
                 stages = [&, w, sc]() {
-                    srp_wave_stages(ctx, scene_view(sc), plan[w].srp, (uint32_t)R.n, splans[R.req], s_partial[R.req],
+                    srp_wave_stages(ctx, scene_view(sc), plan[w].srp.W, (uint32_t)R.n, splans[R.req], s_partial[R.req],
                                     nullptr, (uint32_t)sc->n_tris, s_bq, s_bcount);
                 };
             }
@@ -2041,8 +2063,8 @@ void engine_step(WaveEngine* e, std::vector<uint64_t>& completed) {
         const SrpPlan& SP = *sq->splan;
         srp_n = srp_wave_items(SP, e->srp_cap, sq->srp_next);
         w.n_srp_items = (uint32_t)srp_n;
-        w.srp_sv = scene_view(sq->q.scene);
-        w.srp = srp_wave(SP, sq->d_att, e->srp_state, e->srp_cap, sq->srp_next, srp_n);
+        w.srp = srp_stage(scene_view(sq->q.scene), srp_wave(SP, sq->d_att, e->srp_state, e->srp_cap, sq->srp_next, srp_n),
+                          (uint32_t)srp_n, SP, sq->partial, (uint32_t)sq->q.scene->n_tris);
         sq->srp_next += srp_n;
     }
     w.n_primary = w.n_lidar_items + w.n_paths + w.n_srp_items;
@@ -2059,7 +2081,7 @@ void engine_step(WaveEngine* e, std::vector<uint64_t>& completed) {
         CRT_CUDA(cudaMemsetAsync(e->d_wave_idx, 0, 4, st));
         std::function<void()> stages;
         if (sq) {
-            const SrpWave W = w.srp;
+            const SrpWave W = w.srp.W;
             CRT_CUDA(cudaMemsetAsync(W.hitmask, 0, srp_mask_bytes(srp_n), st));   // before the trace
             stages = [&, W]() {
                 srp_wave_stages(ctx, scene_view(sq->q.scene), W, (uint32_t)srp_n, *sq->splan, sq->partial, nullptr,

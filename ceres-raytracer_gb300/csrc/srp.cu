@@ -23,6 +23,7 @@
 #include "trace.cuh"
 
 #include <cmath>
+#include <cstring>
 #include <vector>
 
 namespace {
@@ -154,7 +155,7 @@ struct SrpShadeArgs {
 // summed in FP64, every step in a fixed order.  Blocks without a hit skip the reduction (GB300 runs
 // FP64 at a small fraction of its FP32 rate, and most blocks of a sun grid miss the body).
 template <bool FIRST>
-__global__ void __launch_bounds__(SRP_SHADE_THREADS) k_srp_shade(SceneView sv, SrpWave W, SrpShadeArgs A) {
+__device__ __forceinline__ void srp_shade(const SceneView& sv, const SrpWave& W, const SrpShadeArgs& A) {
     __shared__ double red[SRP_SHADE_THREADS / 32][6];
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
@@ -260,6 +261,59 @@ __global__ void __launch_bounds__(SRP_SHADE_THREADS) k_srp_shade(SceneView sv, S
     }
 }
 
+template <bool FIRST>
+__global__ void __launch_bounds__(SRP_SHADE_THREADS) k_srp_shade(SceneView sv, SrpWave W, SrpShadeArgs A) {
+    srp_shade<FIRST>(sv, W, A);
+}
+
+// the same, for the range of a device stage descriptor (blocks past its items, or segments past its
+// request's, return at once: the condition is uniform over the block)
+template <bool FIRST>
+__global__ void __launch_bounds__(SRP_SHADE_THREADS) k_srp_shade_dev(const SrpStage* __restrict__ S, uint32_t seg,
+                                                                    uint32_t* q_out, uint32_t* q_count) {
+    const uint32_t n = S->n, nb = S->nb;
+    if (seg > nb || blockIdx.x * SRP_BLOCK_ITEMS >= n) return;
+    SrpShadeArgs A;
+    A.n_items = n;
+    A.seg = seg;
+    A.nb = nb;
+    A.inv_c = S->inv_c;
+    for (int k = 0; k < 3; ++k) A.cm[k] = S->cm[k];
+    A.partial = S->partial;
+    A.block0 = 0;
+    A.facet = nullptr;
+    A.n_tris = S->n_tris;
+    A.q_out = q_out;
+    A.q_count = q_count;
+    const SceneView sv = S->sv;
+    const SrpWave W = S->W;
+    srp_shade<FIRST>(sv, W, A);
+}
+
+// continuing rays of a device stage descriptor's range
+struct SrpBounceJobDev {
+    const SrpStage* S;
+    const uint32_t* q;
+    struct Item {
+        uint32_t i;
+    };
+    __device__ __forceinline__ SceneView view(const SceneView&, const Item&) const { return S->sv; }
+    __device__ bool ray(uint32_t k, TRay& r, Item& it) const {
+        const uint32_t i = q[k];
+        const float4 o = S->W.st_o[i], d = S->W.st_d[i];
+        r.o = f3(o.x, o.y, o.z);
+        r.d = f3(d.x, d.y, d.z);
+        r.tmin = 0.f;
+        r.tmax = 3.402823466e38f;
+        r.skip = __float_as_uint(d.w);
+        it.i = i;
+        return true;
+    }
+    __device__ void write(const SceneView&, uint32_t, const TRay&, const THit& h, const Item& it) const {
+        S->W.hit[it.i] = make_float4(h.t, h.u, h.v, __uint_as_float(h.slot));
+    }
+};
+
 }  // namespace
 
 void srp_frame(crt_scene* s, const crt_srp_desc* desc, SrpPlan& P, SrpFrame& F) {
@@ -363,7 +417,9 @@ uint64_t srp_wave_items(const SrpPlan& P, uint64_t cap, uint64_t i0) {
                         : std::min<uint64_t>(cap, P.ipa - i0 % P.ipa);
 }
 
-SrpWave srp_wave(const SrpPlan& P, const SrpAtt* d_att, char* state, uint64_t cap, uint64_t i0, uint64_t n) {
+SrpWave srp_wave(const SrpPlan& P, const SrpAtt* d_att, char* state, uint64_t cap, uint64_t i0, uint64_t n,
+                 int layout_nb) {
+    const uint32_t nb = layout_nb < 0 ? P.nb : (uint32_t)layout_nb;
     SrpWave W;
     W.att = d_att;
     W.G = P.G;
@@ -379,10 +435,10 @@ SrpWave srp_wave(const SrpPlan& P, const SrpAtt* d_att, char* state, uint64_t ca
         W.box_hi[k] = P.box_hi[k];
     }
     W.hit = (float4*)state;
-    W.hitmask = (uint32_t*)(state + srp_mask_offset(cap, P.nb));
-    W.st_o = P.nb ? (float4*)(state + cap * 16) : nullptr;
-    W.st_d = P.nb ? (float4*)(state + cap * 32) : nullptr;
-    W.alive = P.nb ? (uint8_t*)(state + cap * 48) : nullptr;
+    W.hitmask = (uint32_t*)(state + srp_mask_offset(cap, nb));
+    W.st_o = nb ? (float4*)(state + cap * 16) : nullptr;
+    W.st_d = nb ? (float4*)(state + cap * 32) : nullptr;
+    W.alive = nb ? (uint8_t*)(state + cap * 48) : nullptr;
     return W;
 }
 
@@ -414,6 +470,41 @@ void srp_wave_stages(crt_context* ctx, const SceneView& sv, const SrpWave& W, ui
             J.q = bq;
             launch_trace<false>(ctx, sv, J, n, bcount + ((seg - 1) & 1), trace_queue);
             k_srp_shade<false><<<nblk, SRP_SHADE_THREADS, 0, st>>>(sv, W, A);
+        }
+        check_launch(ctx, "k_srp_shade");
+    }
+}
+
+SrpStage srp_stage(const SceneView& sv, const SrpWave& W, uint32_t n, const SrpPlan& P, double* partial,
+                   uint32_t n_tris) {
+    SrpStage S;
+    std::memset(&S, 0, sizeof(S));
+    S.sv = sv;
+    S.W = W;
+    S.partial = partial;
+    S.n = n;
+    S.nb = P.nb;
+    S.n_tris = n_tris;
+    S.inv_c = P.inv_c;
+    for (int k = 0; k < 3; ++k) S.cm[k] = P.cm[k];
+    return S;
+}
+
+void srp_wave_stages_dev(crt_context* ctx, const SrpStage* d_stage, uint32_t n_max, uint32_t nb_max, uint32_t* bq,
+                         uint32_t* bcount, uint32_t* trace_queue) {
+    cudaStream_t st = ctx->stream;
+    const uint32_t nblk = std::max<uint32_t>(1, (n_max + SRP_BLOCK_ITEMS - 1) / SRP_BLOCK_ITEMS);
+    for (uint32_t seg = 0; seg <= nb_max; ++seg) {
+        uint32_t* q_count = bcount + (seg & 1);   // filled by this segment's shade
+        if (seg < nb_max) CRT_CUDA(cudaMemsetAsync(q_count, 0, sizeof(uint32_t), st));
+        if (seg == 0) {
+            k_srp_shade_dev<true><<<nblk, SRP_SHADE_THREADS, 0, st>>>(d_stage, 0, bq, q_count);
+        } else {
+            SrpBounceJobDev J;
+            J.S = d_stage;
+            J.q = bq;
+            launch_trace<false>(ctx, SceneView{}, J, n_max, bcount + ((seg - 1) & 1), trace_queue);
+            k_srp_shade_dev<false><<<nblk, SRP_SHADE_THREADS, 0, st>>>(d_stage, seg, bq, q_count);
         }
         check_launch(ctx, "k_srp_shade");
     }

@@ -103,6 +103,21 @@ struct SrpFrame {
     double Rb, h, E0;
 };
 
+// One wave's SRP range as the stage kernels read it from device memory (a batched wave's descriptor):
+// the launches of a wave stay the same from wave to wave, so the wave can be replayed as one CUDA
+// graph; the range they work on, and its request's constants, come from here.
+struct SrpStage {
+    SceneView sv;        // the request's scene
+    SrpWave W;           // the range's items and per-item state
+    double* partial;     // the request's partial sums (slot = block of the request)
+    uint32_t n;          // items in the range (0: the wave has none)
+    uint32_t nb;         // specular segments of the request
+    uint32_t n_tris;
+    float inv_c;
+    float cm[3];
+    uint32_t pad;
+};
+
 // Per-wave SRP state for waves of at most `cap` items: hits (16 B per item), continuation state when
 // there are specular segments (33 B per item), then the primary segment's hit mask (1 bit per item).
 constexpr size_t srp_mask_offset(uint64_t cap, uint32_t nb) {
@@ -133,7 +148,10 @@ void srp_set_attitudes(SrpPlan& P, size_t n_att);
 void srp_attitude(const SrpFrame& F, const double q[4], SrpAtt& out);
 // Wave descriptor over `state` (room for `cap` items) for items [i0, i0 + n) of the request
 // (d_att: its attitude table on the device)
-SrpWave srp_wave(const SrpPlan& P, const SrpAtt* d_att, char* state, uint64_t cap, uint64_t i0, uint64_t n);
+// (state laid out for `layout_nb` specular segments, default P.nb: requests sharing one state buffer
+// use the largest)
+SrpWave srp_wave(const SrpPlan& P, const SrpAtt* d_att, char* state, uint64_t cap, uint64_t i0, uint64_t n,
+                 int layout_nb = -1);
 // Largest wave at most `cap` items long that starts at item i0: whole attitudes when one fits,
 // else the rest of the current attitude
 uint64_t srp_wave_items(const SrpPlan& P, uint64_t cap, uint64_t i0);
@@ -145,5 +163,13 @@ uint64_t srp_wave_items(const SrpPlan& P, uint64_t cap, uint64_t i0);
 void srp_wave_stages(crt_context* ctx, const SceneView& sv, const SrpWave& W, uint32_t n, const SrpPlan& P,
                      double* partial, double* facet, uint32_t n_tris, uint32_t* bq, uint32_t* bcount,
                      uint64_t partial_block0 = 0, uint32_t* trace_queue = nullptr);
+// The stage descriptor of items [W.i0, W.i0 + n) of a request (plan P, partial sums `partial`)
+SrpStage srp_stage(const SceneView& sv, const SrpWave& W, uint32_t n, const SrpPlan& P, double* partial,
+                   uint32_t n_tris);
+// srp_wave_stages for the range in d_stage (device memory, filled before the launches run): launches
+// nb_max specular segments over n_max items; segments and blocks beyond the range's own do nothing.
+// No argument depends on the range, so the launches can be captured once and replayed per wave.
+void srp_wave_stages_dev(crt_context* ctx, const SrpStage* d_stage, uint32_t n_max, uint32_t nb_max, uint32_t* bq,
+                         uint32_t* bcount, uint32_t* trace_queue);
 // Per-attitude force and torque from the request's partial sums (device outputs)
 void srp_reduce(crt_context* ctx, const double* partial, const SrpPlan& P, double* force, double* torque);

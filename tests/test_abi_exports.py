@@ -43,7 +43,7 @@ def test_binding_covers_header():
 
 def test_abi_version_without_gpu():
     L = lib.load()
-    assert L.crt_abi_version() == 2
+    assert L.crt_abi_version() == 3
     assert L.crt_status_string(-4) == b"timeout"
 
 

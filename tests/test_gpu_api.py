@@ -130,12 +130,18 @@ def test_transform_to_body_moves_queries(tmp_path):
     cam2 = SimpleCamera(cam["focal_length"], cam["resolution"], cam["sensor_size"], cam["z_positive"],
                         position=Rz.T @ cam["position"] + t, rotation=cam["rotation"] @ Rz)
     ids = group.instance_pass(cam2)
-    # the same body-frame rays up to FP64 rounding: ids equal except on rays at triangle edges
+    xyz2 = group.intersection_pass(cam2)   # body-frame points of the posed query
+    # the same body-frame rays up to FP64 rounding of the pose arithmetic: ids equal the oracle's
+    # except on rays at triangle edges (of the oracle's triangle, or of one at the GPU's hit point)
     o = oracle.Scene(entities_from(d))
-    _, oi, _, oprim = o.passes(cam)
+    ox, oi, _, oprim = o.passes(cam)
     rays = workloads.camera_rays(cam)
     index = TriIndex(o.tris())
-    for got in (ref_ids, ids):
+    for got, gx in ((ref_ids, None), (ids, xyz2)):
         diff = np.nonzero((got != oi).ravel())[0]
-        bad = unexcused(index, rays[diff], edge_eps(rays[diff], index.extent), prims=[oprim.ravel()[diff]])
-        assert len(bad) == 0, diff[bad][:5]
+        pts = [np.where((oi.ravel()[diff] > 0)[:, None], ox.reshape(-1, 3)[diff], np.nan)]
+        if gx is not None:
+            pts.append(np.where((got.ravel()[diff] > 0)[:, None], gx.reshape(-1, 3)[diff], np.nan))
+        bad = unexcused(index, rays[diff], edge_eps(rays[diff], index.extent), prims=[oprim.ravel()[diff]],
+                        points=pts)
+        assert len(bad) == 0, (diff[bad][:5], got.ravel()[diff[bad][:5]], oi.ravel()[diff[bad][:5]])

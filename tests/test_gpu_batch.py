@@ -141,19 +141,20 @@ def srp_requests(ctx, ast):
     ]
 
 
-@pytest.mark.parametrize("wave_paths", [1 << 23, 1 << 16])
-def test_mixed_batch_with_srp_equals_standalone(setup, wave_paths):
+@pytest.mark.parametrize("wave_paths,graphs", [(1 << 23, True), (1 << 16, True), (1 << 16, False)])
+def test_mixed_batch_with_srp_equals_standalone(setup, wave_paths, graphs):
     """crt_batch_mixed: SRP requests ride in the waves' primary traces beside camera paths and LiDAR
     beams.  Renders and LiDAR scans equal their standalone calls bit for bit, and force and torque
     equal crt_srp's bit for bit however the sun-ray grids are cut into waves (partial sums are kept
-    per block of the request's items)."""
+    per block of the request's items), with the waves replayed as one CUDA graph (the SRP stages read
+    the wave's range from its device descriptor) or launched one by one."""
     ctx, d, cornell, ast = setup
     reqs = make_requests(d, cornell, ast)[:8]
     srps = srp_requests(ctx, ast)
     mixed = reqs[:3] + [srps[0]] + reqs[3:6] + srps[1:] + reqs[6:]
     ctx.set_tuning(queue_chunk=1, wave_paths=1 << 23, use_graphs=True)
     alone = [standalone(q) for q in mixed]
-    ctx.set_tuning(queue_chunk=1, wave_paths=wave_paths, use_graphs=True)
+    ctx.set_tuning(queue_chunk=1, wave_paths=wave_paths, use_graphs=graphs)
     outs, st = ctx.batch(mixed)
     ctx.set_tuning()
     for q, a, b in zip(mixed, alone, outs):

@@ -80,7 +80,7 @@ def check_lidar(index, pos, rot, rng, prim, rng_ref, prim_ref, z_positive=False)
 
 
 def test_abi_version_and_context(ctx):
-    assert lib.load().crt_abi_version() == 2
+    assert lib.load().crt_abi_version() == 3
 
 
 @pytest.mark.parametrize("name", ["cornell", "asteroid"])
