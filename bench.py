@@ -242,15 +242,20 @@ def profiled_counters():
 
 
 def read_peaks(ctx, dev):
-    """Streaming-read bandwidth measured here with the library's read kernel (crt_measure_read):
-    a 48 MiB buffer that stays in L2 after the first pass, and a 4 GiB buffer from HBM.  GB/s."""
+    """Streaming-read bandwidth measured here with the library's read kernel (crt_measure_read, at
+    least 1 GiB read per launch): the best of 64, 80 and 96 MiB buffers, which stay in the L2 cache
+    after the first pass (the plateau of a 4 MiB .. 4 GiB sweep on this GPU; 128 MiB no longer fits),
+    and a 4 GiB buffer read from HBM.  GB/s."""
     import torch
-    small = torch.ones(48 << 20, dtype=torch.uint8, device=dev)
-    ms_l2 = ctx.measure_read(small, reps=200)
+    l2 = 0.0
+    for mib in (64, 80, 96):
+        b = torch.ones(mib << 20, dtype=torch.uint8, device=dev)
+        l2 = max(l2, b.numel() / ctx.measure_read(b, reps=5) / 1e6)
+        del b
     big = torch.ones(4 << 30, dtype=torch.uint8, device=dev)
-    ms_hbm = ctx.measure_read(big, reps=10)
-    out = {"l2_read_gbs": round(small.numel() / ms_l2 / 1e6, 1), "hbm_read_gbs": round(big.numel() / ms_hbm / 1e6, 1)}
-    del small, big
+    ms_hbm = ctx.measure_read(big, reps=5)
+    out = {"l2_read_gbs": round(l2, 1), "hbm_read_gbs": round(big.numel() / ms_hbm / 1e6, 1)}
+    del big
     torch.cuda.empty_cache()
     return out
 
@@ -464,7 +469,7 @@ def gpu_arm(args):
         roof.update(traffic_source="ncu capture of the same kernel, BVH and rays (" + PROFILE + ", counters "
                                    "dram__bytes_read.sum + dram__bytes_write.sum, lts__t_bytes.sum) over the "
                                    "kernel time measured in this run",
-                    dram_gbs=round(dram_gbs, 1), dram_frac=round(dram_gbs / pk["hbm_read_gbs"], 4),
+                    dram_gbs=round(dram_gbs, 1), dram_frac=round(dram_gbs / peak, 4),
                     l2_gbs=round(l2_gbs, 1), l2_frac=round(l2_gbs / pk["l2_read_gbs"], 4))
     if prof.get("warp_inst") and prof.get("rays"):
         roof.update(warp_inst_per_32_rays=round(prof["warp_inst"] / (prof["rays"] / 32.0), 1),

@@ -291,7 +291,7 @@ class Context:
         return Scene(self, entities)
 
     def set_tuning(self, queue_chunk=1, wave_paths=1 << 23, use_graphs=True, build_sah=True, collapse_tri_cost=0.15,
-                   treelet_passes=2):
+                   treelet_passes=1):
         t = Tuning(int(queue_chunk), int(wave_paths), int(bool(use_graphs)), int(bool(build_sah)),
                    float(collapse_tri_cost), int(treelet_passes))
         self._check(self.L.crt_context_set_tuning(self.h, ctypes.byref(t)))

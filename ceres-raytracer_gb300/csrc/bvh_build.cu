@@ -1611,7 +1611,7 @@ void scene_build(crt_scene* s, const crt_entity_desc* ents, uint32_t n_ents) {
             k_karras<<<cdiv(n - 1, BLOCK), BLOCK, 0, st>>>(ka, (int)n, child, range, parent);
             check_launch(ctx, "k_karras");
         }
-        if (sah && root_index >= 0 && ctx->treelet_passes > 0 && n >= 8) {
+        if (ctx->treelet_passes > 0 && n >= 8) {
             // treelet restructuring of the binary tree, then leaves renumbered depth-first
             k_tl_boxes<<<cdiv(n, BLOCK), BLOCK, 0, st>>>(va, tbox, (int)n, child, parent, nbox, flags, ctx->d_error);
             check_launch(ctx, "k_tl_boxes");

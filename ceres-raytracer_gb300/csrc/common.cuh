@@ -90,7 +90,7 @@ struct crt_context {
     int use_graphs = 1;              // replay batched waves as CUDA graphs
     int build_sah = 1;               // scene builds: binned-SAH topology (1) or Karras radix tree (0)
     float collapse_tri_cost = 0.15f; // scene builds: triangle-test cost of the 8-wide collapse (node = 1)
-    uint32_t treelet_passes = 2;     // scene builds (binned SAH): treelet-restructuring passes
+    uint32_t treelet_passes = 1;     // scene builds: treelet-restructuring passes over the binary tree
 };
 
 // Grow-only device scratch buffer for one purpose.  Synchronises the stream before reallocating.

@@ -227,19 +227,23 @@ int crt_context_synchronize(crt_context* ctx) {
 // Streaming read of a buffer with 16-byte loads that bypass L1 (ld.global.cg): four independent loads
 // in flight per thread per iteration.  The XOR of everything read is stored only when it equals a
 // value it never takes in practice, which keeps the loads without writing.
-__global__ void __launch_bounds__(256) k_read_stream(const uint4* __restrict__ p, size_t n16,
+// `inner` passes per launch, so that a pass over a small (L2-resident) buffer is not shorter than the
+// launch itself.
+__global__ void __launch_bounds__(256) k_read_stream(const uint4* __restrict__ p, size_t n16, uint32_t inner,
                                                     uint32_t* __restrict__ sink) {
     const size_t stride = (size_t)gridDim.x * blockDim.x;
     uint32_t acc = 0;
-    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    for (; i + 3 * stride < n16; i += 4 * stride) {
-        const uint4 a = __ldcg(p + i), b = __ldcg(p + i + stride), c = __ldcg(p + i + 2 * stride),
-                    d = __ldcg(p + i + 3 * stride);
-        acc ^= a.x ^ a.y ^ a.z ^ a.w ^ b.x ^ b.y ^ b.z ^ b.w ^ c.x ^ c.y ^ c.z ^ c.w ^ d.x ^ d.y ^ d.z ^ d.w;
-    }
-    for (; i < n16; i += stride) {
-        const uint4 a = __ldcg(p + i);
-        acc ^= a.x ^ a.y ^ a.z ^ a.w;
+    for (uint32_t r = 0; r < inner; ++r) {
+        size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+        for (; i + 3 * stride < n16; i += 4 * stride) {
+            const uint4 a = __ldcg(p + i), b = __ldcg(p + i + stride), c = __ldcg(p + i + 2 * stride),
+                        d = __ldcg(p + i + 3 * stride);
+            acc ^= a.x ^ a.y ^ a.z ^ a.w ^ b.x ^ b.y ^ b.z ^ b.w ^ c.x ^ c.y ^ c.z ^ c.w ^ d.x ^ d.y ^ d.z ^ d.w;
+        }
+        for (; i < n16; i += stride) {
+            const uint4 a = __ldcg(p + i);
+            acc ^= a.x ^ a.y ^ a.z ^ a.w;
+        }
     }
     if (acc == 0x9E3779B9u) sink[threadIdx.x & 31] = acc;
 }
@@ -254,13 +258,15 @@ int crt_measure_read(crt_context* ctx, const void* buf, size_t bytes, uint32_t r
         const int grid = occupancy_grid(ctx, (const void*)k_read_stream, 256, 0);
         const uint4* p = (const uint4*)buf;
         const size_t n16 = bytes / 16;
+        // passes per launch: at least 1 GiB read per launch
+        const uint32_t inner = (uint32_t)std::max<size_t>(1, std::min<size_t>(4096, (size_t(1) << 30) / bytes));
         cudaEvent_t e0, e1;
         CRT_CUDA(cudaEventCreate(&e0));
         CRT_CUDA(cudaEventCreate(&e1));
-        k_read_stream<<<grid, 256, 0, ctx->stream>>>(p, n16, sink);   // warm-up pass (fills L2 for small buffers)
+        k_read_stream<<<grid, 256, 0, ctx->stream>>>(p, n16, 1, sink);   // warm-up pass (fills L2 for small buffers)
         check_launch(ctx, "k_read_stream");
         CRT_CUDA(cudaEventRecord(e0, ctx->stream));
-        for (uint32_t r = 0; r < reps; ++r) k_read_stream<<<grid, 256, 0, ctx->stream>>>(p, n16, sink);
+        for (uint32_t r = 0; r < reps; ++r) k_read_stream<<<grid, 256, 0, ctx->stream>>>(p, n16, inner, sink);
         check_launch(ctx, "k_read_stream");
         CRT_CUDA(cudaEventRecord(e1, ctx->stream));
         CRT_CUDA(cudaEventSynchronize(e1));
@@ -269,7 +275,7 @@ int crt_measure_read(crt_context* ctx, const void* buf, size_t bytes, uint32_t r
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
         ctx->launches += reps - 1;
-        *ms_per_pass = ms / reps;
+        *ms_per_pass = ms / ((double)reps * inner);
     });
 }
 

@@ -306,16 +306,19 @@ struct SceneHandle {
     }
 };
 
-// sah: -1 the context's setting, 0 radix tree, 1 binned SAH (for this scene's build only)
+// sah: -1 the context's setting, 0 radix tree without treelet restructuring (the shortest build),
+// 1 binned SAH with the context's treelet passes (for this scene's build only)
 std::unique_ptr<SceneHandle> build_scene(const std::vector<crt_entity_desc>& descs, int sah = -1) {
     auto h = std::make_unique<SceneHandle>();
     py::gil_scoped_release nogil;
     std::lock_guard<std::mutex> lk(g_mu);
     crt_tuning saved;
-    const bool swap = sah >= 0 && crt_context_get_tuning(ctx(), &saved) == CRT_OK && saved.build_sah != sah;
+    const bool swap = sah >= 0 && crt_context_get_tuning(ctx(), &saved) == CRT_OK &&
+                      (saved.build_sah != sah || (sah == 0 && saved.treelet_passes != 0));
     if (swap) {
         crt_tuning t = saved;
         t.build_sah = sah;
+        if (sah == 0) t.treelet_passes = 0;
         crt_context_set_tuning(ctx(), &t);
     }
     int rc = crt_scene_create(ctx(), descs.data(), (uint32_t)descs.size(), &h->s);
@@ -478,10 +481,10 @@ struct BodyFixedGroup : Pose {
     crt_scene* sc() const { return scene->s; }
 };
 
-// The dynamic path rebuilds the BVH on every call.  The binned-SAH topology costs about 5.4 ns per
-// triangle more to build than the radix tree (2M triangles: 15.2 vs 4.5 ms) and saves about 10 % of
-// the traversal, ~0.018 ns of ~0.18 ns per ray, so a call uses it only when it traces more than
-// about 300 rays per triangle; `rays` is the call's estimate.
+// The dynamic path rebuilds the BVH on every call.  The binned-SAH topology with one treelet pass
+// costs about 9.5 ns per triangle more to build than the radix tree (2M triangles: 23.7 vs 4.7 ms)
+// and saves about 10 % of the traversal, ~0.018 ns of ~0.18 ns per ray, so a call uses it only when
+// it traces more than about 500 rays per triangle; `rays` is the call's estimate.
 std::unique_ptr<SceneHandle> dynamic_scene(const py::list& entities, bool assign_ids, double rays) {
     std::vector<crt_entity_desc> descs;
     uint32_t id = 1;
@@ -492,7 +495,7 @@ std::unique_ptr<SceneHandle> dynamic_scene(const py::list& entities, bool assign
         descs.push_back(entity_desc(e, *e.mesh, e.id));
         n_tris += (double)e.mesh->n;
     }
-    return build_scene(descs, rays > 300.0 * n_tris ? 1 : 0);
+    return build_scene(descs, rays > 500.0 * n_tris ? 1 : 0);
 }
 
 double pixels(const SimpleCamera& c) { return (double)std::max(c.width(), 0) * (double)std::max(c.height(), 0); }

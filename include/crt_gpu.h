@@ -165,9 +165,9 @@ typedef struct {
                                              an 8-wide node test in the 8-wide collapse (default 0.15,
                                              best for coherent rays; ~0.5 suits multi-bounce path
                                              tracing); 0.01 .. 10 */
-    uint32_t treelet_passes;              /* scenes built afterwards with the binned-SAH topology: passes of
-                                             treelet restructuring over the binary tree before the 8-wide
-                                             collapse (0 .. 8; 0 skips the optimisation, faster build) */
+    uint32_t treelet_passes;              /* scenes built afterwards: passes of treelet restructuring over
+                                             the binary tree before the 8-wide collapse (default 1; 0 .. 8;
+                                             0 skips the optimisation: faster build) */
 } crt_tuning;
 
 typedef struct {

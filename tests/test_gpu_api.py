@@ -115,33 +115,38 @@ def test_render_and_lidar_through_api(tmp_path):
 
 
 def test_transform_to_body_moves_queries(tmp_path):
-    """A group pose is applied to cameras through transform_to_body (body_fixed.py:87-101)."""
+    """A group pose is applied to cameras through transform_to_body (body_fixed.py:87-101): posing the
+    group and the camera together gives the unposed query's body-frame rays, so instance ids equal the
+    oracle's on the unposed camera except on rays at triangle edges."""
     import crt
     from crt.cameras import SimpleCamera
     d = load_golden("cornell")
     objs, camera = crt_objects(d, tmp_path)
     group = crt.BodyFixedGroup(objs)
-    ref_ids = group.instance_pass(camera)
-    # rotate the group by 90 deg about z and move it; rotate/move the camera with it
+    cam = camera_from(d)
+
+    def query(position, rotation):
+        # the passes move the camera they are given into the body frame (as the reference does), so
+        # each pass gets a fresh camera object
+        mk = lambda: SimpleCamera(cam["focal_length"], cam["resolution"], cam["sensor_size"], cam["z_positive"],
+                                  position=position, rotation=rotation)
+        return group.instance_pass(mk()), group.intersection_pass(mk())
+
+    results = [query(cam["position"], cam["rotation"])]
+    # rotate the group by 90 deg about z and move it; rotate / move the camera with it
     Rz = np.array([[0.0, -1.0, 0.0], [1.0, 0.0, 0.0], [0.0, 0.0, 1.0]])
     t = np.array([10.0, -3.0, 2.0])
     group.set_pose(t, Rz)
-    cam = camera_from(d)
-    cam2 = SimpleCamera(cam["focal_length"], cam["resolution"], cam["sensor_size"], cam["z_positive"],
-                        position=Rz.T @ cam["position"] + t, rotation=cam["rotation"] @ Rz)
-    ids = group.instance_pass(cam2)
-    xyz2 = group.intersection_pass(cam2)   # body-frame points of the posed query
-    # the same body-frame rays up to FP64 rounding of the pose arithmetic: ids equal the oracle's
-    # except on rays at triangle edges (of the oracle's triangle, or of one at the GPU's hit point)
+    results.append(query(Rz.T @ cam["position"] + t, cam["rotation"] @ Rz))
     o = oracle.Scene(entities_from(d))
     ox, oi, _, oprim = o.passes(cam)
     rays = workloads.camera_rays(cam)
     index = TriIndex(o.tris())
-    for got, gx in ((ref_ids, None), (ids, xyz2)):
+    for got, gx in results:
         diff = np.nonzero((got != oi).ravel())[0]
-        pts = [np.where((oi.ravel()[diff] > 0)[:, None], ox.reshape(-1, 3)[diff], np.nan)]
-        if gx is not None:
-            pts.append(np.where((got.ravel()[diff] > 0)[:, None], gx.reshape(-1, 3)[diff], np.nan))
+        pts = [np.where((oi.ravel()[diff] > 0)[:, None], ox.reshape(-1, 3)[diff], np.nan),
+               np.where((got.ravel()[diff] > 0)[:, None], gx.reshape(-1, 3)[diff], np.nan)]
         bad = unexcused(index, rays[diff], edge_eps(rays[diff], index.extent), prims=[oprim.ravel()[diff]],
                         points=pts)
         assert len(bad) == 0, (diff[bad][:5], got.ravel()[diff[bad][:5]], oi.ravel()[diff[bad][:5]])
+    np.testing.assert_array_equal(results[0][0], results[1][0])
