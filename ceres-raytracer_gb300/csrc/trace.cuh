@@ -7,6 +7,10 @@
 #ifndef CRT_TRACE_BLOCK
 #define CRT_TRACE_BLOCK 128
 #endif
+// resident blocks per SM the trace kernel is compiled for (registers per thread: 65536 / (128 x 8) = 64)
+#ifndef CRT_TRACE_MIN_BLOCKS
+#define CRT_TRACE_MIN_BLOCKS 8
+#endif
 
 __host__ __device__ __forceinline__ SceneView scene_view(const crt_scene* s) {
     SceneView v;
@@ -79,7 +83,7 @@ struct JobBase {
 // left so that the last grabs stay small (few atomics on the queue counter while much work is left,
 // balance at the end).
 template <bool ANY, bool COUNT, class Job>
-__global__ void __launch_bounds__(CRT_TRACE_BLOCK, 8) k_trace(SceneView sv, Job job, uint32_t n_items,
+__global__ void __launch_bounds__(CRT_TRACE_BLOCK, CRT_TRACE_MIN_BLOCKS) k_trace(SceneView sv, Job job, uint32_t n_items,
                                                             const uint32_t* __restrict__ n_dev,
                                                             uint32_t* __restrict__ queue, uint32_t* __restrict__ err,
                                                             unsigned long long* __restrict__ counters, uint32_t chunk) {
