@@ -63,9 +63,10 @@ def parse():
     ap.add_argument("--probe", type=int, default=0,
                     help="profiling aid (the commands of the ncu summaries under profiles/ run it): only run "
                          "the --probe-kind workload this many times")
-    ap.add_argument("--probe-kind", default="closest", choices=["closest", "batched", "srp"],
+    ap.add_argument("--probe-kind", default="closest", choices=["closest", "batched", "srp", "step"],
                     help="closest: crt_trace_closest on the 2048^2 primary rays; batched: one crt_batch of the "
-                         "64-request mix; srp: 8 attitudes x 4096^2 rays x 2 bounces with per-facet flux")
+                         "64-request mix; srp: 8 attitudes x 4096^2 rays x 2 bounces with per-facet flux; step: "
+                         "the bench's step (L2 flush, render, LiDAR scan) with device outputs")
     return ap.parse_args()
 
 
@@ -92,6 +93,21 @@ def probe(args):
         ctx.set_tuning(collapse_tri_cost=0.5)   # as the bench's batched measurement builds its scene
     sc = ctx.scene(ents)
     ctx.set_tuning()
+    if args.probe_kind == "step":
+        lid = cfg["lidar"]
+        rgba = torch.empty((args.res, args.res, 4), dtype=torch.uint8, device="cuda")
+        rng = torch.empty((lid["ny"], lid["nx"]), dtype=torch.float64, device="cuda")
+        prim = torch.empty((lid["ny"], lid["nx"]), dtype=torch.int32, device="cuda")
+        flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+        for _ in range(args.probe):
+            flush.zero_()
+            sc.render(cfg["camera"], cfg["lights"], 1, 1, 1.0, cfg["bounces"], want_radiance=False, out_rgba=rgba)
+            sc.lidar_grid(lid["position"], lid["rotation"], lid["nx"], lid["ny"], lid["half_x"], lid["half_y"],
+                          out_range=rng, out_prim=prim)
+        ctx.synchronize()
+        print(json.dumps({"probe_launches": args.probe, "kind": "step"}))
+        ctx.close()
+        return
     if args.probe_kind == "batched":
         reqs = []
         for q in workloads.batched_config(seed=1):

@@ -1,7 +1,7 @@
 """Build the reference implementation into oracle/_ref/ (TEST INFRASTRUCTURE ONLY).
 
-Compiles the unmodified ceres-raytracer sources where they lie (default /root/reference,
-override with CRT_REFERENCE_DIR) with g++ directly, as the reference's own setup.py/CMake
+Compiles the unmodified ceres-raytracer sources where they lie (the directory given as the first
+argument, or in CRT_REFERENCE_DIR) with g++ directly, as the reference's own setup.py/CMake
 would, into:
 
   oracle/_ref/golden/_crt<ext>         the reference pybind11 module (src/pybind.cpp +
@@ -22,7 +22,7 @@ import sysconfig
 from concurrent.futures import ThreadPoolExecutor
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = os.environ.get("CRT_REFERENCE_DIR", "/root/reference")
+REF = os.environ.get("CRT_REFERENCE_DIR", "")
 OUT = os.path.join(HERE, "_ref")
 
 # CMakeLists.txt:15-16 (release flags of the reference)
@@ -39,13 +39,33 @@ def pybind_includes():
         return [os.path.join(os.path.dirname(torch.__file__), "include")]
 
 
-def available():
-    return os.path.isfile(os.path.join(REF, "src", "pybind.cpp"))
+def available(ref=None):
+    ref = REF if ref is None else ref
+    return bool(ref) and os.path.isfile(os.path.join(ref, "src", "pybind.cpp"))
 
 
-def build(verbose=False):
+def _sources(ref):
+    return [os.path.join(ref, "src", "pybind.cpp"), os.path.join(ref, "lib", "lodepng", "lodepng.cpp"),
+            os.path.join(HERE, "ref_driver.cpp"), os.path.join(HERE, "ref_shim.h")]
+
+
+def up_to_date(ref):
+    """The three outputs exist and are newer than the recipe's own sources (the reference is read-only)."""
+    ext = sysconfig.get_config_var("EXT_SUFFIX")
+    outs = [os.path.join(OUT, "golden", "_crt" + ext), os.path.join(OUT, "golden", "libref_driver.so"),
+            os.path.join(OUT, "perf", "_crt" + ext)]
+    if not all(os.path.exists(o) for o in outs):
+        return False
+    t = min(os.path.getmtime(o) for o in outs)
+    return all(os.path.getmtime(s) <= t for s in _sources(ref) + [os.path.abspath(__file__)] if os.path.exists(s))
+
+
+def build(verbose=False, ref=None):
+    global REF
+    REF = REF if ref is None else ref
     if not available():
-        raise FileNotFoundError(f"reference sources not found under {REF}")
+        raise FileNotFoundError("reference sources not found: pass their directory as the first argument or set "
+                                "CRT_REFERENCE_DIR")
     ext = sysconfig.get_config_var("EXT_SUFFIX")
     py_inc = sysconfig.get_paths()["include"]
     incs = ["-I" + os.path.join(REF, "lib"), "-I" + os.path.join(REF, "src"), "-I" + os.path.join(REF, "src", "crt"),
@@ -73,6 +93,6 @@ def build(verbose=False):
 
 
 if __name__ == "__main__":
-    build(verbose=True)
+    build(verbose=True, ref=sys.argv[1] if len(sys.argv) > 1 else None)
     print("built", OUT)
     sys.exit(0)

@@ -1,7 +1,7 @@
 """Generate the golden fixtures in tests/golden/ from the reference implementation itself.
 
-Run where the reference sources are available (default /root/reference) after
-`python oracle/build_ref.py`:
+Run where the reference sources are available, after `python oracle/build_ref.py <reference dir>`
+(or with CRT_REFERENCE_DIR set):
 
     python tests/golden/make_golden.py
 
