@@ -1496,6 +1496,17 @@ struct WaveEngine {
     char* srp_state = nullptr;
     uint32_t* srp_bq = nullptr;
     uint32_t* srp_bcount = nullptr;
+    // executable graphs of one wave, per (bounce count, specular segments of the wave's SRP range, -1
+    // without one), valid for the buffers they were captured with (their addresses are kernel
+    // arguments): every launch of a wave reads the wave from d_cur, so one capture serves every wave
+    // of the same shape
+    struct WaveGraph {
+        int bounces, srp_nb;
+        const void *paths, *units, *bytes;
+        cudaGraphExec_t exec;
+        uint64_t launches;
+    };
+    std::vector<WaveGraph> graphs;
 
     float4* pix() const { return (float4*)units_mem; }
     uint32_t* taken() const { return (uint32_t*)(units_mem + up256(units.cap() * 16)); }
@@ -1687,6 +1698,7 @@ void engine_destroy(WaveEngine* e) {
     if (e->err_pin) cudaFreeHost(e->err_pin);
     for (WaveEngine::Flight& f : e->flights)
         if (f.ev) cudaEventDestroy(f.ev);
+    for (WaveEngine::WaveGraph& g : e->graphs) cudaGraphExecDestroy(g.exec);
     delete e;
 }
 
@@ -2063,7 +2075,10 @@ void engine_step(WaveEngine* e, std::vector<uint64_t>& completed) {
         const SrpPlan& SP = *sq->splan;
         srp_n = srp_wave_items(SP, e->srp_cap, sq->srp_next);
         w.n_srp_items = (uint32_t)srp_n;
-        w.srp = srp_stage(scene_view(sq->q.scene), srp_wave(SP, sq->d_att, e->srp_state, e->srp_cap, sq->srp_next, srp_n),
+        // state laid out for specular segments (as allocated) whatever the request, so that the hit
+        // mask sits at one address for every wave
+        w.srp = srp_stage(scene_view(sq->q.scene),
+                          srp_wave(SP, sq->d_att, e->srp_state, e->srp_cap, sq->srp_next, srp_n, 1),
                           (uint32_t)srp_n, SP, sq->partial, (uint32_t)sq->q.scene->n_tris);
         sq->srp_next += srp_n;
     }
@@ -2077,7 +2092,60 @@ void engine_step(WaveEngine* e, std::vector<uint64_t>& completed) {
         engine_upload(e, e->d_desc, &w, sizeof(WaveDesc));
     }
     engine_flush_uploads(e);
-    if (any_work) {
+    const bool graph = any_work && ctx->use_graphs && !ctx->counting;
+    if (graph) {
+        CRT_CUDA(cudaMemsetAsync(e->d_wave_idx, 0, 4, st));
+        const int srp_nb = sq ? (int)sq->splan->nb : -1;
+        WaveEngine::WaveGraph* g = nullptr;
+        for (size_t k = 0; k < e->graphs.size();) {
+            WaveEngine::WaveGraph& c = e->graphs[k];
+            if (c.paths != e->paths || c.units != e->units_mem || c.bytes != e->bytes_mem) {   // stale
+                cudaGraphExecDestroy(c.exec);
+                e->graphs.erase(e->graphs.begin() + (long)k);
+                continue;
+            }
+            if (c.bounces == max_bounces && c.srp_nb == srp_nb) g = &c;
+            ++k;
+        }
+        if (!g) {
+            // capture the wave's launches once for this shape: the primary trace's item bound is the
+            // largest any wave can have (its grid is the persistent one), SRP stages read the range
+            // from d_cur and launch srp_nb segments over the wave capacity
+            std::function<void()> stages;
+            uint32_t* mask = nullptr;
+            if (srp_nb >= 0) {
+                const SrpStage* d_stage = &e->d_cur->srp;
+                stages = [&, d_stage]() {
+                    srp_wave_stages_dev(ctx, d_stage, (uint32_t)e->srp_cap, (uint32_t)srp_nb, e->srp_bq,
+                                        e->srp_bcount, e->d_tqueue);
+                };
+                mask = (uint32_t*)(e->srp_state + srp_mask_offset(e->srp_cap, 1));
+            }
+            cudaGraph_t cg = nullptr;
+            cudaGraphExec_t ge = nullptr;
+            CRT_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+            const uint64_t before = ctx->launches;
+            try {
+                launch_wave_kernels(ctx, B, P, NL, 0xF0000000u, max_bounces, qa, qb, e->d_tqueue,
+                                    srp_nb >= 0 ? (uint32_t)e->srp_cap : 0u, srp_nb >= 0 ? &stages : nullptr, mask,
+                                    srp_nb >= 0 ? srp_mask_bytes(e->srp_cap) : 0);
+            } catch (...) {
+                cudaStreamEndCapture(st, &cg);
+                if (cg) cudaGraphDestroy(cg);
+                throw;
+            }
+            CRT_CUDA(cudaStreamEndCapture(st, &cg));
+            const cudaError_t ie = cudaGraphInstantiate(&ge, cg, 0);
+            cudaGraphDestroy(cg);
+            CRT_CUDA(ie);
+            e->graphs.push_back(WaveEngine::WaveGraph{max_bounces, srp_nb, e->paths, e->units_mem, e->bytes_mem, ge,
+                                                      ctx->launches - before});
+            ctx->launches = before;
+            g = &e->graphs.back();
+        }
+        CRT_CUDA(cudaGraphLaunch(g->exec, st));
+        ctx->launches += g->launches;
+    } else if (any_work) {
         CRT_CUDA(cudaMemsetAsync(e->d_wave_idx, 0, 4, st));
         std::function<void()> stages;
         if (sq) {
