@@ -545,6 +545,8 @@ class Server:
             raise CrtError(rc, self.L.crt_status_string(rc).decode())
         self.h = h
         self._inflight = {}
+        self.config = dict(lanes=int(lanes), lane_budget_bytes=int(lane_budget_bytes), max_batch=int(max_batch),
+                           count_rays=bool(count_rays), wave_paths=int(wave_paths))
 
     def scene(self, entities):
         return Scene(self.ctx, entities)
