@@ -225,3 +225,46 @@ def test_spacecraft_srp_grid4096_vs_oracle():
             assert (o_prim >= 0).any()
     finally:
         ctx.close()
+
+
+def test_batched_mix_requests_vs_oracle(ast2m):
+    """The 64-request mix of the batched configuration (renders 128^2..2048^2 at 1..64 spp with 2
+    bounces, LiDAR scans 64^2..1024^2) run as one crt_batch; every LiDAR scan and every render of at
+    most 2^20 paths is compared with the oracle: scans by the edge rule on their FP64 beams, renders
+    (the oracle's identical Philox streams) by the 4-sigma rule."""
+    ctx, sc, o, index, cfg = ast2m
+    reqs = []
+    for q in workloads.batched_config(seed=1):
+        if q["kind"] == "render":
+            reqs.append(dict(kind="render", scene=sc, camera=q["camera"], lights=q["lights"], min_samples=q["spp"],
+                             max_samples=q["spp"], noise_threshold=0.0, num_bounces=q["bounces"], seed=1,
+                             request=q["request"], radiance=True))
+        else:
+            reqs.append(dict(kind="lidar", scene=sc, position=q["position"], rotation=q["rotation"], nx=q["nx"],
+                             ny=q["ny"], half_x=q["half_x"], half_y=q["half_y"]))
+    outs, st = ctx.batch(reqs)
+    assert st["waves"] >= 1
+    renders = scans = 0
+    for q, out in zip(reqs, outs):
+        if q["kind"] == "lidar":
+            lid = dict(position=q["position"], rotation=q["rotation"], nx=q["nx"], ny=q["ny"], half_x=q["half_x"],
+                       half_y=q["half_y"])
+            rays = workloads.lidar_grid_rays(lid)
+            o_prim, o_t, o_u, o_v = o.trace_closest(rays)
+            tris = index.tris
+            pr = np.where(o_prim >= 0, o_prim, 0)
+            x = tris[pr, 0:3] - o_u[:, None] * tris[pr, 3:6] + o_v[:, None] * tris[pr, 6:9]
+            o_rng = np.where(o_prim >= 0, np.linalg.norm(x - rays[:, 0:3], axis=1), 0.0)
+            g_rng, g_prim = out[0].ravel(), out[1].ravel()
+            gp = np.where(g_prim == lib.CRT_MISS, -1, g_prim.astype(np.int64))
+            check_hits(index, rays, gp, g_rng, o_prim, o_rng, what=f"batched LiDAR {q['nx']}^2")
+            scans += 1
+        else:
+            W, H = q["camera"]["resolution"]
+            if W * H * q["max_samples"] > (1 << 20):
+                continue
+            orad, _, taken, m2 = o.render(q["camera"], q["lights"], q["min_samples"], q["max_samples"], 0.0,
+                                          q["num_bounces"], seed=1, request=q["request"], with_m2=True)
+            check_mc_radiance(out[1], orad, m2, taken, what=f"batched render {W}^2 x {q['max_samples']} spp")
+            renders += 1
+    assert scans == 32 and renders >= 10
