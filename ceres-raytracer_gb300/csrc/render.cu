@@ -444,15 +444,10 @@ __device__ __forceinline__ uint32_t block_append_buckets8(uint32_t* counter, uin
     return r;
 }
 
-__device__ __forceinline__ float maxabs3(float3 a) { return fmaxf(fabsf(a.x), fmaxf(fabsf(a.y), fabsf(a.z))); }
-
 // Flat unit normal of path p's current triangle (xyz) and the distance from its hit point to the
-// nearest edge of the triangle (barycentric x height), less an error margin for the gap between this
-// FP32 hit point and the reference's FP64 one (w): 4e-6 of the incoming ray's coordinates and length
-// over cos(incidence), plus 4e-6 |x| (10x the FP32 rounding of the ray, of the triangle and of the
-// point).  w is NaN for a degenerate triangle.  Reloads the hit and the triangle (cached) instead of
-// keeping them live in k_shade.
-__device__ __forceinline__ float4 edge_clearance(const Batch& B, int bounce, uint32_t p, const RReq& R) {
+// nearest edge of the triangle (barycentric x height, w).  w is NaN for a degenerate triangle.
+// Reloads the hit and the triangle (cached) instead of keeping them live in k_shade.
+__device__ __forceinline__ float4 edge_clearance(const Batch& B, uint32_t p, const RReq& R) {
     const float4 hv = B.hit[p];
     const float4* tp = R.sv.tris + 3ull * __float_as_uint(hv.w);
     const float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
@@ -463,18 +458,8 @@ __device__ __forceinline__ float4 edge_clearance(const Batch& B, int bounce, uin
     const float d1 = hv.y * an / sqrtf(dot3(e2, e2));            // edge p0-p2, opposite p1
     const float d2 = hv.z * an / sqrtf(dot3(e1, e1));            // edge p0-p1, opposite p2
     const float d0 = w * an / sqrtf(dot3(e1 + e2, e1 + e2));     // edge p1-p2, opposite p0
-    float3 o_in;
-    if (bounce == 0) o_in = f3(R.cam.o[0], R.cam.o[1], R.cam.o[2]);
-    else {
-        const float4 ro = B.ray[2ull * p];   // this bounce's ray: called only when it was not replaced
-        o_in = f3(ro.x, ro.y, ro.z);
-    }
-    const float3 v_in = x - o_in;
-    const float t_in = sqrtf(dot3(v_in, v_in));
-    const float cos_in = fabsf(dot3(v_in, n)) / (t_in * an);
-    const float margin = 4e-6f * ((maxabs3(o_in) + t_in) / fmaxf(cos_in, 1e-3f) + maxabs3(x));
     const float3 fn = n * (1.0f / an);   // normalize3(n), as surface_point
-    return make_float4(fn.x, fn.y, fn.z, fminf(fminf(d0, d1), d2) - margin);
+    return make_float4(fn.x, fn.y, fn.z, fminf(fminf(d0, d1), d2));
 }
 
 // Whether the reference's shadow ray toward `dir` (light at distance `dist`) stops on the triangle it
@@ -482,20 +467,25 @@ __device__ __forceinline__ float4 edge_clearance(const Batch& B, int bounce, uin
 // for c = d . n > 0 it meets that triangle's plane at t = 1e-4 / c, 1e-4 tan(theta) from x, and the
 // any-hit traversal stops there when that point lies inside the triangle (triangle.hpp:140-160, t in
 // [0, tmax]): the light is occluded by the surface itself.  The device ray starts farther off the
-// surface (origin_offset) and skips that triangle, so the crossing is decided here: inside when the
-// tangential shift is shorter than the edge clearance.  Rays whose crossing lies near an edge are traced.
+// surface (origin_offset: 4 ulps, more than 1e-4 at kilometre coordinates) and skips that triangle, so
+// the crossing is decided here, from the FP32 surface point: inside when the tangential shift is
+// shorter than the distance to the nearest edge.  Only rays that cross the plane outside the triangle
+// are traced: the reference's ray goes on there too.  (Tracing the others instead gives other answers:
+// the device's larger offset moves a grazing ray's crossing past the edge, and a ray sent through the
+// whole body can slip through an FP32 crack at its exit; within the FP32 error of the surface point
+// near an edge either answer is the reference's up to rounding.)
 __device__ __forceinline__ bool shadow_self_occluded(float3 dir, float dist, float3 flat_n, float clear) {
     const float c = dot3(dir, flat_n);
-    if (!(c > 1e-3f)) return false;
+    if (!(c > 0.0f)) return false;
     const float shift = 1.01e-4f * sqrtf(fmaxf(0.0f, 1.0f - c * c)) / c;   // 1e-4 tan(theta), +1 %
     return shift < clear && 1e-4f < 0.5f * dist * c;                       // inside; t = 1e-4 / c < tmax
 }
 
 // Of the shadow rays of path p whose lights are in `into`, those that stop on the path's own triangle
 // (shadow_self_occluded): occluded now, and dropped from the returned mask of rays to trace
-__device__ __noinline__ uint32_t mark_self_occluded(const Batch& B, int bounce, uint32_t p, const RReq& R,
-                                                    uint32_t into, uint32_t keep) {
-    const float4 nc = edge_clearance(B, bounce, p, R);
+__device__ __noinline__ uint32_t mark_self_occluded(const Batch& B, uint32_t p, const RReq& R, uint32_t into,
+                                                    uint32_t keep) {
+    const float4 nc = edge_clearance(B, p, R);
     for (uint32_t m = into; m; m &= m - 1) {
         const uint32_t l = __ffs(m) - 1;
         const size_t k = (size_t)p * B.L + l;
@@ -563,10 +553,9 @@ __device__ __forceinline__ uint32_t shade_path(const Batch& B, int bounce, uint3
         B.wgt[(bounce + 1) & 1][p] = make_float4(wt.x * bc, wt.y * bc, wt.z * bc, 0.f);
         oct = (__float_as_uint(nd.x) >> 31) | ((__float_as_uint(nd.y) >> 31) << 1) | ((__float_as_uint(nd.z) >> 31) << 2);
     }
-    // self-occluded shadow rays: at bounce 0 (incoming ray from the camera) and at the path's last
-    // bounce (its ray is not replaced above); middle bounces of longer paths are traced as they are
+    // shadow rays that stop on their own triangle (at every bounce): occluded now, not traced
     const uint32_t all = (1u << nl) - 1u;   // nl <= 16
-    const uint32_t keep = into && (bounce == 0 || !cont) ? mark_self_occluded(B, bounce, p, R, into, all) : all;
+    const uint32_t keep = into ? mark_self_occluded(B, p, R, into, all) : all;
     return keep | (oct << 16);
 }
 

@@ -318,9 +318,10 @@ def check_direct_render(index, rays, g_rad, o_rad, o_x, o_prim, g_x, g_prim, lig
          passes within the edge distance of an edge of the triangle that occludes it on either side
          (trace_o / trace_g: closest hits of [k, 8] FP64 rays -> (prim, t));
       3. for some light, its shadow ray points into the surface it leaves and crosses that triangle's
-         plane within the shade stage's decision margin (twice the device's, plus the edge distance)
-         of the triangle's edge: the reference then stops the ray on its own triangle or not by a
-         hair, and the device decides that case from FP32 data.
+         plane near the triangle's edge: within twice a bound on the FP32 error of the surface point,
+         4e-6 x ((|origin| + range) / cos(incidence) + |x|), plus the edge distance and the FP32 error
+         of the crossing's shift: the reference then stops the ray on its own triangle or not by a
+         hair, and the device decides that case from its FP32 surface point.
     Returns counts."""
     g = np.asarray(g_rad, np.float64).reshape(-1, np.asarray(g_rad).shape[-1])[:, :3]
     r = np.asarray(o_rad, np.float64).reshape(-1, np.asarray(o_rad).shape[-1])[:, :3]
@@ -367,7 +368,8 @@ def check_direct_render(index, rays, g_rad, o_rad, o_x, o_prim, g_x, g_prim, lig
         t_in = np.linalg.norm(v_in, axis=1)
         cos_in = np.abs((v_in * n_in).sum(1)) / t_in
         margin = 4e-6 * ((np.abs(rays[k, 0:3]).max(1) + t_in) / np.maximum(cos_in, 1e-3) + np.abs(ox[k]).max(1))
-        re = (c > 1e-3) & (de <= 2 * margin + s_eps)
+        shift = 1e-4 * np.sqrt(np.maximum(0.0, 1.0 - c * c)) / np.where(c > 0, c, 1.0)
+        re = (c > 0) & (de <= 2 * margin + s_eps + shift * 4e-6 / np.where(c > 0, c, 1.0))
         n_reentry += int((re & ~excused).sum())
         excused |= re
     bad = np.concatenate([left[oprim[left] < 0], k[~excused]])
