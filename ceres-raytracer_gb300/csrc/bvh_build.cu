@@ -84,40 +84,28 @@ __global__ void k_transform(const float* __restrict__ xyz, const float* __restri
         if (xf[k].first <= i) e = k;
     const EntXform& X = xf[e];
     const float* q = xyz + 9ull * i;
-    D3 p0 = {q[0], q[1], q[2]}, p1 = {q[3], q[4], q[5]}, p2 = {q[6], q[7], q[8]};
-    // Triangle(p0, p1, p2): e1 = p0 - p1, e2 = p2 - p0 (triangle.hpp:31-33)
-    D3 e1 = d3sub(p0, p1), e2 = d3sub(p2, p0);
-    // resize_triangles: p0' = s p0, p1' = s p1(), p2' = s p2() with p1() = p0 - e1, p2() = p0 + e2
-    {
-        D3 a = d3scl(p0, X.scale), b = d3scl(d3sub(p0, e1), X.scale), c = d3scl(d3add(p0, e2), X.scale);
-        p0 = a; e1 = d3sub(a, b); e2 = d3sub(c, a);
-    }
-    // rotate_triangles (also rotates vertex normals)
-    {
-        D3 a = d3rot(p0, X.rot), b = d3rot(d3sub(p0, e1), X.rot), c = d3rot(d3add(p0, e2), X.rot);
-        p0 = a; e1 = d3sub(a, b); e2 = d3sub(c, a);
-    }
-    // translate_triangles
-    {
-        D3 t = {X.pos[0], X.pos[1], X.pos[2]};
-        D3 a = d3add(p0, t), b = d3add(d3sub(p0, e1), t), c = d3add(d3add(p0, e2), t);
-        p0 = a; e1 = d3sub(a, b); e2 = d3sub(c, a);
-    }
-    D3 nn = d3cross(e1, e2);
-    geo[3ull * i + 0] = make_float4((float)p0.x, (float)p0.y, (float)p0.z, (float)e1.x);
-    geo[3ull * i + 1] = make_float4((float)e1.y, (float)e1.z, (float)e2.x, (float)e2.y);
-    geo[3ull * i + 2] = make_float4((float)e2.z, (float)nn.x, (float)nn.y, (float)nn.z);
-    // Box of the FP32 triangle as the intersection test sees it (p0, p0 - e1, p0 + e2 evaluated
-    // exactly in FP64 from the FP32 values), rounded outward.
-    double P0[3] = {(float)p0.x, (float)p0.y, (float)p0.z};
-    double E1[3] = {(float)e1.x, (float)e1.y, (float)e1.z};
-    double E2[3] = {(float)e2.x, (float)e2.y, (float)e2.z};
+    const D3 p0 = {q[0], q[1], q[2]}, p1 = {q[3], q[4], q[5]}, p2 = {q[6], q[7], q[8]};
+    // resize_triangles, rotate_triangles, translate_triangles (p' = R (s p) + t), applied to each vertex
+    // directly so that a vertex shared by several triangles gets one FP32 value in all of them (the
+    // watertight test relies on it).  The reference carries each triangle as p0, e1 = p0 - p1,
+    // e2 = p2 - p0 through the three steps (triangle.hpp:31-33, 81-82); the results differ by FP64
+    // rounding only.
+    const D3 t = {X.pos[0], X.pos[1], X.pos[2]};
+    const D3 a = d3add(d3rot(d3scl(p0, X.scale), X.rot), t);
+    const D3 b = d3add(d3rot(d3scl(p1, X.scale), X.rot), t);
+    const D3 c = d3add(d3rot(d3scl(p2, X.scale), X.rot), t);
+    const D3 nn = d3cross(d3sub(a, b), d3sub(c, a));   // n = e1 x e2
+    const float P[3][3] = {{(float)a.x, (float)a.y, (float)a.z}, {(float)b.x, (float)b.y, (float)b.z},
+                           {(float)c.x, (float)c.y, (float)c.z}};
+    geo[3ull * i + 0] = make_float4(P[0][0], P[0][1], P[0][2], P[1][0]);
+    geo[3ull * i + 1] = make_float4(P[1][1], P[1][2], P[2][0], P[2][1]);
+    geo[3ull * i + 2] = make_float4(P[2][2], (float)nn.x, (float)nn.y, (float)nn.z);
+    // box of the FP32 triangle (exact), centroid of its vertices
     float lo[3], hi[3], cc[3];
     for (int k = 0; k < 3; ++k) {
-        double a = P0[k], b = P0[k] - E1[k], c = P0[k] + E2[k];
-        lo[k] = __double2float_rd(fmin(a, fmin(b, c)));
-        hi[k] = __double2float_ru(fmax(a, fmax(b, c)));
-        cc[k] = (float)((a + b + c) * (1.0 / 3.0));
+        lo[k] = fminf(P[0][k], fminf(P[1][k], P[2][k]));
+        hi[k] = fmaxf(P[0][k], fmaxf(P[1][k], P[2][k]));
+        cc[k] = (float)(((double)P[0][k] + (double)P[1][k] + (double)P[2][k]) * (1.0 / 3.0));
     }
     box[2ull * i] = make_float4(lo[0], lo[1], lo[2], 0.f);
     box[2ull * i + 1] = make_float4(hi[0], hi[1], hi[2], 0.f);

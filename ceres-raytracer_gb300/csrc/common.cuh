@@ -167,7 +167,7 @@ struct crt_scene {
     size_t n_nodes = 0;
     uint32_t depth = 0;
     WideNode* nodes = nullptr;
-    float4* tris = nullptr;           // 3 float4 per leaf slot: (p0, e1.x) (e1.yz, e2.xy) (e2.z, n)
+    float4* tris = nullptr;           // 3 float4 per leaf slot: (p0, p1.x) (p1.yz, p2.xy) (p2.z, n)
     uint32_t* leaf_prim = nullptr;    // leaf slot -> scene primitive index
     float4* leaf_vn = nullptr;        // 3 float4 per leaf slot: vertex normals vn0, vn1, vn2 (xyz)
     uint32_t* leaf_entity = nullptr;  // leaf slot -> entity index
@@ -221,31 +221,84 @@ struct THit {
     uint32_t slot;   // CRT_MISS when nothing was hit
 };
 
-// FP32 form of Triangle::intersect (lib/bvh/triangle.hpp:140-160): c = p0 - o, r = d x c,
-// inv_det = 1 / (n . d), u = (r . e2) inv_det, v = (r . e1) inv_det, w = 1 - u - v; accepts
-// u, v, w >= 0 (comparisons reject NaN) and tmin <= t <= tmax with t = (n . c) inv_det.
-__device__ __forceinline__ bool tri_test(const float4 a, const float4 b, const float4 c4, const TRay& r, float& t,
-                                         float& u, float& v) {
-    const float3 p0 = f3(a.x, a.y, a.z);
-    const float3 e1 = f3(a.w, b.x, b.y);
-    const float3 e2 = f3(b.z, b.w, c4.x);
-    const float3 n = f3(c4.y, c4.z, c4.w);
-    const float3 c = p0 - r.o;
-    const float3 rr = cross3(r.d, c);
-    const float inv_det = 1.0f / dot3(n, r.d);
-    const float uu = dot3(rr, e2) * inv_det;
-    const float vv = dot3(rr, e1) * inv_det;
-    const float ww = 1.0f - uu - vv;
-    if (uu >= 0.0f && vv >= 0.0f && ww >= 0.0f) {
-        const float tt = dot3(n, c) * inv_det;
-        if (tt >= r.tmin && tt <= r.tmax) {
-            t = tt;
-            u = uu;
-            v = vv;
-            return true;
-        }
+// Per-ray constants of the watertight triangle test: the shear of Woop, Benthin and Wald ("Watertight
+// Ray/Triangle Intersection", JCGT 2(1), 2013) that maps the ray onto its dominant axis kz, written as
+// two vectors, x' = (p - o) . bx and y' = (p - o) . by with bx = e_kx - (d_kx / d_kz) e_kz (by
+// likewise), so the projection of a vertex needs no per-vertex permutation of components; ox, oy are
+// the projected origin (o . bx, o . by, set by the caller).
+struct TShear {
+    float3 bx, by;
+    float ox, oy;
+};
+__device__ __forceinline__ TShear make_shear(float3 d) {
+    const float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+    const int kz = ax > ay ? (ax > az ? 0 : 2) : (ay > az ? 1 : 2);
+    int kx = kz == 2 ? 0 : kz + 1, ky = kx == 2 ? 0 : kx + 1;
+    const float dz = kz == 0 ? d.x : (kz == 1 ? d.y : d.z);
+    if (dz < 0.0f) {   // keeps the winding of the projected triangle
+        const int k = kx;
+        kx = ky;
+        ky = k;
     }
-    return false;
+    const float rz = 1.0f / dz;
+    const float sx = (kx == 0 ? d.x : (kx == 1 ? d.y : d.z)) * rz;
+    const float sy = (ky == 0 ? d.x : (ky == 1 ? d.y : d.z)) * rz;
+    TShear s;
+    s.bx = f3(kx == 0 ? 1.0f : (kz == 0 ? -sx : 0.0f), kx == 1 ? 1.0f : (kz == 1 ? -sx : 0.0f),
+              kx == 2 ? 1.0f : (kz == 2 ? -sx : 0.0f));
+    s.by = f3(ky == 0 ? 1.0f : (kz == 0 ? -sy : 0.0f), ky == 1 ? 1.0f : (kz == 1 ? -sy : 0.0f),
+              ky == 2 ? 1.0f : (kz == 2 ? -sy : 0.0f));
+    return s;
+}
+
+// Point u p1 + v p2 + (1 - u - v) p0 of the triangle record (a, b, c) (passes.hpp:53), evaluated as
+// p0 + u (p1 - p0) + v (p2 - p0): the edge differences are exact for the nearby vertices of a mesh.
+__device__ __forceinline__ float3 tri_point(const float4 a, const float4 b, const float4 c, float u, float v) {
+    return f3(__fmaf_rn(v, b.z - a.x, __fmaf_rn(u, a.w - a.x, a.x)), __fmaf_rn(v, b.w - a.y, __fmaf_rn(u, b.x - a.y, a.y)),
+              __fmaf_rn(v, c.x - a.z, __fmaf_rn(u, b.y - a.z, a.z)));
+}
+
+// Watertight form of Triangle::intersect (lib/bvh/triangle.hpp:140-160), same acceptance: the ray
+// meets the triangle (barycentrics u, v, w >= 0) at tmin <= t <= tmax.  The vertices are sheared onto
+// the ray's dominant axis and moved to the ray origin (p . b - o . b, three fused multiply-adds per
+// coordinate); each vertex's 2-D image depends only on the vertex and the ray, and the edge functions
+// are products and one difference without fused multiply-adds, so the two triangles on an edge
+// compute the same value with opposite signs and no ray passes between them (the FP32 form of
+// c = p0 - o, (d x c) . e of every triangle from its own p0 leaves cracks about one ulp of the ray's
+// coordinates wide along shared edges).  A ray on an edge (an edge function exactly zero) hits both
+// sides.  The image's rounding is that of the coordinates (about 2^-24 |p|), the FP32 vertices' own.
+// t is the plane distance (n . (p0 - o)) / (n . d) as in the reference; the weights of p1 and p2 come
+// back unnormalised (wv, ww, their sum with the weight of p0 in det): u = wv / det, v = ww / det,
+// divided once for the final hit.
+__device__ __forceinline__ float shear_proj(float3 a, float3 b) {
+    return __fmaf_rn(a.z, b.z, __fmaf_rn(a.y, b.y, __fmul_rn(a.x, b.x)));
+}
+__device__ __forceinline__ float edge_fn(float px, float py, float qx, float qy) {
+    return __fsub_rn(__fmul_rn(qx, py), __fmul_rn(qy, px));
+}
+__device__ __forceinline__ bool tri_test(const float4 a, const float4 b, const float4 c4, const TRay& r,
+                                         const TShear& s, float& t, float& wv, float& ww, float& det) {
+    const float ax = __fmaf_rn(a.z, s.bx.z, __fmaf_rn(a.y, s.bx.y, __fmaf_rn(a.x, s.bx.x, -s.ox)));
+    const float ay = __fmaf_rn(a.z, s.by.z, __fmaf_rn(a.y, s.by.y, __fmaf_rn(a.x, s.by.x, -s.oy)));
+    const float bx = __fmaf_rn(b.y, s.bx.z, __fmaf_rn(b.x, s.bx.y, __fmaf_rn(a.w, s.bx.x, -s.ox)));
+    const float by = __fmaf_rn(b.y, s.by.z, __fmaf_rn(b.x, s.by.y, __fmaf_rn(a.w, s.by.x, -s.oy)));
+    const float cx = __fmaf_rn(c4.x, s.bx.z, __fmaf_rn(b.w, s.bx.y, __fmaf_rn(b.z, s.bx.x, -s.ox)));
+    const float cy = __fmaf_rn(c4.x, s.by.z, __fmaf_rn(b.w, s.by.y, __fmaf_rn(b.z, s.by.x, -s.oy)));
+    const float3 A = f3(a.x - r.o.x, a.y - r.o.y, a.z - r.o.z);
+    const float U = edge_fn(bx, by, cx, cy);   // edge p1 -> p2: weight of p0
+    const float V = edge_fn(cx, cy, ax, ay);   // edge p2 -> p0: weight of p1
+    const float W = edge_fn(ax, ay, bx, by);   // edge p0 -> p1: weight of p2
+    if (fminf(U, fminf(V, W)) < 0.0f && fmaxf(U, fmaxf(V, W)) > 0.0f) return false;
+    const float dt = U + V + W;
+    if (!(fabsf(dt) > 0.0f)) return false;   // also rejects NaN
+    const float3 n = f3(c4.y, c4.z, c4.w);
+    const float tt = __fdividef(dot3(n, A), dot3(n, r.d));
+    if (!(tt >= r.tmin && tt <= r.tmax)) return false;
+    t = tt;
+    wv = V;
+    ww = W;
+    det = dt;
+    return true;
 }
 
 // Vector::safe_inverse (lib/bvh/vector.hpp:75-80) in FP32.
@@ -316,7 +369,10 @@ __device__ __forceinline__ double plane_t64(const float4* __restrict__ tris, uin
 __device__ __forceinline__ bool bary64(const float4* __restrict__ tris, uint32_t slot, const double o[3],
                                        const double d[3], double& u, double& v) {
     const float4 a = __ldg(tris + 3ull * slot), b = __ldg(tris + 3ull * slot + 1), c4 = __ldg(tris + 3ull * slot + 2);
-    const double p0[3] = {a.x, a.y, a.z}, e1[3] = {a.w, b.x, b.y}, e2[3] = {b.z, b.w, c4.x}, n[3] = {c4.y, c4.z, c4.w};
+    const double p0[3] = {a.x, a.y, a.z}, n[3] = {c4.y, c4.z, c4.w};
+    // e1 = p0 - p1, e2 = p2 - p0 (triangle.hpp:31-33), exact in FP64 from the FP32 vertices
+    const double e1[3] = {p0[0] - (double)a.w, p0[1] - (double)b.x, p0[2] - (double)b.y};
+    const double e2[3] = {(double)b.z - p0[0], (double)b.w - p0[1], (double)c4.x - p0[2]};
     const double c[3] = {p0[0] - o[0], p0[1] - o[1], p0[2] - o[2]};
     const double r[3] = {d[1] * c[2] - d[2] * c[1], d[2] * c[0] - d[0] * c[2], d[0] * c[1] - d[1] * c[0]};
     const double det = n[0] * d[0] + n[1] * d[1] + n[2] * d[2];

@@ -26,10 +26,11 @@
 //
 // FP32 secondary-ray origins: the reference offsets the hit point by 1e-4 along the flat normal
 // (unidirectional.hpp:59-61).  In FP32 at kilometre coordinates 1e-4 is about one ulp, so the
-// offset used here is max(1e-4, 4 ulp of the largest coordinate) and the triangle the ray leaves
-// is not re-tested.  In FP64 the reference meets that triangle again when the ray points into the
-// surface; for shadow rays the shade stage decides that case itself (mark_self_occluded), other
-// rays meet the rest of the mesh, which on closed meshes occludes them anyway.
+// offset used here is max(1e-4, 4 ulp of the largest coordinate), and the triangle a bounce ray
+// leaves is not re-tested.  A shadow ray that points into the surface meets the plane of its own
+// triangle in the reference; the shade stage decides from the reference's geometry whether that
+// crossing lies inside the triangle (mark_self_occluded) and traces the others with their own
+// triangle tested like any other, so that the watertight test settles crossings at its edges.
 #include "common.cuh"
 #include "srp.cuh"
 #include "trace.cuh"
@@ -451,13 +452,13 @@ __device__ __forceinline__ float4 edge_clearance(const Batch& B, uint32_t p, con
     const float4 hv = B.hit[p];
     const float4* tp = R.sv.tris + 3ull * __float_as_uint(hv.w);
     const float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
-    const float3 p0 = f3(a.x, a.y, a.z), e1 = f3(a.w, b.x, b.y), e2 = f3(b.z, b.w, c.x), n = f3(c.y, c.z, c.w);
-    const float3 x = p0 - hv.y * e1 + hv.z * e2;   // as surface_point
+    const float3 p0 = f3(a.x, a.y, a.z), p1 = f3(a.w, b.x, b.y), p2 = f3(b.z, b.w, c.x), n = f3(c.y, c.z, c.w);
+    const float3 e1 = p0 - p1, e2 = p2 - p0;       // triangle.hpp:31-33
     const float an = sqrtf(dot3(n, n));            // twice the area
     const float w = 1.0f - hv.y - hv.z;
     const float d1 = hv.y * an / sqrtf(dot3(e2, e2));            // edge p0-p2, opposite p1
     const float d2 = hv.z * an / sqrtf(dot3(e1, e1));            // edge p0-p1, opposite p2
-    const float d0 = w * an / sqrtf(dot3(e1 + e2, e1 + e2));     // edge p1-p2, opposite p0
+    const float d0 = w * an / sqrtf(dot3(p2 - p1, p2 - p1));     // edge p1-p2, opposite p0
     const float3 fn = n * (1.0f / an);   // normalize3(n), as surface_point
     return make_float4(fn.x, fn.y, fn.z, fminf(fminf(d0, d1), d2));
 }
@@ -467,13 +468,12 @@ __device__ __forceinline__ float4 edge_clearance(const Batch& B, uint32_t p, con
 // for c = d . n > 0 it meets that triangle's plane at t = 1e-4 / c, 1e-4 tan(theta) from x, and the
 // any-hit traversal stops there when that point lies inside the triangle (triangle.hpp:140-160, t in
 // [0, tmax]): the light is occluded by the surface itself.  The device ray starts farther off the
-// surface (origin_offset: 4 ulps, more than 1e-4 at kilometre coordinates) and skips that triangle, so
-// the crossing is decided here, from the FP32 surface point: inside when the tangential shift is
-// shorter than the distance to the nearest edge.  Only rays that cross the plane outside the triangle
-// are traced: the reference's ray goes on there too.  (Tracing the others instead gives other answers:
-// the device's larger offset moves a grazing ray's crossing past the edge, and a ray sent through the
-// whole body can slip through an FP32 crack at its exit; within the FP32 error of the surface point
-// near an edge either answer is the reference's up to rounding.)
+// surface (origin_offset: 4 ulps, more than 1e-4 at kilometre coordinates), which moves a grazing
+// ray's crossing away from the hit point, so the crossing is decided here, from the FP32 surface
+// point and the reference's offset: inside when the tangential shift is shorter than the distance to
+// the nearest edge.  The rays that cross the plane outside the triangle are traced, their own
+// triangle included: the watertight test then gives a crossing at an edge to this triangle or to its
+// neighbour, never to neither (skipping this triangle would let such rays through the edge).
 __device__ __forceinline__ bool shadow_self_occluded(float3 dir, float dist, float3 flat_n, float clear) {
     const float c = dot3(dir, flat_n);
     if (!(c > 0.0f)) return false;
@@ -481,18 +481,21 @@ __device__ __forceinline__ bool shadow_self_occluded(float3 dir, float dist, flo
     return shift < clear && 1e-4f < 0.5f * dist * c;                       // inside; t = 1e-4 / c < tmax
 }
 
-// Of the shadow rays of path p whose lights are in `into`, those that stop on the path's own triangle
-// (shadow_self_occluded): occluded now, and dropped from the returned mask of rays to trace
-__device__ __noinline__ uint32_t mark_self_occluded(const Batch& B, uint32_t p, const RReq& R, uint32_t into,
+// Of the shadow rays of path p whose lights are in `cross` (rays toward the surface's plane), those
+// that stop on the path's own triangle (shadow_self_occluded) are occluded now and dropped from the
+// returned mask of rays to trace; the others are traced without skipping that triangle.
+__device__ __noinline__ uint32_t mark_self_occluded(const Batch& B, uint32_t p, const RReq& R, uint32_t cross,
                                                     uint32_t keep) {
     const float4 nc = edge_clearance(B, p, R);
-    for (uint32_t m = into; m; m &= m - 1) {
+    for (uint32_t m = cross; m; m &= m - 1) {
         const uint32_t l = __ffs(m) - 1;
         const size_t k = (size_t)p * B.L + l;
         const float4 db = B.sray[2 * k + 1];   // direction and distance as written by shade_path
         if (shadow_self_occluded(f3(db.x, db.y, db.z), db.w, f3(nc.x, nc.y, nc.z), nc.w)) {
             B.occ[k] = 1;
             keep &= ~(1u << l);
+        } else {
+            B.sray[2 * k].w = __uint_as_float(CRT_MISS);
         }
     }
     return keep;
@@ -511,7 +514,7 @@ __device__ __forceinline__ uint32_t shade_path(const Batch& B, int bounce, uint3
     const float3 col = f3(E.color[0], E.color[1], E.color[2]);
     const float3 x = sp.x - origin_offset(sp.x) * sp.flat_n;   // intersect_point - 1e-4 normal
     const uint32_t nl = R.n_lights;
-    uint32_t into = 0;   // lights whose shadow ray points into the surface
+    uint32_t cross = 0;   // lights whose shadow ray points into the plane of the triangle
     uint32_t oct = 0;    // octant of the bounce ray
     for (uint32_t l = 0; l < nl; ++l) {
         const LightDev& lt = B.lights[R.light_base + l];
@@ -536,7 +539,7 @@ __device__ __forceinline__ uint32_t shade_path(const Batch& B, int bounce, uint3
         const float3 cb = col * ldn;
         B.contrib[(size_t)p * B.L + l] = make_float4(cb.x * inten, cb.y * inten, cb.z * inten, 0.f);
         B.occ[(size_t)p * B.L + l] = 0;
-        if (ldn < 0.0f) into |= 1u << l;   // towards the surface (shading normal): checked below
+        if (dot3(dir, sp.flat_n) > 0.0f) cross |= 1u << l;   // checked below
         const size_t k = (size_t)p * B.L + l;
         B.sray[2 * k] = make_float4(x.x, x.y, x.z, __uint_as_float(h.slot));   // tmin 0; skip the origin triangle
         B.sray[2 * k + 1] = make_float4(dir.x, dir.y, dir.z, dist);
@@ -555,7 +558,7 @@ __device__ __forceinline__ uint32_t shade_path(const Batch& B, int bounce, uint3
     }
     // shadow rays that stop on their own triangle (at every bounce): occluded now, not traced
     const uint32_t all = (1u << nl) - 1u;   // nl <= 16
-    const uint32_t keep = into ? mark_self_occluded(B, p, R, into, all) : all;
+    const uint32_t keep = cross ? mark_self_occluded(B, p, R, cross, all) : all;
     return keep | (oct << 16);
 }
 

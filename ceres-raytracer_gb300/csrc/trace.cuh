@@ -48,9 +48,9 @@ __device__ __forceinline__ SurfacePoint surface_point(const SceneView& sv, const
     SurfacePoint sp;
     const float4* tp = sv.tris + 3ull * h.slot;
     const float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
-    const float3 p0 = f3(a.x, a.y, a.z), e1 = f3(a.w, b.x, b.y), e2 = f3(b.z, b.w, c.x), n = f3(c.y, c.z, c.w);
-    // u (p0 - e1) + v (p0 + e2) + (1 - u - v) p0 = p0 - u e1 + v e2
-    sp.x = p0 - h.u * e1 + h.v * e2;
+    const float3 p0 = f3(a.x, a.y, a.z), n = f3(c.y, c.z, c.w);
+    // u p1 + v p2 + (1 - u - v) p0 = p0 + u (p1 - p0) + v (p2 - p0)
+    sp.x = tri_point(a, b, c, h.u, h.v);
     sp.flat_n = normalize3(n);
     sp.entity = __ldg(sv.leaf_entity + h.slot);
     const EntityDev& E = sv.entities[sp.entity];

@@ -38,6 +38,14 @@ __device__ __forceinline__ float byte_f15(uint32_t w, int k) {
     return __uint_as_float(__byte_perm(w, 0x47000000u, 0x7404u | ((uint32_t)k << 4)));
 }
 
+// barycentrics of a hit from tri_test's weights
+__device__ __forceinline__ THit normalized(THit h, float det) {
+    const float inv = 1.0f / det;
+    h.u *= inv;
+    h.v *= inv;
+    return h;
+}
+
 template <bool ANY, bool COUNT>
 __device__ __forceinline__ THit traverse(const SceneView& sv, TRay ray, uint2* __restrict__ sstack, int sstride,
                                          TravStats& st, uint32_t* __restrict__ err) {
@@ -49,10 +57,14 @@ __device__ __forceinline__ THit traverse(const SceneView& sv, TRay ray, uint2* _
     const uint32_t oct = (__float_as_uint(ray.d.x) >> 31) | ((__float_as_uint(ray.d.y) >> 31) << 1) |
                          ((__float_as_uint(ray.d.z) >> 31) << 2);
     const float3 idir = f3(safe_rcp(ray.d.x), safe_rcp(ray.d.y), safe_rcp(ray.d.z));
+    TShear shear = make_shear(ray.d);
+    shear.ox = shear_proj(ray.o, shear.bx);
+    shear.oy = shear_proj(ray.o, shear.by);
     uint2 lstack[CRT_STACK_TOTAL - CRT_STACK_SMEM];
     int sp = 0;
     // root = slot 0 of a virtual parent whose children start at node 0
     uint2 ngroup = make_uint2(0u, (1u << (24u + oct)) | 1u);
+    float hit_det = 1.0f;   // weight sum of the hit's barycentrics (tri_test)
     uint2 tgroup = make_uint2(0u, 0u);
     while (true) {
         // ---- leaf triangles of the last visited node
@@ -64,13 +76,14 @@ __device__ __forceinline__ THit traverse(const SceneView& sv, TRay ray, uint2* _
             const float4* tp = sv.tris + 3ull * slot;
             const float4 a = __ldg(tp), bb = __ldg(tp + 1), c = __ldg(tp + 2);
             if (COUNT) st.tris++;
-            float t, u, v;
-            if (tri_test(a, bb, c, ray, t, u, v)) {
+            float t, wv, ww, det;
+            if (tri_test(a, bb, c, ray, shear, t, wv, ww, det)) {
                 hit.t = t;
-                hit.u = u;
-                hit.v = v;
+                hit.u = wv;
+                hit.v = ww;
+                hit_det = det;
                 hit.slot = slot;
-                if (ANY) return hit;
+                if (ANY) return normalized(hit, hit_det);
                 ray.tmax = t;
             }
         }
@@ -90,7 +103,7 @@ __device__ __forceinline__ THit traverse(const SceneView& sv, TRay ray, uint2* _
             else if (sp < CRT_STACK_TOTAL) lstack[sp - CRT_STACK_SMEM] = ngroup;
             else {
                 atomicOr(err, (uint32_t)DEVERR_STACK_OVERFLOW);
-                return hit;
+                return normalized(hit, hit_det);
             }
             ++sp;
         }
@@ -139,5 +152,5 @@ __device__ __forceinline__ THit traverse(const SceneView& sv, TRay ray, uint2* _
         ngroup = make_uint2(__float_as_uint(w1.x), (hitmask & 0xFF000000u) | imask);
         tgroup = make_uint2(__float_as_uint(w1.y), hitmask & 0x00FFFFFFu);
     }
-    return hit;
+    return normalized(hit, hit_det);
 }

@@ -265,6 +265,7 @@ def test_batched_mix_requests_vs_oracle(ast2m):
                 continue
             orad, _, taken, m2 = o.render(q["camera"], q["lights"], q["min_samples"], q["max_samples"], 0.0,
                                           q["num_bounces"], seed=1, request=q["request"], with_m2=True)
-            check_mc_radiance(out[1], orad, m2, taken, what=f"batched render {W}^2 x {q['max_samples']} spp")
+            st = check_mc_radiance(out[1], orad, m2, taken, what=f"batched render {W}^2 x {q['max_samples']} spp")
+            print(f"batched render {W}^2 x {q['max_samples']} spp", st)
             renders += 1
     assert scans == 32 and renders >= 10
