@@ -27,10 +27,12 @@
 // FP32 secondary-ray origins: the reference offsets the hit point by 1e-4 along the flat normal
 // (unidirectional.hpp:59-61).  In FP32 at kilometre coordinates 1e-4 is about one ulp, so the
 // offset used here is max(1e-4, 4 ulp of the largest coordinate), and the triangle a bounce ray
-// leaves is not re-tested.  A shadow ray that points into the surface meets the plane of its own
-// triangle in the reference; the shade stage decides from the reference's geometry whether that
-// crossing lies inside the triangle (mark_self_occluded) and traces the others with their own
-// triangle tested like any other, so that the watertight test settles crossings at its edges.
+// leaves is not re-tested unless the ray points into its plane (smooth shading: the reference then
+// meets that triangle again, and so does the device ray).  A shadow ray that points into the surface
+// meets the plane of its own triangle in the reference; the shade stage decides from the reference's
+// geometry whether that crossing lies inside the triangle (mark_self_occluded) and traces the others
+// with their own triangle tested like any other, so that the watertight test settles crossings at
+// its edges.
 #include "common.cuh"
 #include "srp.cuh"
 #include "trace.cuh"
@@ -550,7 +552,9 @@ __device__ __forceinline__ uint32_t shade_path(const Batch& B, int bounce, uint3
         const float3 nd = cosine_importance(sp.shading_n, r1, r2);
         B.ray[2ull * p] = make_float4(x.x, x.y, x.z, 0.f);
         B.ray[2ull * p + 1] = make_float4(nd.x, nd.y, nd.z, 3.402823466e38f);
-        B.skip[p] = h.slot;
+        // the triangle the ray leaves is not tested, unless the ray points into its plane (a direction
+        // sampled about a smooth-shading normal): the reference meets that triangle again there
+        B.skip[p] = dot3(nd, sp.flat_n) > 0.0f ? CRT_MISS : h.slot;
         const float bc = 1.0f - r1;
         const float4 wt = path_weight(B, p, bounce);
         B.wgt[(bounce + 1) & 1][p] = make_float4(wt.x * bc, wt.y * bc, wt.z * bc, 0.f);

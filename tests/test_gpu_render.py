@@ -212,18 +212,20 @@ def test_terminator_shadow_rays_resolved_in_shade(ctx):
     assert shadow < 0.9 * hits
 
 
-def test_smooth_shaded_two_bounce_render_vs_oracle(ctx):
-    """Smooth-shaded asteroid, 2 bounces, the oracle's random streams: bounce directions sampled about
-    the interpolated normal can point into the flat surface they leave (the reference then meets its
-    own triangle again); per-pixel radiance within 4 sigma, image mean within 0.5 %."""
+@pytest.mark.parametrize("bounces", [2, 3])
+def test_smooth_shaded_multi_bounce_render_vs_oracle(ctx, bounces):
+    """Smooth-shaded asteroid, 2 and 3 bounces, 128^2 x 32 spp, the oracle's random streams: bounce
+    directions sampled about the interpolated normal can point into the flat surface they leave (the
+    reference then meets its own triangle again, and so does the device ray, which tests that
+    triangle in this case); per-pixel radiance within 4 sigma, image mean within 0.5 %."""
     ents = [scenes.EntitySpec("a", scenes.asteroid(100_000, seed=3), (0.3, 0.3, 0.3), smooth=True)]
     sc, o = ctx.scene(ents), oracle.Scene(ents)
     view = scenes.unit_vector(21)
     sun = view + 0.5 * scenes.unit_vector(22)   # lit from near the camera: most of the view is sunlit
     sun /= np.linalg.norm(sun)
     lights = [dict(type="point", intensity=1.0e18, position=1.0e9 * sun)]
-    cam = scenes.fov_camera(scenes.TAN5 * 2.4, (48, 48), 5000.0 * view, (0.0, 0.0, 0.0))
-    _, rad = sc.render(cam, lights, 4, 4, 0.0, 2, seed=11)
-    orad, _, _, m2 = o.render(cam, lights, 4, 4, 0.0, 2, seed=11, with_m2=True)
+    cam = scenes.fov_camera(scenes.TAN5 * 2.4, (128, 128), 5000.0 * view, (0.0, 0.0, 0.0))
+    _, rad = sc.render(cam, lights, 32, 32, 0.0, bounces, seed=11)
+    orad, _, _, m2 = o.render(cam, lights, 32, 32, 0.0, bounces, seed=11, with_m2=True)
     assert (orad[..., 0] > 0).mean() > 0.5
-    check_mc_radiance(rad, orad, m2, 4, what="smooth-shaded 2-bounce asteroid")
+    check_mc_radiance(rad, orad, m2, 32, what=f"smooth-shaded {bounces}-bounce asteroid")
