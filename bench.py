@@ -492,6 +492,11 @@ def gpu_arm(args):
                     issue_active_pct=prof.get("issue_active_pct"),
                     binding="SM instruction issue (ncu issue-active % above; DRAM and L2 fractions low)")
 
+    # ---- end to end through the public crt API (host numpy outputs), right after the step it repeats
+    e2e = None
+    if not args.no_e2e and rank == 0:
+        e2e = e2e_measure(args, ents, cfg, rays_step)
+
     # ---- batched vs per-call on the config-3 request set
     batched = None
     if not args.no_batched and rank == 0:
@@ -508,11 +513,6 @@ def gpu_arm(args):
     served = None
     if not args.no_served and rank == 0:
         served = served_measure(args, local)
-
-    # ---- end to end through the public crt API (host numpy outputs)
-    e2e = None
-    if not args.no_e2e and rank == 0:
-        e2e = e2e_measure(args, ents, cfg, rays_step)
 
     line = None
     if rank == 0:
@@ -995,7 +995,7 @@ def e2e_measure(args, ents, cfg, rays_step):
     for _ in range(max(3, args.warmup)):
         img = group.render(camera, light, 1, 1, 1.0, cfg["bounces"])
         rng, prim = group.lidar_scan(lidar)
-    n = max(3, min(args.steps, 20))
+    n = max(3, min(args.steps, 50))
     t = time.perf_counter()
     for _ in range(n):
         img = group.render(camera, light, 1, 1, 1.0, cfg["bounces"])

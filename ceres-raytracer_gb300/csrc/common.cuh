@@ -112,10 +112,17 @@ struct PinnedStaging {
     PinnedStaging& operator=(const PinnedStaging&) = delete;
 };
 bool is_device_ptr(const void* p);
+// Page-locked host memory that the device writes at the same address (cudaHostAlloc'd or registered).
+bool is_host_mapped(const void* p);
+// Host memory (any kind): a call writing it completes before returning.
+inline bool host_output(const void* p) { return p && !is_device_ptr(p); }
 // Copy helpers: ensure `bytes` of `src` are readable on the device; return a device pointer.
 const void* to_device(crt_context* ctx, const void* src, size_t bytes, ScratchSlot slot);
 // Output staging: returns a device pointer to write into (dst itself when it is device memory).
 void* out_device(crt_context* ctx, void* dst, size_t bytes, ScratchSlot slot);
+// As out_device, and dst itself also when it is mapped page-locked host memory: the kernel's stores
+// cross the host link while it runs, instead of a copy after it (outputs written once, not read).
+void* out_direct(crt_context* ctx, void* dst, size_t bytes, ScratchSlot slot);
 // Copy a staged output back to host memory (no-op for device outputs); synchronous for host outputs.
 void out_finish(crt_context* ctx, void* dst, const void* staged, size_t bytes);
 void check_launch(crt_context* ctx, const char* what);

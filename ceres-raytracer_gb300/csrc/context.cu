@@ -60,6 +60,16 @@ bool is_device_ptr(const void* p) {
     return attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged;
 }
 
+bool is_host_mapped(const void* p) {
+    if (!p) return false;
+    cudaPointerAttributes attr;
+    if (cudaPointerGetAttributes(&attr, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return attr.type == cudaMemoryTypeHost && attr.devicePointer == p;
+}
+
 const void* to_device(crt_context* ctx, const void* src, size_t bytes, ScratchSlot slot) {
     if (!src || bytes == 0) return src;
     if (is_device_ptr(src)) return src;
@@ -71,6 +81,12 @@ const void* to_device(crt_context* ctx, const void* src, size_t bytes, ScratchSl
 void* out_device(crt_context* ctx, void* dst, size_t bytes, ScratchSlot slot) {
     if (!dst) return nullptr;
     if (is_device_ptr(dst)) return dst;
+    return ctx_scratch(ctx, slot, bytes);
+}
+
+void* out_direct(crt_context* ctx, void* dst, size_t bytes, ScratchSlot slot) {
+    if (!dst) return nullptr;
+    if (is_device_ptr(dst) || is_host_mapped(dst)) return dst;
     return ctx_scratch(ctx, slot, bytes);
 }
 

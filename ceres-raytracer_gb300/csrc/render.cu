@@ -869,6 +869,11 @@ void check_request(const crt_request& q) {
     }
 }
 
+// Outputs the kernels write in place: device memory, or mapped page-locked host memory (k_finalize and
+// the LiDAR trace store each value once, so the stores cross the host link while the kernels run and
+// no copy follows); other host memory is staged in device scratch and copied back.
+bool direct_out(const void* p) { return is_device_ptr(p) || is_host_mapped(p); }
+
 // srps: SRP requests of a mixed batch (crt_batch_mixed); their sun rays ride in the waves' primary
 // traces after the LiDAR beams and camera paths, one request's item range per wave.
 void run_batch(crt_context* ctx, const crt_request* reqs, size_t n, crt_batch_stats* stats,
@@ -925,8 +930,8 @@ void run_batch(crt_context* ctx, const crt_request* reqs, size_t n, crt_batch_st
             pix_total += R.npix;
             R.rgba = nullptr;
             R.rad = nullptr;
-            if (q.rgba8 && !is_device_ptr(q.rgba8)) host_out_bytes += (size_t)R.npix * 4;
-            if (q.radiance && !is_device_ptr(q.radiance)) host_out_bytes += (size_t)R.npix * 16;
+            if (q.rgba8 && !direct_out(q.rgba8)) host_out_bytes += (size_t)R.npix * 4;
+            if (q.radiance && !direct_out(q.radiance)) host_out_bytes += (size_t)R.npix * 16;
             HostReq h;
             h.src = &q;
             h.adaptive = p.noise_threshold > 0 && p.min_samples < p.max_samples;
@@ -955,8 +960,8 @@ void run_batch(crt_context* ctx, const crt_request* reqs, size_t n, crt_batch_st
             lidar_items += tiles_items(g.nx, g.ny);
             Lq.range = nullptr;
             Lq.prim = nullptr;
-            if (!is_device_ptr(q.range)) host_out_bytes += (size_t)g.nx * g.ny * 8;
-            if (q.prim && !is_device_ptr(q.prim)) host_out_bytes += (size_t)g.nx * g.ny * 4;
+            if (!direct_out(q.range)) host_out_bytes += (size_t)g.nx * g.ny * 8;
+            if (q.prim && !direct_out(q.prim)) host_out_bytes += (size_t)g.nx * g.ny * 4;
             lr.push_back(Lq);
         }
     }
@@ -1112,21 +1117,21 @@ void run_batch(crt_context* ctx, const crt_request* reqs, size_t n, crt_batch_st
         if (q.kind == CRT_REQUEST_RENDER) {
             RReq& R = rr[ri++];
             if (q.rgba8) {
-                if (is_device_ptr(q.rgba8)) R.rgba = (uchar4*)q.rgba8;
+                if (direct_out(q.rgba8)) R.rgba = (uchar4*)q.rgba8;
                 else { R.rgba = (uchar4*)(stage + stage_off); stage_off += (size_t)R.npix * 4; }
             }
             if (q.radiance) {
                 stage_off = (stage_off + 15) & ~size_t(15);
-                if (is_device_ptr(q.radiance)) R.rad = (float4*)q.radiance;
+                if (direct_out(q.radiance)) R.rad = (float4*)q.radiance;
                 else { R.rad = (float4*)(stage + stage_off); stage_off += (size_t)R.npix * 16; }
             }
         } else {
             LReq& Lq = lr[li++];
             stage_off = (stage_off + 15) & ~size_t(15);
-            if (is_device_ptr(q.range)) Lq.range = q.range;
+            if (direct_out(q.range)) Lq.range = q.range;
             else { Lq.range = (double*)(stage + stage_off); stage_off += (size_t)Lq.nx * Lq.ny * 8; }
             if (q.prim) {
-                if (is_device_ptr(q.prim)) Lq.prim = q.prim;
+                if (direct_out(q.prim)) Lq.prim = q.prim;
                 else { Lq.prim = (uint32_t*)(stage + stage_off); stage_off += (size_t)Lq.nx * Lq.ny * 4; }
             }
         }
@@ -1320,12 +1325,14 @@ void run_batch(crt_context* ctx, const crt_request* reqs, size_t n, crt_batch_st
         const crt_request& q = reqs[i];
         if (q.kind == CRT_REQUEST_RENDER) {
             const RReq& R = rr[ri++];
-            if (q.rgba8 && (void*)R.rgba != (void*)q.rgba8) { out_finish(ctx, q.rgba8, R.rgba, (size_t)R.npix * 4); host_out = true; }
-            if (q.radiance && (void*)R.rad != (void*)q.radiance) { out_finish(ctx, q.radiance, R.rad, (size_t)R.npix * 16); host_out = true; }
+            if (q.rgba8 && (void*)R.rgba != (void*)q.rgba8) out_finish(ctx, q.rgba8, R.rgba, (size_t)R.npix * 4);
+            if (q.radiance && (void*)R.rad != (void*)q.radiance) out_finish(ctx, q.radiance, R.rad, (size_t)R.npix * 16);
+            host_out = host_out || host_output(q.rgba8) || host_output(q.radiance);
         } else {
             const LReq& Lq = lr[li++];
-            if ((void*)Lq.range != (void*)q.range) { out_finish(ctx, q.range, Lq.range, (size_t)Lq.nx * Lq.ny * 8); host_out = true; }
-            if (q.prim && (void*)Lq.prim != (void*)q.prim) { out_finish(ctx, q.prim, Lq.prim, (size_t)Lq.nx * Lq.ny * 4); host_out = true; }
+            if ((void*)Lq.range != (void*)q.range) out_finish(ctx, q.range, Lq.range, (size_t)Lq.nx * Lq.ny * 8);
+            if (q.prim && (void*)Lq.prim != (void*)q.prim) out_finish(ctx, q.prim, Lq.prim, (size_t)Lq.nx * Lq.ny * 4);
+            host_out = host_out || host_output(q.range) || host_output(q.prim);
         }
     }
     for (size_t j = 0; j < n_srp; ++j) {   // per-attitude totals in a fixed order, as crt_srp

@@ -231,10 +231,10 @@ int crt_trace_closest(crt_scene* s, const crt_ray* rays, size_t n, crt_hit* hits
         if (!n) return;
         CRT_CUDA(cudaSetDevice(ctx->device));
         const float4* d_rays = (const float4*)to_device(ctx, rays, n * sizeof(crt_ray), SCR_IN0);
-        crt_hit* d_hits = (crt_hit*)out_device(ctx, hits, n * sizeof(crt_hit), SCR_OUT0);
+        crt_hit* d_hits = (crt_hit*)out_direct(ctx, hits, n * sizeof(crt_hit), SCR_OUT0);
         launch_trace<false>(s, RayClosestJob{{}, d_rays, d_hits}, (uint32_t)n);
         out_finish(ctx, hits, d_hits, n * sizeof(crt_hit));
-        finish(ctx, d_hits != (void*)hits, "crt_trace_closest");
+        finish(ctx, host_output(hits), "crt_trace_closest");
     });
 }
 
@@ -247,10 +247,10 @@ int crt_trace_any(crt_scene* s, const crt_ray* rays, size_t n, uint8_t* occluded
         if (!n) return;
         CRT_CUDA(cudaSetDevice(ctx->device));
         const float4* d_rays = (const float4*)to_device(ctx, rays, n * sizeof(crt_ray), SCR_IN0);
-        uint8_t* d_occ = (uint8_t*)out_device(ctx, occluded, n, SCR_OUT0);
+        uint8_t* d_occ = (uint8_t*)out_direct(ctx, occluded, n, SCR_OUT0);
         launch_trace<true>(s, RayAnyJob{{}, d_rays, d_occ}, (uint32_t)n);
         out_finish(ctx, occluded, d_occ, n);
-        finish(ctx, d_occ != occluded, "crt_trace_any");
+        finish(ctx, host_output(occluded), "crt_trace_any");
     });
 }
 
@@ -265,14 +265,14 @@ int crt_passes(crt_scene* s, const crt_camera_desc* cam, double* xyz, uint32_t* 
                   CRT_ERR_INVALID, "camera pose or intrinsics are not finite");
         CRT_CUDA(cudaSetDevice(ctx->device));
         const size_t np = (size_t)cb.width * cb.height;
-        double* d_xyz = (double*)out_device(ctx, xyz, np * 24, SCR_OUT0);
-        uint32_t* d_ids = (uint32_t*)out_device(ctx, ids, np * 4, SCR_OUT1);
-        double* d_nrm = (double*)out_device(ctx, normals, np * 24, SCR_OUT2);
+        double* d_xyz = (double*)out_direct(ctx, xyz, np * 24, SCR_OUT0);
+        uint32_t* d_ids = (uint32_t*)out_direct(ctx, ids, np * 4, SCR_OUT1);
+        double* d_nrm = (double*)out_direct(ctx, normals, np * 24, SCR_OUT2);
         launch_trace<false>(s, PassJob{{}, cb, d_xyz, d_ids, d_nrm}, tiles_items(cb.width, cb.height));
         out_finish(ctx, xyz, d_xyz, np * 24);
         out_finish(ctx, ids, d_ids, np * 4);
         out_finish(ctx, normals, d_nrm, np * 24);
-        finish(ctx, (xyz && d_xyz != xyz) || (ids && d_ids != ids) || (normals && d_nrm != normals), "crt_passes");
+        finish(ctx, host_output(xyz) || host_output(ids) || host_output(normals), "crt_passes");
     });
 }
 
@@ -287,12 +287,12 @@ int crt_lidar_batch(crt_scene* s, const double* positions, const double* rotatio
         CRT_CUDA(cudaSetDevice(ctx->device));
         const double* d_pos = (const double*)to_device(ctx, positions, n * 24, SCR_IN0);
         const double* d_rot = (const double*)to_device(ctx, rotations, n * 72, SCR_IN1);
-        double* d_rng = (double*)out_device(ctx, range, n * 8, SCR_OUT0);
-        uint32_t* d_prim = (uint32_t*)out_device(ctx, prim, n * 4, SCR_OUT1);
+        double* d_rng = (double*)out_direct(ctx, range, n * 8, SCR_OUT0);
+        uint32_t* d_prim = (uint32_t*)out_direct(ctx, prim, n * 4, SCR_OUT1);
         launch_trace<false>(s, LidarBatchJob{{}, d_pos, d_rot, z_positive ? 1.0f : -1.0f, d_rng, d_prim}, (uint32_t)n);
         out_finish(ctx, range, d_rng, n * 8);
         out_finish(ctx, prim, d_prim, n * 4);
-        finish(ctx, d_rng != range || (prim && d_prim != prim), "crt_lidar_batch");
+        finish(ctx, host_output(range) || host_output(prim), "crt_lidar_batch");
     });
 }
 
@@ -319,12 +319,12 @@ int crt_lidar_grid(crt_scene* s, const crt_lidar_grid_desc* g, double* range, ui
         J.tx = d_tan;
         J.ty = d_tan + g->nx;
         const size_t nb = (size_t)g->nx * g->ny;
-        J.range = (double*)out_device(ctx, range, nb * 8, SCR_OUT0);
-        J.prim = (uint32_t*)out_device(ctx, prim, nb * 4, SCR_OUT1);
+        J.range = (double*)out_direct(ctx, range, nb * 8, SCR_OUT0);
+        J.prim = (uint32_t*)out_direct(ctx, prim, nb * 4, SCR_OUT1);
         launch_trace<false>(s, J, tiles_items(g->nx, g->ny));
         out_finish(ctx, range, J.range, nb * 8);
         out_finish(ctx, prim, J.prim, nb * 4);
-        finish(ctx, J.range != range || (prim && J.prim != prim), "crt_lidar_grid");
+        finish(ctx, host_output(range) || host_output(prim), "crt_lidar_grid");
     });
 }
 
