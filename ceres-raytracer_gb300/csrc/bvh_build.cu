@@ -3,8 +3,8 @@
 // parallel_reinsertion_optimizer.hpp:140-211, node_layout_optimizer.hpp:30-92).
 //
 // Pipeline, one stream, no host round trips except one frontier count per collapse level:
-//   k_transform      entity transform chain in FP64 (transform.hpp:43-85), FP32 triangle
-//                    records (p0, e1, e2, n), conservative FP32 boxes, centroids, normals
+//   k_transform      entity transform in FP64 (transform.hpp:43-85), FP32 triangle records
+//                    (p0, p1, p2, n), exact FP32 boxes, centroids, normals
 //   k_bounds         scene and centroid bounds (order-preserving integer atomics)
 //   k_morton         30-bit Morton codes of centroids in the centroid bounds
 //   radix_sort       stable LSD radix sort, 8-bit digits, 4 passes (histogram / scan / scatter)
