@@ -34,7 +34,10 @@ for _p in (PKG, REPO):
 
 METRIC = "Mrays/s and p50/p99 request latency, batched/served vs per-call GPU, one GB300"
 UNIT = "Mrays/s"
+# algorithmic bytes per unit of work: an 8-wide node's planes as bytes (80 B), a triangle (48 B), a ray
+# (32 B) and its hit (16 B); the node as stored is 128 B (planes as halves: NODE_BYTES_STORED)
 NODE_BYTES, TRI_BYTES, RAY_BYTES, HIT_BYTES = 80, 48, 32, 16
+NODE_BYTES_STORED = 128
 
 
 def parse():
@@ -475,8 +478,10 @@ def gpu_arm(args):
             "kernel": "k_trace<closest> on 2048^2 primary camera rays in 8x4 tiles (crt_trace_closest)",
             "bytes_per_ray": round(b_ray, 1), "nodes_per_ray": round(nodes_ray, 2), "tris_per_ray": round(tris_ray, 2),
             "kernel_ms": round(t_kernel * 1e3, 3), "kernel_mrays_s": round(cnt["rays"] / t_kernel / 1e6, 1),
-            "frac_note": "algorithmic bytes (80 B per node and 48 B per triangle fetched, 48 B ray + hit) over "
-                         "the measured HBM copy bandwidth; most are served from L1 / L2, see dram_frac / l2_frac",
+            "bytes_per_ray_stored": round(NODE_BYTES_STORED * nodes_ray + TRI_BYTES * tris_ray + RAY_BYTES + HIT_BYTES, 1),
+            "frac_note": "algorithmic bytes (80 B per node: its planes as bytes, as the node is 128 B stored with "
+                         "planes as halves; 48 B per triangle, 48 B ray + hit) over the measured HBM copy "
+                         "bandwidth; most are served from L1 / L2, see dram_frac / l2_frac",
             "read_peaks_gbs": pk}
     if prof.get("dram_bytes") and prof.get("lts_bytes"):
         # the ncu capture's bytes for one launch of this kernel on these rays, over the time measured here

@@ -913,12 +913,16 @@ __global__ void k_collapse(CollapseArgs A, const int2* __restrict__ frontier, ui
     w.w[0] = make_float4(p[0], p[1], p[2], __uint_as_float(eword));
     w.w[1] = make_float4(__uint_as_float(child_base), __uint_as_float(tri_base), __uint_as_float(pack4(meta)),
                          __uint_as_float(pack4(meta + 4)));
-    w.w[2] = make_float4(__uint_as_float(pack4(qlo[0])), __uint_as_float(pack4(qlo[0] + 4)),
-                         __uint_as_float(pack4(qlo[1])), __uint_as_float(pack4(qlo[1] + 4)));
-    w.w[3] = make_float4(__uint_as_float(pack4(qlo[2])), __uint_as_float(pack4(qlo[2] + 4)),
-                         __uint_as_float(pack4(qhi[0])), __uint_as_float(pack4(qhi[0] + 4)));
-    w.w[4] = make_float4(__uint_as_float(pack4(qhi[1])), __uint_as_float(pack4(qhi[1] + 4)),
-                         __uint_as_float(pack4(qhi[2])), __uint_as_float(pack4(qhi[2] + 4)));
+    // planes: per axis 8 halves 0x5C00 | q (= 256 + q / 4), lo x/y/z then hi x/y/z
+    auto pack_h = [](const uint8_t* b) {
+        uint32_t v[4];
+        for (int j = 0; j < 4; ++j) v[j] = (0x5C00u | b[2 * j]) | ((0x5C00u | b[2 * j + 1]) << 16);
+        return make_float4(__uint_as_float(v[0]), __uint_as_float(v[1]), __uint_as_float(v[2]), __uint_as_float(v[3]));
+    };
+    for (int a = 0; a < 3; ++a) {
+        w.w[2 + a] = pack_h(qlo[a]);
+        w.w[5 + a] = pack_h(qhi[a]);
+    }
     A.nodes[wnode] = w;
 }
 

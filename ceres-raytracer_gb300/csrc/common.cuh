@@ -147,17 +147,20 @@ int crt_guard(crt_context* ctx, F&& f) {
 }
 
 // ------------------------------------------------------------------ scene
-// 8-wide compressed node, 80 bytes = 5 x float4:
+// 8-wide compressed node, 128 bytes = 8 x float4:
 //  w0: origin p (float x3), exponents ex/ey/ez (int8) + imask (uint8)
 //  w1: child_base (uint32), tri_base (uint32), meta[0..7] (uint8)
-//  w2: qlo_x[8], qlo_y[8]     w3: qlo_z[8], qhi_x[8]     w4: qhi_y[8], qhi_z[8]
+//  w2..w4: qlo_x[8], qlo_y[8], qlo_z[8]     w5..w7: qhi_x[8], qhi_y[8], qhi_z[8]
+//  each plane q (0..255, in quanta 2^e from p) stored as the half 0x5C00 | q = 256 + q / 4: the
+//  traversal converts it with one half-to-float conversion on the FMA pipe, where a byte extraction
+//  (PRMT) would load the ALU pipe that the slab test's min / max already keeps busy.
 // meta per slot: 0 = empty; internal child: (1 << 5) | (24 + slot);
 //                leaf: (unary triangle count << 5) | offset from tri_base (< 24).
 // Internal children are stored contiguously from child_base in slot order.
 struct WideNode {
-    float4 w[5];
+    float4 w[8];
 };
-static_assert(sizeof(WideNode) == 80, "wide node must be 80 bytes");
+static_assert(sizeof(WideNode) == 128, "wide node must be 128 bytes");
 
 struct EntityDev {
     float color[3];

@@ -7,9 +7,11 @@
 #ifndef CRT_TRACE_BLOCK
 #define CRT_TRACE_BLOCK 128
 #endif
-// resident blocks per SM the trace kernel is compiled for (registers per thread: 65536 / (128 x 8) = 64)
+// resident blocks per SM the trace kernel is compiled for (registers per thread: 65536 / (128 x 7),
+// 72 after allocation granularity).  With the half-precision plane rows of the 8-wide node, 8 blocks
+// (64 registers) spill in the traversal loop and lose more than the eighth block's warps bring.
 #ifndef CRT_TRACE_MIN_BLOCKS
-#define CRT_TRACE_MIN_BLOCKS 8
+#define CRT_TRACE_MIN_BLOCKS 7
 #endif
 
 __host__ __device__ __forceinline__ SceneView scene_view(const crt_scene* s) {

@@ -5,10 +5,13 @@
 // ends the traversal (any hit).  Leaves are intersected as soon as their parent node is visited
 // (the reference's "eager" leaves); internal children are visited nearest-first by the octant
 // order fixed at build time.  Node groups (base index, hit bits, slot mask) live on a per-thread
-// stack whose first STACK_SMEM entries are in shared memory and the rest in local memory.
+// stack whose first STACK_SMEM entries are in shared memory and the rest in local memory.  The
+// triangle test is watertight (tri_test); the child-box test reads the node's planes as halves
+// (WideNode), so the ray octant picks each axis's entry / exit row by address.
 #pragma once
 
 #include "common.cuh"
+#include <cuda_fp16.h>
 
 #ifndef CRT_STACK_SMEM
 #define CRT_STACK_SMEM 8
@@ -29,21 +32,22 @@ struct TravStats {
     uint32_t nodes, tris;
 };
 
-// 32768 + (byte k of w) as an exact float: the byte lands in bits 8..15 of the mantissa of 2^15
-// (result bytes {0x00, w_k, 0x00, 0x47}).  Plane distances are then fma(32768 + b, s, a - 32768 s):
-// one PRMT and one FFMA per plane, with the node-constant offset folded into a - 32768 s.  Its
-// rounding adds at most 2^-24 (|a| + 2^15 |s|), i.e. the size of the existing rounding of a plus
-// 0.002 quantum, well inside the build's one-quantum slack on every child box.
-__device__ __forceinline__ float byte_f15(uint32_t w, int k) {
-    return __uint_as_float(__byte_perm(w, 0x47000000u, 0x7404u | ((uint32_t)k << 4)));
-}
-
 // barycentrics of a hit from tri_test's weights
 __device__ __forceinline__ THit normalized(THit h, float det) {
     const float inv = 1.0f / det;
     h.u *= inv;
     h.v *= inv;
     return h;
+}
+
+// Plane c (0..3) of half a row (4 halves 256 + q / 4) as an exact float (one half-to-float
+// conversion).  Plane distances are then fma(256 + q / 4, 4 s, a - 1024 s) with s = quantum / d: one
+// conversion and one FFMA per plane, the node-constant offset folded into a - 1024 s, whose rounding
+// adds at most 2^-24 (|a| + 2^10 |s|), well inside the build's one-quantum slack on every child box.
+__device__ __forceinline__ float half_at2(const float2 r, int c) {
+    const float w = (c >> 1) == 0 ? r.x : r.y;
+    const __half2 h = *reinterpret_cast<const __half2*>(&w);
+    return (c & 1) ? __high2float(h) : __low2float(h);
 }
 
 template <bool ANY, bool COUNT>
@@ -57,6 +61,8 @@ __device__ __forceinline__ THit traverse(const SceneView& sv, TRay ray, uint2* _
     const uint32_t oct = (__float_as_uint(ray.d.x) >> 31) | ((__float_as_uint(ray.d.y) >> 31) << 1) |
                          ((__float_as_uint(ray.d.z) >> 31) << 2);
     const float3 idir = f3(safe_rcp(ray.d.x), safe_rcp(ray.d.y), safe_rcp(ray.d.z));
+    // rows of the entry planes per axis (lo rows 2..4, hi rows 5..7; a negative direction enters at hi)
+    const int offx = (oct & 1u) ? 3 : 0, offy = (oct & 2u) ? 3 : 0, offz = (oct & 4u) ? 3 : 0;
     TShear shear = make_shear(ray.d);
     shear.ox = shear_proj(ray.o, shear.bx);
     shear.oy = shear_proj(ray.o, shear.by);
@@ -109,44 +115,42 @@ __device__ __forceinline__ THit traverse(const SceneView& sv, TRay ray, uint2* _
         }
         // ---- visit: test the 8 quantised child boxes
         const float4* np = reinterpret_cast<const float4*>(sv.nodes + node);
-        const float4 w0 = __ldg(np), w1 = __ldg(np + 1), w2 = __ldg(np + 2), w3 = __ldg(np + 3), w4 = __ldg(np + 4);
+        const float4 w0 = __ldg(np), w1 = __ldg(np + 1);
         if (COUNT) st.nodes++;
         const uint32_t ew = __float_as_uint(w0.w);
-        const float sx = __uint_as_float((uint32_t)(((int)(int8_t)(ew & 0xFF) + 127) << 23)) * idir.x;
-        const float sy = __uint_as_float((uint32_t)(((int)(int8_t)((ew >> 8) & 0xFF) + 127) << 23)) * idir.y;
-        const float sz = __uint_as_float((uint32_t)(((int)(int8_t)((ew >> 16) & 0xFF) + 127) << 23)) * idir.z;
-        const float ax = fmaf(-32768.0f, sx, (w0.x - ray.o.x) * idir.x);
-        const float ay = fmaf(-32768.0f, sy, (w0.y - ray.o.y) * idir.y);
-        const float az = fmaf(-32768.0f, sz, (w0.z - ray.o.z) * idir.z);
+        // 4 x quantum x 1/d per axis (the planes are stored as 256 + q / 4)
+        const float sx4 = __uint_as_float((uint32_t)(((int)(int8_t)(ew & 0xFF) + 129) << 23)) * idir.x;
+        const float sy4 = __uint_as_float((uint32_t)(((int)(int8_t)((ew >> 8) & 0xFF) + 129) << 23)) * idir.y;
+        const float sz4 = __uint_as_float((uint32_t)(((int)(int8_t)((ew >> 16) & 0xFF) + 129) << 23)) * idir.z;
+        const float ax = fmaf(-256.0f, sx4, (w0.x - ray.o.x) * idir.x);
+        const float ay = fmaf(-256.0f, sy4, (w0.y - ray.o.y) * idir.y);
+        const float az = fmaf(-256.0f, sz4, (w0.z - ray.o.z) * idir.z);
         const uint32_t imask = ew >> 24;
-        // entry / exit planes per axis depend on the ray octant
-        uint32_t xlo0 = __float_as_uint(w2.x), xlo1 = __float_as_uint(w2.y);
-        uint32_t ylo0 = __float_as_uint(w2.z), ylo1 = __float_as_uint(w2.w);
-        uint32_t zlo0 = __float_as_uint(w3.x), zlo1 = __float_as_uint(w3.y);
-        uint32_t xhi0 = __float_as_uint(w3.z), xhi1 = __float_as_uint(w3.w);
-        uint32_t yhi0 = __float_as_uint(w4.x), yhi1 = __float_as_uint(w4.y);
-        uint32_t zhi0 = __float_as_uint(w4.z), zhi1 = __float_as_uint(w4.w);
-        if (oct & 1u) { uint32_t t0 = xlo0, t1 = xlo1; xlo0 = xhi0; xlo1 = xhi1; xhi0 = t0; xhi1 = t1; }
-        if (oct & 2u) { uint32_t t0 = ylo0, t1 = ylo1; ylo0 = yhi0; ylo1 = yhi1; yhi0 = t0; yhi1 = t1; }
-        if (oct & 4u) { uint32_t t0 = zlo0, t1 = zlo1; zlo0 = zhi0; zlo1 = zhi1; zhi0 = t0; zhi1 = t1; }
         const uint32_t meta0 = __float_as_uint(w1.z), meta1 = __float_as_uint(w1.w);
+        // entry / exit planes per axis by the ray octant: the lo / hi rows swap by address; each half
+        // of a row (children 0-3, 4-7) is loaded when its children are tested
+        const float2* rp = reinterpret_cast<const float2*>(np);
         uint32_t hitmask = 0;
 #pragma unroll
-        for (int c = 0; c < 8; ++c) {
-            const int k = c & 3;
-            const uint32_t xl = c < 4 ? xlo0 : xlo1, xh = c < 4 ? xhi0 : xhi1;
-            const uint32_t yl = c < 4 ? ylo0 : ylo1, yh = c < 4 ? yhi0 : yhi1;
-            const uint32_t zl = c < 4 ? zlo0 : zlo1, zh = c < 4 ? zhi0 : zhi1;
-            const float tx0 = fmaf(byte_f15(xl, k), sx, ax), tx1 = fmaf(byte_f15(xh, k), sx, ax);
-            const float ty0 = fmaf(byte_f15(yl, k), sy, ay), ty1 = fmaf(byte_f15(yh, k), sy, ay);
-            const float tz0 = fmaf(byte_f15(zl, k), sz, az), tz1 = fmaf(byte_f15(zh, k), sz, az);
-            const float tmin = fmaxf(fmaxf(tx0, ty0), fmaxf(tz0, ray.tmin));
-            const float tmax = fminf(fminf(tx1, ty1), fminf(tz1, ray.tmax));
-            if (tmin <= tmax) {
-                const uint32_t meta = ((c < 4 ? meta0 : meta1) >> (8 * k)) & 0xFFu;
-                uint32_t shift = meta & 31u;
-                if ((imask >> c) & 1u) shift ^= oct;
-                hitmask |= (meta >> 5) << shift;
+        for (int hlf = 0; hlf < 2; ++hlf) {
+            const float2 xl = __ldg(rp + 2 * (2 + offx) + hlf), xh = __ldg(rp + 2 * (5 - offx) + hlf);
+            const float2 yl = __ldg(rp + 2 * (3 + offy) + hlf), yh = __ldg(rp + 2 * (6 - offy) + hlf);
+            const float2 zl = __ldg(rp + 2 * (4 + offz) + hlf), zh = __ldg(rp + 2 * (7 - offz) + hlf);
+#pragma unroll
+            for (int cc = 0; cc < 4; ++cc) {
+                const int c = 4 * hlf + cc;
+                const int k = c & 3;
+                const float tx0 = fmaf(half_at2(xl, cc), sx4, ax), tx1 = fmaf(half_at2(xh, cc), sx4, ax);
+                const float ty0 = fmaf(half_at2(yl, cc), sy4, ay), ty1 = fmaf(half_at2(yh, cc), sy4, ay);
+                const float tz0 = fmaf(half_at2(zl, cc), sz4, az), tz1 = fmaf(half_at2(zh, cc), sz4, az);
+                const float tmin = fmaxf(fmaxf(tx0, ty0), fmaxf(tz0, ray.tmin));
+                const float tmax = fminf(fminf(tx1, ty1), fminf(tz1, ray.tmax));
+                if (tmin <= tmax) {
+                    const uint32_t meta = ((c < 4 ? meta0 : meta1) >> (8 * k)) & 0xFFu;
+                    uint32_t shift = meta & 31u;
+                    if ((imask >> c) & 1u) shift ^= oct;
+                    hitmask |= (meta >> 5) << shift;
+                }
             }
         }
         ngroup = make_uint2(__float_as_uint(w1.x), (hitmask & 0xFF000000u) | imask);
