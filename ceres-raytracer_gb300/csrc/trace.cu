@@ -15,6 +15,7 @@ namespace {
 
 // ---------------------------------------------------------------- jobs
 struct RayClosestJob : JobBase {
+    static constexpr int kMinBlocks = 6;   // resident trace blocks per SM (trace_min_blocks)
     const float4* rays;   // crt_ray as 2 x float4
     crt_hit* hits;
     __device__ bool ray(uint32_t i, TRay& r, Item&) const {

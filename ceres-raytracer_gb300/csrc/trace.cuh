@@ -4,6 +4,8 @@
 #include "common.cuh"
 #include "traverse.cuh"
 
+#include <type_traits>
+
 #ifndef CRT_TRACE_BLOCK
 #define CRT_TRACE_BLOCK 128
 #endif
@@ -84,8 +86,21 @@ struct JobBase {
 // chunk == 1 one group, otherwise a guided size of up to `chunk` groups, shrinking with the work
 // left so that the last grabs stay small (few atomics on the queue counter while much work is left,
 // balance at the end).
+// Resident blocks per SM for one job type: CRT_TRACE_MIN_BLOCKS unless the job names its own
+// (kMinBlocks).  crt_trace_closest's job runs 5 % faster at 6 blocks (85 registers); the any-hit,
+// LiDAR, pass and render jobs measured the same or slower there.  launch_trace sizes the persistent
+// grid from the occupancy the kernel gets.
+template <class J, class = void>
+struct trace_min_blocks {
+    static constexpr int value = CRT_TRACE_MIN_BLOCKS;
+};
+template <class J>
+struct trace_min_blocks<J, std::void_t<decltype(J::kMinBlocks)>> {
+    static constexpr int value = J::kMinBlocks;
+};
+
 template <bool ANY, bool COUNT, class Job>
-__global__ void __launch_bounds__(CRT_TRACE_BLOCK, CRT_TRACE_MIN_BLOCKS) k_trace(SceneView sv, Job job, uint32_t n_items,
+__global__ void __launch_bounds__(CRT_TRACE_BLOCK, trace_min_blocks<Job>::value) k_trace(SceneView sv, Job job, uint32_t n_items,
                                                             const uint32_t* __restrict__ n_dev,
                                                             uint32_t* __restrict__ queue, uint32_t* __restrict__ err,
                                                             unsigned long long* __restrict__ counters, uint32_t chunk) {
