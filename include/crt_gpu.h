@@ -17,8 +17,9 @@
  *    reference and are reduced to FP32 rays once per request on the host.  Radiation-pressure sums
  *    are FP64.  The FP32 triangle test is watertight: no ray passes between two triangles that
  *    share an edge (its vertices transformed once, so they are bit-identical in both triangles).
- *  - Host outputs in page-locked memory (crt_host_alloc) are written by the kernels in place;
- *    other host outputs are staged in device memory and copied back.
+ *  - Host outputs of renders, passes, LiDAR and ray traces in page-locked memory (crt_host_alloc)
+ *    are written by the kernels in place; other host outputs are staged in device memory and
+ *    copied back.
  *  - A context (and every scene created on it) must not be used from two threads at once.
  */
 #ifndef CRT_GPU_H
