@@ -87,7 +87,7 @@ struct JobBase {
 // left so that the last grabs stay small (few atomics on the queue counter while much work is left,
 // balance at the end).
 // Resident blocks per SM for one job type: CRT_TRACE_MIN_BLOCKS unless the job names its own
-// (kMinBlocks).  crt_trace_closest's job runs 5 % faster at 6 blocks (85 registers); the any-hit,
+// (kMinBlocks).  crt_trace_closest's job runs 5 % faster at 6 blocks (80 registers); the any-hit,
 // LiDAR, pass and render jobs measured the same or slower there.  launch_trace sizes the persistent
 // grid from the occupancy the kernel gets.
 template <class J, class = void>
