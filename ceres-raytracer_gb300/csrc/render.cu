@@ -13,8 +13,10 @@
 //             k_update when the wave has at most one bounce: bounce 0's weight is the constant
 //             2 pi and its radiance starts at zero, so neither is stored)
 //   bounce    closest hit for the continuing-path queue                        (persistent trace)
-//   update    per-pixel running mean and adaptive stop, samples in order       (k_update)
-//   finalize  RGBA float and clamp(v * 256, 0, 255) bytes per request          (k_finalize)
+//   update    per-pixel running mean and adaptive stop, samples in order       (k_update; with a
+//             fixed sample count the request's last slice also stores the outputs)
+//   finalize  RGBA float and clamp(v * 256, 0, 255) bytes per request          (k_finalize; the
+//             adaptive requests)
 //
 // A wave is a list of slices, each slice = samples [s0, s0 + ns) of the pixel set of one request.
 // Path p of a slice maps to sample s0 + q / npix and pixel q % npix (q = p - slice.path_base), and
@@ -76,6 +78,7 @@ struct RReq {            // render request
     uint32_t pix_base, npix;
     uchar4* rgba;        // device outputs (staging when the caller passed host memory)
     float4* rad;
+    uint32_t fin_update; // 1: the request's last slice stores the outputs (k_update), not k_finalize
 };
 
 struct LReq {            // LiDAR beam-grid request
@@ -649,7 +652,19 @@ __global__ void k_accum(Batch B, int bounce, const uint32_t* __restrict__ q_in) 
 }
 
 // ---------------------------------------------------------------- pixel update (do_render.hpp:84-114)
-// ACC0: the wave's only bounce is bounce 0 and its light is added here instead of by k_accum
+// Final RGBA float and clamp(v * 256, 0, 255) bytes of a pixel (do_render.hpp:118-134)
+__device__ __forceinline__ void store_pixel(const RReq& R, uint32_t pixel, float4 m) {
+    const float v[4] = {m.x, m.y, m.z, 1.0f};
+    if (R.rad) R.rad[pixel] = make_float4(v[0], v[1], v[2], v[3]);
+    if (R.rgba) {
+        uint8_t qv[4];
+        for (int k = 0; k < 4; ++k) qv[k] = (uint8_t)fminf(fmaxf(v[k] * 256.0f, 0.0f), 255.0f);
+        R.rgba[pixel] = make_uchar4(qv[0], qv[1], qv[2], qv[3]);
+    }
+}
+
+// ACC0: the wave's only bounce is bounce 0 and its light is added here instead of by k_accum.
+// A request with a fixed sample count (fin_update) gets its outputs from its last slice here.
 template <bool ACC0>
 __global__ void __launch_bounds__(256, 5) k_update(Batch B) {
     const WaveDesc& w = *B.cur;
@@ -699,6 +714,7 @@ __global__ void __launch_bounds__(256, 5) k_update(Batch B) {
         }
         B.pix[g] = m;
         B.taken[g] = t;
+        if (R.fin_update && S.s0 + S.ns == (uint32_t)R.c.max_samples) store_pixel(R, pixel, m);
     }
 }
 
@@ -722,31 +738,16 @@ __global__ void k_finalize(Batch B, uint32_t n_req, uint32_t n_total) {
             else hi = mid;
         }
         const RReq& R = B.rr[lo];
-        const uint32_t pixel = g - R.pix_base;
-        const float4 m = B.pix[g];
-        const float v[4] = {m.x, m.y, m.z, 1.0f};
-        if (R.rad) R.rad[pixel] = make_float4(v[0], v[1], v[2], v[3]);
-        if (R.rgba) {
-            uint8_t qv[4];
-            for (int k = 0; k < 4; ++k) qv[k] = (uint8_t)fminf(fmaxf(v[k] * 256.0f, 0.0f), 255.0f);
-            R.rgba[pixel] = make_uchar4(qv[0], qv[1], qv[2], qv[3]);
-        }
+        if (R.fin_update) continue;   // stored by its last update
+        store_pixel(R, g - R.pix_base, B.pix[g]);
     }
 }
 
 // finalize of one request (the serving engine completes requests one by one)
 __global__ void k_finalize_one(Batch B, uint32_t slot) {
     const RReq& R = B.rr[slot];
-    for (uint32_t pixel = blockIdx.x * blockDim.x + threadIdx.x; pixel < R.npix; pixel += gridDim.x * blockDim.x) {
-        const float4 m = B.pix[(size_t)R.pix_base + pixel];
-        const float v[4] = {m.x, m.y, m.z, 1.0f};
-        if (R.rad) R.rad[pixel] = make_float4(v[0], v[1], v[2], v[3]);
-        if (R.rgba) {
-            uint8_t qv[4];
-            for (int k = 0; k < 4; ++k) qv[k] = (uint8_t)fminf(fmaxf(v[k] * 256.0f, 0.0f), 255.0f);
-            R.rgba[pixel] = make_uchar4(qv[0], qv[1], qv[2], qv[3]);
-        }
-    }
+    for (uint32_t pixel = blockIdx.x * blockDim.x + threadIdx.x; pixel < R.npix; pixel += gridDim.x * blockDim.x)
+        store_pixel(R, pixel, B.pix[(size_t)R.pix_base + pixel]);
 }
 
 __global__ void k_tan_table2(double* __restrict__ out, uint32_t nx, uint32_t ny, double hx, double hy) {
@@ -869,9 +870,10 @@ void check_request(const crt_request& q) {
     }
 }
 
-// Outputs the kernels write in place: device memory, or mapped page-locked host memory (k_finalize and
-// the LiDAR trace store each value once, so the stores cross the host link while the kernels run and
-// no copy follows); other host memory is staged in device scratch and copied back.
+// Outputs the kernels write in place: device memory, or mapped page-locked host memory (the last
+// update or k_finalize and the LiDAR trace store each value once, so the stores cross the host link
+// while the kernels run and no copy follows); other host memory is staged in device scratch and
+// copied back.
 bool direct_out(const void* p) { return is_device_ptr(p) || is_host_mapped(p); }
 
 // srps: SRP requests of a mixed batch (crt_batch_mixed); their sun rays ride in the waves' primary
@@ -941,6 +943,9 @@ void run_batch(crt_context* ctx, const crt_request* reqs, size_t n, crt_batch_st
             h.active = nullptr;
             h.act_sel = 0;
             h.rr_index = (uint32_t)rr.size();
+            // a fixed sample count: every pixel's last sample is in the request's last slice, whose
+            // update stores the outputs
+            R.fin_update = !h.adaptive && h.total > 0 ? 1u : 0u;
             hreq.push_back(h);
             rr.push_back(R);
         } else {
@@ -1313,8 +1318,10 @@ void run_batch(crt_context* ctx, const crt_request* reqs, size_t n, crt_batch_st
         }
     }
 
-    // ---- finalize and copy host outputs
-    if (pix_total) {
+    // ---- finalize (requests whose last update did not store their outputs) and copy host outputs
+    bool any_finalize = false;
+    for (const RReq& R : rr) any_finalize = any_finalize || !R.fin_update;
+    if (pix_total && any_finalize) {
         k_finalize<<<grid_for(ctx, k_finalize, pix_total), 256, 0, st>>>(B, (uint32_t)rr.size(), pix_total);
         check_launch(ctx, "k_finalize");
     }
